@@ -1,0 +1,342 @@
+#!/usr/bin/env python3
+"""Benchmark: pair-tests/s of the all-pairs Boolean epistasis scan.
+
+One step = one whole scan of the workload (every SNP pair s > t, all 4 allele-
+row pairs x 5 Boolean functions, plus the same-SNP row pairs), ranked top-k on
+the device, top-k back on the host.  The default workload is the metric's
+configuration: 100,000 SNPs x 10,000 samples (5,000 cases / 5,000 controls),
+HWE genotypes with MAF ~ U(0.01, 0.5), 1% missing, 10 planted pairs, top-10,000
+-- seeded synthetic data from the package's generator.
+
+  value : pair-tests/s with the genotype planes resident in HBM (CUDA events
+          on the library stream around each scan).
+  e2e   : the same metric through the public C ABI from a pinned host .bed
+          image: H2D copy + device decode + scan + top-k D2H every step.
+
+`--impl reference` times the reference's CPU gold loop (the oracle's
+restatement of proc_gold_1.h:98-134, all host threads) on a bounded leading
+sub-triangle of the same workload.  Under torchrun every rank scans its own
+cohort (weak scaling: seed + rank, no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+CONFIGS = {
+    "cfg1": dict(n_snps=1024, n_cases=256, n_controls=256, maf_lo=0.05, maf_hi=0.5, missing=0.02,
+                 n_planted=0, seed=1001, k=100),
+    "cfg2": dict(n_snps=20000, n_cases=2000, n_controls=2000, maf_lo=0.01, maf_hi=0.5,
+                 missing=0.01, n_planted=3, seed=1002, k=1000),
+    "cfg3": dict(n_snps=100000, n_cases=5000, n_controls=5000, maf_lo=0.01, maf_hi=0.5,
+                 missing=0.01, n_planted=10, seed=1003, k=10000),
+}
+METRIC = "pair-tests/sec at 100k SNP x 10k samples"
+UNIT = "pair-tests/s"
+
+
+def describe(name: str, c: dict) -> str:
+    s = c["n_cases"] + c["n_controls"]
+    return (f"{name}: {c['n_snps']:,} SNPs x {s:,} samples ({c['n_cases']:,} cases / "
+            f"{c['n_controls']:,} controls), MAF U({c['maf_lo']}, {c['maf_hi']}), "
+            f"{c['missing']:.0%} missing, {c['n_planted']} planted pairs, top-{c['k']:,}")
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def cpu_baseline(cfg: dict, bed, ph, target_s: float, threads: int):
+    """Time the reference gold loop (oracle restatement) on a leading
+    sub-triangle sized to about target_s seconds."""
+    sys.path.insert(0, os.path.join(HERE, "tests"))
+    import numpy as np
+
+    import helpers as H
+
+    fs = H.Fileset(bed=bed, pheno=ph, n_lines=cfg["n_snps"], bim=[])
+    # Decode only the leading rows we need.
+    lib = H.oracle()
+    nw = (ph.size + 63) // 64
+    probe_rows = 256
+    n_lines = min(cfg["n_snps"], 20000)
+    sub = H.Fileset(bed=bed[: 3 + n_lines * ((ph.size + 3) // 4)], pheno=ph, n_lines=n_lines, bim=[])
+    bits, valid, m1, m2 = H.decode_rows(sub)
+    chk = H.ctypes.c_double()
+    t0 = time.perf_counter()
+    lib.orc_gold_loop(H.ptr(bits), H.ptr(valid), H.ptr(m1), H.ptr(m2), nw, 0, probe_rows, threads,
+                      H.ctypes.byref(chk))
+    dt = max(time.perf_counter() - t0, 1e-6)
+    per_pair = dt / (probe_rows * (probe_rows + 1) / 2)
+    want_pairs = target_s / per_pair
+    r1 = int(min(2 * n_lines, max(probe_rows, (2 * want_pairs) ** 0.5)))
+    t0 = time.perf_counter()
+    row_pairs = lib.orc_gold_loop(H.ptr(bits), H.ptr(valid), H.ptr(m1), H.ptr(m2), nw, 0, r1,
+                                  threads, H.ctypes.byref(chk))
+    dt = time.perf_counter() - t0
+    snp_pairs = row_pairs / 4.0
+    return dict(value=snp_pairs / dt, unit=UNIT, seconds=dt, rows=r1,
+                sample=(f"allele rows 0..{r1 - 1} against every row <= them (leading "
+                        f"sub-triangle, {row_pairs:,} row pairs = {snp_pairs:,.0f} SNP-pair "
+                        f"equivalents) of the same workload, 5 functions, float entropy"))
+
+
+def run_reference(args, cfg):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import numpy as np
+
+    import gepicount_gb300 as g
+
+    g.lib()
+    spec = g.SynthSpec(**{k: v for k, v in cfg.items() if k != "k"})
+    bed, ph, _ = g.synth_bed(spec)
+    threads = os.cpu_count() or 1
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(cfg, bed, ph, target_s=args.ref_seconds, threads=threads)
+        if i >= args.warmup:
+            vals.append(r)
+    value = statistics.median(v["value"] for v in vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * statistics.median(v["seconds"] for v in vals),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+        "data": "synthetic", "config": {"workload": describe(args.config, cfg)},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": vals[-1]["sample"]},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, cfg):
+    import numpy as np
+    import torch
+
+    import gepicount_gb300 as g
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    g.lib()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    kw = {k: v for k, v in cfg.items() if k != "k"}
+    kw["seed"] = cfg["seed"] + 7919 * rank
+    spec = g.SynthSpec(**kw)
+    nbytes = g.lib().gepi_synth_bed_bytes(g.ctypes.byref(spec._c()))
+    pinned = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    bed = pinned.numpy()
+    _, ph, _ = g.synth_bed(spec, out=bed)
+    k = cfg["k"]
+    method = {"auto": g.METHOD_AUTO, "popc": g.METHOD_POPC, "tensor": g.METHOD_TENSOR}[args.method]
+
+    planes = g.Planes.from_bed(bed, spec.n_snps, ph, device=local)
+    for _ in range(args.warmup):
+        planes.scan(k, method=method)
+    barrier()
+    stats = []
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            tops = planes.scan(k, method=method)
+            stats.append(planes.last_stats())
+        barrier()
+        wall = time.perf_counter() - t0
+    dev_ms = sum(s["scan_ms"] for s in stats)
+    pairs_per_scan = stats[0]["snp_pairs"]
+    # max over ranks of the device time
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([dev_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_ms = float(t.item())
+    value = world * pairs_per_scan * args.steps / (dev_ms / 1000.0)
+    launches = sum(s["count_launches"] + s["other_launches"] for s in stats)
+
+    # Roofline of the dominant kernel (the counting kernel): algorithmic work
+    # = 9 bit-products per sample per SNP pair (3x3 plane Gram), counted as
+    # 2 ops per 0/1 multiply-accumulate; peak = dense bf16 tensor rate.
+    n_samples = spec.n_cases + spec.n_controls
+    pairs_total = pairs_per_scan + stats[0]["diag_snps"]
+    count_ms = sum(s["count_ms"] for s in stats)
+    nlaunch = sum(s["count_launches"] for s in stats)
+    avg_launch_s = count_ms / 1000.0 / max(1, nlaunch)
+    ops_per_launch = 2.0 * 9.0 * n_samples * pairs_total / max(1, stats[0]["count_launches"])
+    peaks, peak_kind = measured_peaks()
+    achieved = ops_per_launch / avg_launch_s / 1e12
+    peak = float(peaks.get("bf16_tflops", 1900.0))
+    roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "traffic": None, "kernel": "popc_tile_kernel",
+            "peak_source": f"{peak_kind} dense bf16 (burst)",
+            "work": "2 x 9 x samples ops per SNP pair (0/1 Gram), per launch",
+            "avg_launch_ms": avg_launch_s * 1e3, "launches": nlaunch}
+
+    # End-to-end through the C ABI from pinned host memory.
+    planes.close()
+    e2e_times = []
+    d2h = k * 48
+    for i in range(max(1, min(args.steps, 3))):
+        barrier()
+        t1 = time.perf_counter()
+        with g.Planes.from_bed(bed, spec.n_snps, ph, device=local) as pl:
+            pl.scan(k, method=method)
+        torch.cuda.synchronize()
+        e2e_times.append(time.perf_counter() - t1)
+    e2e_t = max(e2e_times) if world == 1 else max(e2e_times)
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([e2e_t], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_t = float(t.item())
+    e2e_value = world * pairs_per_scan / e2e_t
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        r = cpu_baseline(cfg, bed, ph, target_s=args.cpu_seconds, threads=1)
+        cpu = {"value": r["value"], "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": r["sample"]}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (seeded generator, HWE, planted pairs)",
+            "config": {"workload": describe(args.config, cfg), "n_snps": spec.n_snps,
+                       "n_samples": n_samples, "k": k, "method": args.method,
+                       "pair_tests_per_step": pairs_per_scan,
+                       "boolean_tests_per_step": 5 * (2 * spec.n_snps) * (2 * spec.n_snps + 1) // 2,
+                       "l2": "inputs larger than L2 (genotype planes "
+                             f"{3 * spec.n_snps * ((n_samples + 255) // 256) * 32 / 1e6:.0f} MB)"},
+            "clocks": clk.summary(),
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(nbytes),
+                    "d2h_bytes_per_step": int(d2h), "seconds_per_step": e2e_t},
+            "gpu_launches": launches,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "wall_s": wall,
+            "scan_stats": {k_: v for k_, v in stats[-1].items()},
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", choices=sorted(CONFIGS), default="cfg3")
+    ap.add_argument("--method", choices=["auto", "popc", "tensor"], default="auto")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    cfg = CONFIGS[args.config]
+    if args.impl == "reference":
+        return run_reference(args, cfg)
+    return run_ours(args, cfg)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

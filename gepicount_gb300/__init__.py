@@ -1,0 +1,420 @@
+"""gepicount_gb300 -- GB300-native pairwise Boolean epistasis scan.
+
+Python host mirror of gEpiCount's interface over the C ABI in include/gepi.h
+(libgepi.so, built by ``python -m gepicount_gb300.build``):
+
+* ``BinPlinkReader(base)`` -- the reader (src/reader/BinPlinkReader.h): parses
+  BASE.fam/.bim/.bed with the reference's semantics.
+* ``Params`` -- struct _paramP1 (inc/gEpiCount.h:116-132).
+* ``process_gpu_1(reader, tops, par)`` -- the reference's GPU entry point
+  (src/kernels/kernel1.cu:508-511): fills ``tops`` (a RESULT_DTYPE array of
+  length par.topmost, the InteractionResult layout) ascending by objective.
+* ``Planes`` -- device-resident genotype bit-planes, decoded on the GPU from a
+  .bed image; ``Planes.scan`` / ``scan_range`` / ``pair_counts``.
+
+There is no CPU fallback: every compute call goes through the CUDA library and
+raises ``GepiError`` if it is missing or fails.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+__all__ = [
+    "GepiError", "RESULT_DTYPE", "FUNC_NAMES", "Params", "BinPlinkReader", "Planes",
+    "process_gpu_1", "fisher_pval", "fisher_log10p", "SynthSpec", "synth_bed", "synth_write",
+    "library_path", "lib",
+]
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_PKG, "_build", "libgepi.so")
+
+RESULT_DTYPE = np.dtype(
+    [("sA", "<i4"), ("sB", "<i4"), ("_pad0", "<i4", (2,)), ("n", "<i4", (4,)), ("ent", "<f4"),
+     ("fun", "i1"), ("_pad1", "i1", (11,))]
+)
+assert RESULT_DTYPE.itemsize == 48
+
+FUNC_NAMES = ["AND", "NAND", "ANDN", "NANDN", "XOR"]
+ENTROPY, FISHER = 0, 1
+METHOD_AUTO, METHOD_POPC, METHOD_TENSOR = 0, 1, 2
+
+_STATUS = {
+    0: "ok", 1: "invalid argument", 2: "i/o error", 3: "format error", 4: "CUDA error",
+    5: "out of device memory", 6: "phenotype class 1 or 2 is empty", 7: "device wait timed out",
+    8: "unsupported", 9: "request beyond a documented limit",
+}
+
+
+class GepiError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{_STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [("gpu_num", ctypes.c_int32), ("topmost", ctypes.c_int32),
+                ("objective", ctypes.c_int32), ("method", ctypes.c_int32),
+                ("verbose", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7)]
+
+
+class _SynthSpec(ctypes.Structure):
+    _fields_ = [("n_snps", ctypes.c_int32), ("n_cases", ctypes.c_int32),
+                ("n_controls", ctypes.c_int32), ("maf_lo", ctypes.c_double),
+                ("maf_hi", ctypes.c_double), ("missing", ctypes.c_double),
+                ("n_planted", ctypes.c_int32), ("odds_ratio", ctypes.c_double),
+                ("seed", ctypes.c_uint64)]
+
+
+class _ScanStats(ctypes.Structure):
+    _fields_ = [("scan_ms", ctypes.c_double), ("count_ms", ctypes.c_double),
+                ("max_count_ms", ctypes.c_double), ("count_launches", ctypes.c_int32),
+                ("other_launches", ctypes.c_int32), ("batches", ctypes.c_int32),
+                ("overflows", ctypes.c_int32), ("snp_pairs", ctypes.c_uint64),
+                ("diag_snps", ctypes.c_uint64), ("tiles", ctypes.c_uint64),
+                ("candidates", ctypes.c_uint64), ("method", ctypes.c_int32),
+                ("tile_snps", ctypes.c_int32)]
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _LIB_PATH
+
+
+def lib():
+    """The loaded libgepi.so (raises GepiError if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIB_PATH):
+        raise GepiError(8, f"native library missing: {_LIB_PATH} "
+                           "(run python -m gepicount_gb300.build)")
+    L = ctypes.CDLL(_LIB_PATH)
+    P, i32, u64, sz = ctypes.c_void_p, ctypes.c_int, ctypes.c_uint64, ctypes.c_size_t
+    PP = ctypes.POINTER(ctypes.c_void_p)
+    L.gepi_status_string.restype = ctypes.c_char_p
+    L.gepi_status_string.argtypes = [i32]
+    L.gepi_last_error.restype = ctypes.c_char_p
+    L.gepi_abi_version.restype = i32
+    L.gepi_plink_open.argtypes = [ctypes.c_char_p, PP]
+    L.gepi_plink_close.argtypes = [P]
+    for f in ("gepi_plink_num_rows", "gepi_plink_num_samples", "gepi_plink_elements_snp"):
+        getattr(L, f).argtypes = [P]
+        getattr(L, f).restype = i32
+    L.gepi_plink_bed.argtypes = [P, ctypes.POINTER(sz)]
+    L.gepi_plink_bed.restype = P
+    L.gepi_plink_phenotypes.argtypes = [P]
+    L.gepi_plink_phenotypes.restype = P
+    L.gepi_plink_row_info.argtypes = [P, i32, ctypes.POINTER(ctypes.c_char_p),
+                                      ctypes.POINTER(ctypes.c_char), ctypes.POINTER(i32),
+                                      ctypes.POINTER(i32)]
+    L.gepi_plink_decode_rows.argtypes = [P, P, P, P, P]
+    L.gepi_planes_from_bed.argtypes = [P, sz, i32, i32, P, i32, PP]
+    L.gepi_planes_from_rows.argtypes = [P, P, i32, i32, P, P, i32, PP]
+    L.gepi_planes_destroy.argtypes = [P]
+    L.gepi_planes_destroy.restype = None
+    L.gepi_planes_num_snps.argtypes = [P]
+    L.gepi_planes_num_snps.restype = i32
+    L.gepi_planes_class_sizes.argtypes = [P, ctypes.POINTER(i32), ctypes.POINTER(i32)]
+    L.gepi_scan.argtypes = [P, ctypes.POINTER(_Params), P, i32]
+    L.gepi_scan_range.argtypes = [P, ctypes.POINTER(_Params), i32, i32, i32, i32, P, i32]
+    L.gepi_pair_counts.argtypes = [P, i32, i32, i32, i32, i32, P]
+    L.gepi_process_gpu_1.argtypes = [P, P, i32, i32, P, P, P, ctypes.POINTER(_Params)]
+    L.gepi_last_scan_stats.argtypes = [P, ctypes.POINTER(_ScanStats)]
+    L.gepi_fisher_pval.argtypes = [i32, i32, i32, i32]
+    L.gepi_fisher_pval.restype = ctypes.c_float
+    L.gepi_fisher_log10p.argtypes = [i32, i32, i32, i32]
+    L.gepi_fisher_log10p.restype = ctypes.c_double
+    L.gepi_synth_bed_bytes.argtypes = [ctypes.POINTER(_SynthSpec)]
+    L.gepi_synth_bed_bytes.restype = sz
+    L.gepi_synth_bed.argtypes = [ctypes.POINTER(_SynthSpec), P, P, P]
+    L.gepi_synth_write.argtypes = [ctypes.POINTER(_SynthSpec), ctypes.c_char_p]
+    for f in ("gepi_plink_open", "gepi_plink_row_info", "gepi_plink_decode_rows",
+              "gepi_planes_from_bed", "gepi_planes_from_rows", "gepi_planes_class_sizes",
+              "gepi_scan", "gepi_scan_range", "gepi_pair_counts", "gepi_process_gpu_1",
+              "gepi_last_scan_stats",
+              "gepi_synth_bed", "gepi_synth_write"):
+        getattr(L, f).restype = i32
+    _lib = L
+    return L
+
+
+def _check(status: int):
+    if status != 0:
+        msg = lib().gepi_last_error().decode(errors="replace")
+        raise GepiError(status, msg)
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+# ---- parameters (struct _paramP1) ------------------------------------------
+@dataclass
+class Params:
+    """struct _paramP1 (inc/gEpiCount.h:116-132) plus the counting method."""
+
+    gpuNum: int = 0
+    topmost: int = 1000000
+    gold: bool = False
+    shmem: bool = False
+    alt: bool = False
+    intermediate: bool = False
+    name: str = ""
+    blkSzX: int = 16
+    blkSzY: int = 16
+    maxGridBlocks: int = 16
+    ffun: int = ENTROPY
+    qaMissSNPs: float = 0.05
+    qaMissSamp: float = 0.05
+    qaRemoveMissing: bool = False
+    method: int = METHOD_AUTO
+    verbose: int = 0
+
+    def _c(self) -> _Params:
+        p = _Params()
+        p.gpu_num = self.gpuNum
+        p.topmost = self.topmost
+        p.objective = self.ffun
+        p.method = self.method
+        p.verbose = self.verbose
+        return p
+
+
+# ---- reader ----------------------------------------------------------------
+class BinPlinkReader:
+    """Host PLINK reader with BinPlinkReader/PlinkReader semantics."""
+
+    ELEMENT_SIZE = 8
+
+    def __init__(self, base: str):
+        self.basepath = base
+        self._h = ctypes.c_void_p()
+        self._bits = self._valid = self._m1 = self._m2 = None
+
+    def checkConsistency(self) -> bool:
+        if self._h:
+            return True
+        st = lib().gepi_plink_open(self.basepath.encode(), ctypes.byref(self._h))
+        if st != 0:
+            self._h = ctypes.c_void_p()
+            self.error = lib().gepi_last_error().decode(errors="replace")
+            return False
+        return True
+
+    def readData(self) -> bool:
+        if not self.checkConsistency():
+            return False
+        nr, nw = self.numSNPs(), self.elementsSNP()
+        self._bits = np.zeros((nr, nw), dtype=np.uint64)
+        self._valid = np.zeros((nr, nw), dtype=np.uint64)
+        self._m1 = np.zeros(nw, dtype=np.uint64)
+        self._m2 = np.zeros(nw, dtype=np.uint64)
+        _check(lib().gepi_plink_decode_rows(self._h, _ptr(self._bits), _ptr(self._valid),
+                                            _ptr(self._m1), _ptr(self._m2)))
+        return True
+
+    def numSNPs(self) -> int:
+        return lib().gepi_plink_num_rows(self._h)
+
+    def numSamples(self) -> int:
+        return lib().gepi_plink_num_samples(self._h)
+
+    def elementsSNP(self) -> int:
+        return lib().gepi_plink_elements_snp(self._h)
+
+    def DataSize(self) -> int:
+        return self.ELEMENT_SIZE * self.elementsSNP() * self.numSNPs()
+
+    def BitData(self) -> np.ndarray:
+        return self._bits
+
+    def ValidData(self) -> np.ndarray:
+        return self._valid
+
+    def classMask(self, key: int) -> np.ndarray | None:
+        return {1: self._m1, 2: self._m2}.get(key)
+
+    def bed(self) -> np.ndarray:
+        n = ctypes.c_size_t()
+        p = lib().gepi_plink_bed(self._h, ctypes.byref(n))
+        return np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_uint8)),
+                                     shape=(n.value,))
+
+    def phenotypes(self) -> np.ndarray:
+        p = lib().gepi_plink_phenotypes(self._h)
+        return np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_int32)),
+                                     shape=(self.numSamples(),)).copy()
+
+    def getSnp(self, row: int):
+        """(id, allele, chr, pos) of allele row `row`."""
+        sid, al = ctypes.c_char_p(), ctypes.c_char()
+        ch, pos = ctypes.c_int(), ctypes.c_int()
+        _check(lib().gepi_plink_row_info(self._h, row, ctypes.byref(sid), ctypes.byref(al),
+                                         ctypes.byref(ch), ctypes.byref(pos)))
+        return sid.value.decode(), al.value.decode(), ch.value, pos.value
+
+    def close(self):
+        if self._h:
+            lib().gepi_plink_close(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---- device planes ------------------------------------------------------------
+class Planes:
+    """Device-resident class-sorted genotype bit-planes of one cohort."""
+
+    def __init__(self, handle: ctypes.c_void_p, device: int):
+        self._h = handle
+        self.device = device
+
+    @classmethod
+    def from_bed(cls, bed: np.ndarray, n_bim_snps: int, phenotype: np.ndarray,
+                 device: int = 0) -> "Planes":
+        bed = np.ascontiguousarray(bed, dtype=np.uint8)
+        ph = np.ascontiguousarray(phenotype, dtype=np.int32)
+        h = ctypes.c_void_p()
+        _check(lib().gepi_planes_from_bed(_ptr(bed), bed.size, n_bim_snps, ph.size, _ptr(ph),
+                                          device, ctypes.byref(h)))
+        return cls(h, device)
+
+    @classmethod
+    def from_rows(cls, bits: np.ndarray, valid: np.ndarray, mask1: np.ndarray,
+                  mask2: np.ndarray, device: int = 0) -> "Planes":
+        bits = np.ascontiguousarray(bits, dtype=np.uint64)
+        valid = np.ascontiguousarray(valid, dtype=np.uint64)
+        m1 = np.ascontiguousarray(mask1, dtype=np.uint64)
+        m2 = np.ascontiguousarray(mask2, dtype=np.uint64)
+        h = ctypes.c_void_p()
+        _check(lib().gepi_planes_from_rows(_ptr(bits), _ptr(valid), bits.shape[0], bits.shape[1],
+                                           _ptr(m1), _ptr(m2), device, ctypes.byref(h)))
+        return cls(h, device)
+
+    @property
+    def n_snps(self) -> int:
+        return lib().gepi_planes_num_snps(self._h)
+
+    def class_sizes(self):
+        a, b = ctypes.c_int(), ctypes.c_int()
+        _check(lib().gepi_planes_class_sizes(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def scan(self, k: int, objective: int = ENTROPY, method: int = METHOD_AUTO,
+             verbose: int = 0) -> np.ndarray:
+        par = Params(topmost=k, ffun=objective, method=method, verbose=verbose, gpuNum=self.device)
+        tops = np.zeros(k, dtype=RESULT_DTYPE)
+        _check(lib().gepi_scan(self._h, ctypes.byref(par._c()), _ptr(tops), k))
+        return tops
+
+    def scan_range(self, a0: int, na: int, b0: int, nb: int, k: int, objective: int = ENTROPY,
+                   method: int = METHOD_AUTO) -> np.ndarray:
+        par = Params(topmost=k, ffun=objective, method=method, gpuNum=self.device)
+        tops = np.zeros(k, dtype=RESULT_DTYPE)
+        _check(lib().gepi_scan_range(self._h, ctypes.byref(par._c()), a0, na, b0, nb,
+                                     _ptr(tops), k))
+        return tops
+
+    def pair_counts(self, a0: int, na: int, b0: int, nb: int,
+                    method: int = METHOD_POPC) -> np.ndarray:
+        out = np.zeros((na, nb, 18), dtype=np.uint32)
+        _check(lib().gepi_pair_counts(self._h, method, a0, na, b0, nb, _ptr(out)))
+        return out
+
+    def last_stats(self) -> dict:
+        """Device timings and counters of the last scan on these planes."""
+        st = _ScanStats()
+        _check(lib().gepi_last_scan_stats(self._h, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in _ScanStats._fields_}
+
+    def close(self):
+        if self._h:
+            lib().gepi_planes_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def process_gpu_1(pr: BinPlinkReader, tops: np.ndarray, par: Params) -> None:
+    """Drop-in for process_gpu_1 (kernel1.cu:508-511): fills tops[:par.topmost]."""
+    if tops.dtype != RESULT_DTYPE or tops.size < par.topmost:
+        raise GepiError(1, "tops must be a RESULT_DTYPE array of length >= topmost")
+    bits, valid = pr.BitData(), pr.ValidData()
+    m1, m2 = pr.classMask(1), pr.classMask(2)
+    if bits is None or m1 is None or m2 is None:
+        raise GepiError(1, "reader has no data (call readData first)")
+    _check(lib().gepi_process_gpu_1(_ptr(bits), _ptr(valid), bits.shape[0], bits.shape[1],
+                                    _ptr(m1), _ptr(m2), _ptr(tops), ctypes.byref(par._c())))
+
+
+def fisher_pval(n11: int, n12: int, n21: int, n22: int) -> float:
+    """fisher_pval (src/misc/fisher_p.c:52-76): float log10 of the two-sided p."""
+    return float(lib().gepi_fisher_pval(n11, n12, n21, n22))
+
+
+def fisher_log10p(n11: int, n12: int, n21: int, n22: int) -> float:
+    return float(lib().gepi_fisher_log10p(n11, n12, n21, n22))
+
+
+# ---- seeded synthetic PLINK data --------------------------------------------
+@dataclass
+class SynthSpec:
+    n_snps: int
+    n_cases: int
+    n_controls: int
+    maf_lo: float = 0.05
+    maf_hi: float = 0.5
+    missing: float = 0.02
+    n_planted: int = 0
+    odds_ratio: float = 2.0
+    seed: int = 1000
+
+    def _c(self) -> _SynthSpec:
+        s = _SynthSpec()
+        for f in ("n_snps", "n_cases", "n_controls", "maf_lo", "maf_hi", "missing", "n_planted",
+                  "odds_ratio", "seed"):
+            setattr(s, f, getattr(self, f))
+        return s
+
+    @property
+    def n_samples(self) -> int:
+        return self.n_cases + self.n_controls
+
+
+def synth_bed(spec: SynthSpec, out: np.ndarray | None = None):
+    """-> (bed image uint8, phenotype int32, planted SNP pairs int32[n_planted, 2])."""
+    c = spec._c()
+    nb = lib().gepi_synth_bed_bytes(ctypes.byref(c))
+    if nb == 0:
+        raise GepiError(1, "bad synthetic spec")
+    bed = out if out is not None else np.empty(nb, dtype=np.uint8)
+    if bed.size != nb or bed.dtype != np.uint8:
+        raise GepiError(1, "output buffer has the wrong size")
+    ph = np.empty(spec.n_samples, dtype=np.int32)
+    pl = np.empty(max(1, 2 * spec.n_planted), dtype=np.int32)
+    _check(lib().gepi_synth_bed(ctypes.byref(c), _ptr(bed), _ptr(ph), _ptr(pl)))
+    return bed, ph, pl[: 2 * spec.n_planted].reshape(-1, 2)
+
+
+def synth_write(spec: SynthSpec, base: str) -> None:
+    _check(lib().gepi_synth_write(ctypes.byref(spec._c()), base.encode()))

@@ -1,0 +1,150 @@
+// Genotype loader kernels: PLINK .bed (2-bit calls) or the reference reader's
+// row-major bit planes -> class-sorted device bit-planes (layout in device.cuh).
+//
+// Semantics follow BinPlinkReader::readData (src/reader/BinPlinkReader.h:
+// 160-211): code 00 -> column-5 allele row, 10 -> both rows, 11 -> column-6
+// allele row, 01 -> missing; valid = not missing.  Samples are gathered through
+// a permutation `perm` (output sample slot -> input sample index, -1 = pad), so
+// class 0 (phenotype 1) comes first, then class 1 (phenotype 2), each padded to
+// a multiple of 128 samples; samples of any other phenotype are dropped.
+//
+// HBM-bound: reads N * ceil(S/4) bytes, writes 3 * N * Wp * 4 bytes.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "device.cuh"
+
+namespace gepi {
+
+// One CTA decodes `spc` consecutive SNPs whose .bed rows are staged in shared
+// memory.  Each warp produces 32 consecutive output words of one SNP at a time:
+// iteration j ballots the three plane bits of slot (w0 + j)*32 + lane; lane j
+// keeps word j, then the warp stores 32 words per plane, coalesced.
+__global__ void decode_bed_kernel(const uint8_t *__restrict__ bed, size_t bps, int n_snps,
+                                  const int32_t *__restrict__ perm, int Wp, int spc,
+                                  uint32_t *__restrict__ planes) {
+    extern __shared__ uint8_t srow[];
+    const int s0 = blockIdx.x * spc;
+    const int ns = min(spc, n_snps - s0);
+    const size_t tot = (size_t)ns * bps;
+    const uint8_t *src = bed + (size_t)s0 * bps;
+    for (size_t i = threadIdx.x; i < tot; i += blockDim.x) srow[i] = __ldg(src + i);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const int nchunks = (Wp + 31) / 32;
+    for (int job = warp; job < nchunks * ns; job += nwarp) {
+        const int si = job / nchunks, ch = job - si * nchunks;
+        const int w0 = ch * 32;
+        const uint8_t *row = srow + (size_t)si * bps;
+        uint32_t myA = 0, mya = 0, myV = 0;
+        for (int j = 0; j < 32; ++j) {
+            const int w = w0 + j;
+            if (w >= Wp) break;  // uniform across the warp
+            const int sample = __ldg(perm + (size_t)w * 32 + lane);
+            int code = 1;
+            if (sample >= 0) code = (row[sample >> 2] >> ((sample & 3) * 2)) & 3;
+            const uint32_t A = __ballot_sync(0xffffffffu, code == 0 || code == 2);
+            const uint32_t a = __ballot_sync(0xffffffffu, code >= 2);
+            const uint32_t V = __ballot_sync(0xffffffffu, code != 1);
+            if (lane == j) {
+                myA = A;
+                mya = a;
+                myV = V;
+            }
+        }
+        const int w = w0 + lane;
+        if (w < Wp) {
+            uint32_t *out = planes + (size_t)(s0 + si) * 3 * Wp + w;
+            out[0] = myA;
+            out[(size_t)Wp] = mya;
+            out[2 * (size_t)Wp] = myV;
+        }
+    }
+}
+
+// Same, from the reference reader's host rows (uploaded): bits/valid are
+// rows x nw uint64 with sample j at bit j%64 of word j/64; allele rows 2s and
+// 2s+1 share the valid row.  Bits are masked with valid, as every count of the
+// reference is (proc_gold_1.h:106-112).
+__global__ void decode_rows_kernel(const uint64_t *__restrict__ bits,
+                                   const uint64_t *__restrict__ valid, int nw, int n_snps,
+                                   const int32_t *__restrict__ perm, int Wp,
+                                   uint32_t *__restrict__ planes) {
+    const int lane = threadIdx.x & 31;
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarp = (gridDim.x * blockDim.x) >> 5;
+    const int nchunks = (Wp + 31) / 32;
+    for (long long job = gwarp; job < (long long)nchunks * n_snps; job += nwarp) {
+        const int s = (int)(job / nchunks), ch = (int)(job - (long long)s * nchunks);
+        const int w0 = ch * 32;
+        const uint64_t *bA = bits + (size_t)(2 * s) * nw, *ba = bA + nw;
+        const uint64_t *vv = valid + (size_t)(2 * s) * nw;
+        uint32_t myA = 0, mya = 0, myV = 0;
+        for (int j = 0; j < 32; ++j) {
+            const int w = w0 + j;
+            if (w >= Wp) break;
+            const int sample = __ldg(perm + (size_t)w * 32 + lane);
+            bool A = false, a = false, V = false;
+            if (sample >= 0) {
+                const int k = sample >> 6;
+                const uint64_t bit = 1ull << (sample & 63);
+                V = (__ldg(vv + k) & bit) != 0;
+                A = V && (__ldg(bA + k) & bit) != 0;
+                a = V && (__ldg(ba + k) & bit) != 0;
+            }
+            const uint32_t bAw = __ballot_sync(0xffffffffu, A);
+            const uint32_t baw = __ballot_sync(0xffffffffu, a);
+            const uint32_t bVw = __ballot_sync(0xffffffffu, V);
+            if (lane == j) {
+                myA = bAw;
+                mya = baw;
+                myV = bVw;
+            }
+        }
+        const int w = w0 + lane;
+        if (w < Wp) {
+            uint32_t *out = planes + (size_t)s * 3 * Wp + w;
+            out[0] = myA;
+            out[(size_t)Wp] = mya;
+            out[2 * (size_t)Wp] = myV;
+        }
+    }
+}
+
+cudaError_t launch_decode_bed(const uint8_t *bed_payload, size_t bps, int n_snps,
+                              const int32_t *perm, int Wp, uint32_t *planes,
+                              cudaStream_t stream) {
+    if (n_snps <= 0) return cudaSuccess;
+    const size_t budget = 40 * 1024;
+    int spc = (int)(budget / (bps ? bps : 1));
+    if (spc < 1) spc = 1;
+    if (spc > 32) spc = 32;
+    size_t smem = (size_t)spc * bps;
+    if (smem > 200 * 1024) return cudaErrorInvalidValue;  // > ~800k samples: not supported
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(decode_bed_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    int grid = (n_snps + spc - 1) / spc;
+    decode_bed_kernel<<<grid, 256, smem, stream>>>(bed_payload, bps, n_snps, perm, Wp, spc,
+                                                   planes);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_decode_rows(const uint64_t *bits, const uint64_t *valid, int nw, int n_snps,
+                               const int32_t *perm, int Wp, uint32_t *planes,
+                               cudaStream_t stream, int num_sms) {
+    if (n_snps <= 0) return cudaSuccess;
+    long long jobs = (long long)((Wp + 31) / 32) * n_snps;
+    long long blocks = (jobs + 7) / 8;
+    long long cap = (long long)num_sms * 8;
+    int grid = (int)(blocks < cap ? blocks : cap);
+    if (grid < 1) grid = 1;
+    decode_rows_kernel<<<grid, 256, 0, stream>>>(bits, valid, nw, n_snps, perm, Wp, planes);
+    return cudaGetLastError();
+}
+
+}  // namespace gepi

@@ -1,0 +1,315 @@
+// Device-side shared definitions: plane layout, scan state, candidate records
+// and the fused scoring epilogue used by every counting kernel.
+//
+// Genotype planes (HBM, uint32 words): for .bim SNP s and plane p
+//   p = 0 : carriers of the .bim column-5 allele (reference allele row 2s)
+//   p = 1 : carriers of the .bim column-6 allele (reference allele row 2s+1)
+//   p = 2 : valid (non-missing) call
+// row (3s + p), words [0, W0) hold class-0 samples (phenotype 1) in file order,
+// words [W0, W0+W1) class-1 samples (phenotype 2); each class is zero-padded
+// to a multiple of 128 samples.  Row pitch Wp = W0 + W1 words (16 B multiple).
+//
+// For SNP pair (s, t) and class c the kernels produce the 9 Gram counts
+// G[p*3+q] = popcount(plane_p(s) & plane_q(t)) over class-c words.  For allele
+// rows rA = 2s+i, rB = 2t+j (bits a, b) the 2x2 table of the reference's
+// binFunc (proc_gold.h:38-71) follows exactly:
+//   n11 = G[i][j]; n10 = G[i][2]-n11; n01 = G[2][j]-n11;
+//   n00 = G[2][2]-G[i][2]-G[2][j]+n11
+//   on(AND)=n11, on(NAND ~a&b)=n01, on(ANDN a&~b)=n10, on(NANDN)=n00,
+//   on(XOR)=n10+n01, valid = G[2][2].
+#pragma once
+
+#include <cstdint>
+
+namespace gepi {
+
+constexpr int kNumFuncs = 5;
+constexpr int kClassPadSamples = 128;
+
+// Candidate record appended by the epilogue (32 bytes).
+struct __align__(16) Cand {
+    unsigned long long key;  // order-preserving image of the objective (larger = better)
+    int32_t rA;              // allele row A (larger)
+    int32_t rBfun;           // allele row B * 8 + function
+    int32_t n[4];            // w, x, y, z
+};
+static_assert(sizeof(Cand) == 32, "Cand layout");
+
+// Mutable scan state shared by the kernels of one scan (device memory).
+struct ScanState {
+    unsigned long long tau_key;  // append tests with key >= tau_key
+    float theta;                 // entropy bound threshold (see score_tests)
+    float lp_thr;                // Fisher bound: reject when log P(obs) > lp_thr (nats)
+    uint32_t count;              // appended candidates (may exceed cap)
+    uint32_t overflow;           // set when count went past cap
+    uint32_t exact_evals;        // tests that reached the exact path
+    uint32_t pad;
+};
+
+struct ScanCtx {
+    const uint64_t *T;   // fixed-point n*log2(n) table, n in [0, Smax]
+    int F;               // its fraction bits
+    const double *lf;    // log(n!) table (Fisher exact path)
+    const float *lf32;   // log(n!) as float (Fisher bound)
+    int objective;       // 0 entropy, 1 Fisher
+    Cand *cand;
+    uint32_t cap;
+    ScanState *st;
+};
+
+// Order-preserving map double -> u64 (larger double -> larger key).
+__host__ __device__ inline unsigned long long key_of(double v) {
+    unsigned long long b;
+#ifdef __CUDA_ARCH__
+    b = (unsigned long long)__double_as_longlong(v);
+#else
+    __builtin_memcpy(&b, &v, 8);
+#endif
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__host__ __device__ inline double value_of_key(unsigned long long k) {
+    unsigned long long b = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
+    double v;
+#ifdef __CUDA_ARCH__
+    v = __longlong_as_double((long long)b);
+#else
+    __builtin_memcpy(&v, &b, 8);
+#endif
+    return v;
+}
+
+#ifdef __CUDACC__
+
+// Exact mutual information (bits) from the fixed-point table: the integer
+// numerator m*I*2^F is summed modulo 2^64 (exact, |result| < 2^62), then one
+// ldexp and one IEEE division; identical on host and device.
+__device__ __forceinline__ double exact_mi(const uint64_t *__restrict__ T, int F, int w, int x,
+                                           int y, int z) {
+    int m = y + z, xx = w + x;
+    if (m == 0) return 0.0;
+    uint64_t num = __ldg(T + m) + __ldg(T + w) + __ldg(T + (y - w)) + __ldg(T + x) +
+                   __ldg(T + (z - x)) - __ldg(T + xx) - __ldg(T + (m - xx)) - __ldg(T + y) -
+                   __ldg(T + z);
+    return scalbn((double)(long long)num, -F) / (double)m;
+}
+
+// Two-sided Fisher exact test for the table (n11 n12 / n21 n22), natural-log
+// p-value.  Terms with P(x) <= P(obs) * (1 + 1e-7) are summed (R's rule).  The
+// observed term is anchored with the log-factorial table; the hypergeometric
+// is log-concave, so the tail beyond xo (away from the mode) is walked with
+// the term ratio, a possible plateau between xo and the mode is walked term by
+// term, and the first qualifying term past the mode is found by bisection
+// before that tail is walked.  Walks stop once a term adds < 1e-17 of the sum.
+__device__ inline double fisher_lnp(const double *__restrict__ lf, int n11, int n12, int n21,
+                                    int n22) {
+    const int r1 = n11 + n21;  // column-1 total
+    const int r2 = n12 + n22;  // column-2 total
+    const int c1 = n11 + n12;  // row-1 total
+    const int N = r1 + r2;
+    const int lo = c1 <= r2 ? 0 : c1 - r2;
+    const int hi = c1 < r1 ? c1 : r1;
+    if (lo >= hi) return 0.0;
+    const double K = __ldg(lf + r1) + __ldg(lf + r2) + __ldg(lf + c1) + __ldg(lf + (N - c1)) -
+                     __ldg(lf + N);
+    auto lpx = [&](int x) {
+        return K - __ldg(lf + x) - __ldg(lf + (r1 - x)) - __ldg(lf + (c1 - x)) -
+               __ldg(lf + (r2 - c1 + x));
+    };
+    // P(x+1)/P(x) and P(x-1)/P(x)
+    auto up = [&](int x) {
+        return ((double)(r1 - x) * (double)(c1 - x)) / ((double)(x + 1) * (double)(r2 - c1 + x + 1));
+    };
+    auto down = [&](int x) {
+        return ((double)x * (double)(r2 - c1 + x)) / ((double)(r1 - x + 1) * (double)(c1 - x + 1));
+    };
+    const double tol = 1.0 + 1e-7;
+    const int xo = n11;
+    const double lpo = lpx(xo);
+    const double lim = lpo + 9.99999950000003e-08;  // log1p(1e-7)
+    int xm = (int)(((double)(r1 + 1) * (double)(c1 + 1)) / (double)(N + 2));
+    if (xm < lo) xm = lo;
+    if (xm > hi) xm = hi;
+    double S = 1.0;
+    if (xo <= xm) {
+        // near tail: x < xo
+        double t = 1.0;
+        for (int x = xo; x > lo;) {
+            t *= down(x);
+            --x;
+            S += t;
+            if (t < 1e-17 * S) break;
+        }
+        // plateau between xo and the mode
+        t = 1.0;
+        for (int x = xo; x < xm;) {
+            double t2 = t * up(x);
+            if (t2 > tol) break;
+            ++x;
+            t = t2;
+            S += t;
+        }
+        // falling side x in [xm+1, hi]: first x with lpx(x) <= lim
+        int a = xm + 1, b = hi;
+        if (a <= b && lpx(b) <= lim) {
+            int l = a, h = b;
+            while (l < h) {
+                int mid = (l + h) >> 1;
+                if (lpx(mid) <= lim) h = mid; else l = mid + 1;
+            }
+            double u = exp(lpx(l) - lpo);
+            S += u;
+            for (int x = l; x < hi;) {
+                u *= up(x);
+                ++x;
+                S += u;
+                if (u < 1e-17 * S) break;
+            }
+        }
+    } else {
+        // near tail: x > xo
+        double t = 1.0;
+        for (int x = xo; x < hi;) {
+            t *= up(x);
+            ++x;
+            S += t;
+            if (t < 1e-17 * S) break;
+        }
+        t = 1.0;
+        for (int x = xo; x > xm;) {
+            double t2 = t * down(x);
+            if (t2 > tol) break;
+            --x;
+            t = t2;
+            S += t;
+        }
+        // falling side x in [lo, xm-1]: last x with lpx(x) <= lim
+        int a = lo, b = xm - 1;
+        if (a <= b && lpx(a) <= lim) {
+            int l = a, h = b;
+            while (l < h) {
+                int mid = (l + h + 1) >> 1;
+                if (lpx(mid) <= lim) l = mid; else h = mid - 1;
+            }
+            double u = exp(lpx(l) - lpo);
+            S += u;
+            for (int x = l; x > lo;) {
+                u *= down(x);
+                --x;
+                S += u;
+                if (u < 1e-17 * S) break;
+            }
+        }
+    }
+    double lnp = lpo + log(S);
+    return lnp > 0.0 ? 0.0 : lnp;
+}
+
+__device__ __forceinline__ void append_candidate(const ScanCtx &ctx, double value, int rA,
+                                                 int rB, int fun, int w, int x, int y, int z) {
+    unsigned long long key = key_of(value);
+    if (key < ctx.st->tau_key) return;
+    uint32_t idx = atomicAdd(&ctx.st->count, 1u);
+    if (idx >= ctx.cap) {
+        ctx.st->overflow = 1u;
+        return;
+    }
+    Cand c;
+    c.key = key;
+    c.rA = rA;
+    c.rBfun = rB * 8 + fun;
+    c.n[0] = w;
+    c.n[1] = x;
+    c.n[2] = y;
+    c.n[3] = z;
+    ctx.cand[idx] = c;
+}
+
+// Exact evaluation of one test that passed the bound; appends if it ranks.
+static __device__ __noinline__ void exact_test(const ScanCtx &ctx, int rA, int rB, int fun, int w,
+                                        int x, int y, int z) {
+    long long d = (long long)w * z - (long long)x * y;
+    if (d == 0) return;
+    atomicAdd(&ctx.st->exact_evals, 1u);
+    double value;
+    if (ctx.objective == 0) {
+        value = exact_mi(ctx.T, ctx.F, w, x, y, z);
+    } else {
+        // print order (w, y-w, x, z-x); value = -log10 p
+        value = -fisher_lnp(ctx.lf, w, y - w, x, z - x) * 0.43429448190325182765;
+    }
+    append_candidate(ctx, value, rA, rB, fun, w, x, y, z);
+}
+
+// Scores every test of SNP pair (s >= t) from the Gram counts of both classes
+// (G0 class 0, G1 class 1; float holding exact integers).  Row pairs (2s+i,
+// 2t+j) with 2t+j <= 2s+i, 5 functions each.
+//
+// Bound (entropy): I(F;C) <= log2(1 + phi^2), phi^2 = D^2 / Q with
+// D = w z - x y and Q = (w+x)(m-w-x) y z, since KL <= log(1 + chi^2).  A test
+// is dropped when (|D| + e)^2 < theta * Q, theta = (2^tau - 1)(1 - 2^-10) and e
+// bounding the float rounding of D.
+// Bound (Fisher): p >= P(obs); dropped when log P(obs) > lp_thr.
+__device__ __forceinline__ void score_tests(const ScanCtx &ctx, const float *G0,
+                                            const float *G1, int s, int t, float theta,
+                                            float lp_thr) {
+    const float y = G0[8], z = G1[8];
+    const float m = y + z;
+    const float yz = y * z;
+    const bool diag = (s == t);
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            if (diag && j > i) continue;  // row 2t+j must be <= row 2s+i
+            float on0[5], on1[5];
+            {
+                float n11 = G0[i * 3 + j], r = G0[i * 3 + 2], c = G0[6 + j];
+                float n10 = r - n11, n01 = c - n11, n00 = y - r - c + n11;
+                on0[0] = n11; on0[1] = n01; on0[2] = n10; on0[3] = n00; on0[4] = n10 + n01;
+            }
+            {
+                float n11 = G1[i * 3 + j], r = G1[i * 3 + 2], c = G1[6 + j];
+                float n10 = r - n11, n01 = c - n11, n00 = z - r - c + n11;
+                on1[0] = n11; on1[1] = n01; on1[2] = n10; on1[3] = n00; on1[4] = n10 + n01;
+            }
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+                const float w = on0[f], x = on1[f];
+                bool pass;
+                if (ctx.objective == 0) {
+                    const float xx = w + x;
+                    const float Q = xx * (m - xx) * yz;
+                    const float wz = w * z, xy = x * y;
+                    const float D = fabsf(wz - xy) + (wz + xy) * 2.384185791015625e-07f;  // 2^-22
+                    pass = D * D >= theta * Q;
+                } else {
+                    // log P(obs) = lf(r1)+lf(r2)+lf(y)+lf(z)-lf(m)-lf(w)-lf(y-w)-lf(x)-lf(z-x)
+                    const int iw = (int)w, ix = (int)x, iy = (int)y, iz = (int)z;
+                    const float *L = ctx.lf32;
+                    float lp = __ldg(L + (iw + ix)) + __ldg(L + (iy + iz - iw - ix)) + __ldg(L + iy) +
+                               __ldg(L + iz) - __ldg(L + (iy + iz)) - __ldg(L + iw) -
+                               __ldg(L + (iy - iw)) - __ldg(L + ix) - __ldg(L + (iz - ix));
+                    pass = lp <= lp_thr;
+                }
+                if (pass)
+                    exact_test(ctx, 2 * s + i, 2 * t + j, f, (int)w, (int)x, (int)y, (int)z);
+            }
+        }
+    }
+}
+
+// Out-of-line wrapper: G points at 18 floats (class 0 Gram, class 1 Gram).
+static __device__ __noinline__ void score_pair(const ScanCtx &ctx, const float *G, int s, int t,
+                                        float theta, float lp_thr) {
+    float G0[9], G1[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        G0[k] = G[k];
+        G1[k] = G[9 + k];
+    }
+    score_tests(ctx, G0, G1, s, t, theta, lp_thr);
+}
+
+#endif  // __CUDACC__
+
+}  // namespace gepi

@@ -1,0 +1,616 @@
+// Scan orchestration and the C ABI (include/gepi.h).
+//
+// Replaces launch_process_gpu_1 (src/kernels/kernel1.cu:295-505): instead of
+// square batches of 4096 x 4096 allele rows with a full device sort, a host
+// D2H of every count and a host merge per batch, the scan walks a list of
+// 32 x 32 SNP tile pairs (lower triangle of the SNP-pair matrix, or the
+// rectangle of a range request) in a few adaptive batches.  Each batch is one
+// launch of the counting kernel with the fused epilogue; between batches a
+// device radix select raises the ranking threshold and compacts the candidate
+// buffer.  Only the final survivors (about k records) cross PCIe/C2C.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "common.h"
+#include "device.cuh"
+#include "tables.h"
+
+namespace gepi {
+
+cudaError_t launch_decode_bed(const uint8_t *bed_payload, size_t bps, int n_snps,
+                              const int32_t *perm, int Wp, uint32_t *planes, cudaStream_t stream);
+cudaError_t launch_decode_rows(const uint64_t *bits, const uint64_t *valid, int nw, int n_snps,
+                               const int32_t *perm, int Wp, uint32_t *planes,
+                               cudaStream_t stream, int num_sms);
+cudaError_t launch_popc_tiles(const uint32_t *planes, int Wp, int W0, const int2 *tiles,
+                              int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
+                              uint32_t *dump, cudaStream_t stream);
+cudaError_t run_select_compact(Cand *in, Cand *out, ScanState *st, void *sel, uint32_t cap,
+                               uint32_t k, int n_override, uint32_t n_compact, int objective,
+                               float lp_margin, int num_sms, cudaStream_t stream);
+size_t sel_state_bytes();
+int popc_tile_snps();
+constexpr int kSelectLaunches = 20;  // init + 8 x (histogram, pick) + apply + compact + count
+
+static thread_local std::string g_last_error;
+
+gepi_status set_error(gepi_status s, const std::string &msg) {
+    g_last_error = msg;
+    return s;
+}
+void clear_error() { g_last_error.clear(); }
+
+}  // namespace gepi
+
+using namespace gepi;
+
+struct gepi_planes {
+    int device = 0, num_sms = 0;
+    int n_snps = 0, S0 = 0, S1 = 0, W0 = 0, W1 = 0, Wp = 0;
+    uint32_t *d_planes = nullptr;
+    cudaStream_t stream = nullptr;
+    uint64_t *d_T = nullptr;
+    int F = 0;
+    double *d_lf = nullptr;
+    float *d_lf32 = nullptr;
+    float lf_max = 0.f;
+    Cand *d_cand[2] = {nullptr, nullptr};
+    uint32_t cap = 0;
+    ScanState *d_state = nullptr;
+    ScanState *h_state = nullptr;
+    void *d_sel = nullptr;
+    int2 *d_tiles = nullptr;
+    size_t tiles_cap = 0;
+    std::vector<cudaEvent_t> ev;  // timing events, reused across scans
+    gepi_scan_stats stats{};
+};
+
+namespace {
+
+struct DeviceGuard {
+    int prev = -1;
+    bool ok = false;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        ok = cudaSetDevice(dev) == cudaSuccess;
+    }
+    ~DeviceGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+template <class T>
+void dfree(T *&p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+gepi_status check_mem(size_t bytes, const char *what) {
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return GEPI_OK;
+    if (bytes + (64u << 20) > fr)
+        return set_error(GEPI_ERR_OOM, std::string(what) + ": needs " + std::to_string(bytes >> 20) +
+                                           " MiB, " + std::to_string(fr >> 20) + " MiB free");
+    return GEPI_OK;
+}
+
+// Class-sorted permutation: slot -> source sample (-1 = pad).
+void build_perm(const std::vector<int> &cls0, const std::vector<int> &cls1, int W0, int Wp,
+                std::vector<int32_t> &perm) {
+    perm.assign((size_t)Wp * 32, -1);
+    for (size_t j = 0; j < cls0.size(); ++j) perm[j] = cls0[j];
+    for (size_t j = 0; j < cls1.size(); ++j) perm[(size_t)W0 * 32 + j] = cls1[j];
+}
+
+gepi_status planes_alloc(gepi_planes *pl, int device, int n_snps, int S0, int S1) {
+    pl->device = device;
+    pl->n_snps = n_snps;
+    pl->S0 = S0;
+    pl->S1 = S1;
+    pl->W0 = ((S0 + kClassPadSamples - 1) / kClassPadSamples) * (kClassPadSamples / 32);
+    pl->W1 = ((S1 + kClassPadSamples - 1) / kClassPadSamples) * (kClassPadSamples / 32);
+    pl->Wp = pl->W0 + pl->W1;
+    GEPI_CUDA(cudaDeviceGetAttribute(&pl->num_sms, cudaDevAttrMultiProcessorCount, device));
+    GEPI_CUDA(cudaStreamCreateWithFlags(&pl->stream, cudaStreamNonBlocking));
+    size_t bytes = (size_t)n_snps * 3 * pl->Wp * 4;
+    GEPI_TRY(check_mem(bytes, "genotype planes"));
+    GEPI_CUDA(cudaMalloc(&pl->d_planes, bytes));
+    return GEPI_OK;
+}
+
+void planes_free(gepi_planes *pl) {
+    if (!pl) return;
+    DeviceGuard g(pl->device);
+    if (pl->stream) cudaStreamSynchronize(pl->stream);
+    dfree(pl->d_planes);
+    dfree(pl->d_T);
+    dfree(pl->d_lf);
+    dfree(pl->d_lf32);
+    dfree(pl->d_cand[0]);
+    dfree(pl->d_cand[1]);
+    dfree(pl->d_state);
+    dfree(pl->d_sel);
+    dfree(pl->d_tiles);
+    if (pl->h_state) cudaFreeHost(pl->h_state);
+    pl->h_state = nullptr;
+    for (cudaEvent_t e : pl->ev) cudaEventDestroy(e);
+    pl->ev.clear();
+    if (pl->stream) cudaStreamDestroy(pl->stream);
+    pl->stream = nullptr;
+}
+
+gepi_status ensure_tables(gepi_planes *pl) {
+    if (pl->d_T) return GEPI_OK;
+    const int64_t nmax = (int64_t)pl->S0 + pl->S1;
+    pl->F = tfix_bits(nmax);
+    std::vector<uint64_t> T;
+    build_tfix(nmax, pl->F, T);
+    std::vector<double> lf;
+    std::vector<float> lf32;
+    build_lfact(nmax, lf, lf32);
+    pl->lf_max = (float)lf.back();
+    GEPI_CUDA(cudaMalloc(&pl->d_T, T.size() * 8));
+    GEPI_CUDA(cudaMalloc(&pl->d_lf, lf.size() * 8));
+    GEPI_CUDA(cudaMalloc(&pl->d_lf32, lf32.size() * 4));
+    GEPI_CUDA(cudaMemcpy(pl->d_T, T.data(), T.size() * 8, cudaMemcpyHostToDevice));
+    GEPI_CUDA(cudaMemcpy(pl->d_lf, lf.data(), lf.size() * 8, cudaMemcpyHostToDevice));
+    GEPI_CUDA(cudaMemcpy(pl->d_lf32, lf32.data(), lf32.size() * 4, cudaMemcpyHostToDevice));
+    return GEPI_OK;
+}
+
+gepi_status ensure_scan_buffers(gepi_planes *pl, int k) {
+    uint64_t want = std::max<uint64_t>(1u << 22, ((uint64_t)k * 8 + 1023) & ~1023ull);
+    // GEPI_DEBUG_CAP shrinks the candidate buffer (>= 4k entries) so tests can
+    // drive the overflow / retry path on small inputs.
+    if (const char *e = std::getenv("GEPI_DEBUG_CAP")) {
+        long long v = std::atoll(e);
+        if (v > 0) want = std::max<uint64_t>((uint64_t)v, 4ull * (uint64_t)k);
+        if (pl->cap != want) {
+            dfree(pl->d_cand[0]);
+            dfree(pl->d_cand[1]);
+            pl->cap = 0;
+        }
+    }
+    if (want > (1ull << 31)) return set_error(GEPI_ERR_LIMIT, "topmost too large");
+    if (pl->cap < want) {
+        dfree(pl->d_cand[0]);
+        dfree(pl->d_cand[1]);
+        GEPI_TRY(check_mem(2 * want * sizeof(Cand), "candidate buffers"));
+        GEPI_CUDA(cudaMalloc(&pl->d_cand[0], want * sizeof(Cand)));
+        GEPI_CUDA(cudaMalloc(&pl->d_cand[1], want * sizeof(Cand)));
+        pl->cap = (uint32_t)want;
+    }
+    if (!pl->d_state) GEPI_CUDA(cudaMalloc(&pl->d_state, sizeof(ScanState)));
+    if (!pl->h_state) GEPI_CUDA(cudaMallocHost(&pl->h_state, sizeof(ScanState)));
+    if (!pl->d_sel) GEPI_CUDA(cudaMalloc(&pl->d_sel, sel_state_bytes()));
+    return GEPI_OK;
+}
+
+gepi_status upload_tiles(gepi_planes *pl, const std::vector<int2> &tiles) {
+    if (tiles.size() > pl->tiles_cap) {
+        dfree(pl->d_tiles);
+        GEPI_CUDA(cudaMalloc(&pl->d_tiles, tiles.size() * sizeof(int2)));
+        pl->tiles_cap = tiles.size();
+    }
+    if (!tiles.empty())
+        GEPI_CUDA(cudaMemcpyAsync(pl->d_tiles, tiles.data(), tiles.size() * sizeof(int2),
+                                  cudaMemcpyHostToDevice, pl->stream));
+    return GEPI_OK;
+}
+
+// Tile pairs of [a0,a1) x [b0,b1) holding at least one (s, t) with t <= s.
+void build_tiles(int a0, int a1, int b0, int b1, int T, bool triangle, std::vector<int2> &out) {
+    out.clear();
+    const int nat = (a1 - a0 + T - 1) / T, nbt = (b1 - b0 + T - 1) / T;
+    for (int i = 0; i < nat; ++i) {
+        const int smax = std::min(a0 + i * T + T - 1, a1 - 1);
+        for (int j = 0; j < nbt; ++j) {
+            const int tmin = b0 + j * T;
+            if (triangle && tmin > smax) break;
+            out.push_back(make_int2(i, j));
+        }
+    }
+}
+
+gepi_status ensure_events(gepi_planes *pl, size_t n) {
+    while (pl->ev.size() < n) {
+        cudaEvent_t e;
+        GEPI_CUDA(cudaEventCreate(&e));
+        pl->ev.push_back(e);
+    }
+    return GEPI_OK;
+}
+
+bool cand_better(const Cand &a, const Cand &b) {
+    if (a.key != b.key) return a.key > b.key;
+    if (a.rA != b.rA) return a.rA < b.rA;
+    return a.rBfun < b.rBfun;
+}
+
+gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, int b0, int nb,
+                      gepi_result *tops, int k) {
+    clear_error();
+    if (!pl || !par || !tops || k <= 0) return set_error(GEPI_ERR_ARG, "gepi_scan: bad argument");
+    if (par->objective != GEPI_ENTROPY && par->objective != GEPI_FISHER)
+        return set_error(GEPI_ERR_ARG, "gepi_scan: unknown objective");
+    if (par->method == GEPI_METHOD_TENSOR)
+        return set_error(GEPI_ERR_UNSUPPORTED, "tensor-core counting not available in this build");
+    if (a0 < 0 || b0 < 0 || na < 0 || nb < 0 || a0 + na > pl->n_snps || b0 + nb > pl->n_snps)
+        return set_error(GEPI_ERR_ARG, "gepi_scan: SNP range outside the planes");
+    DeviceGuard g(pl->device);
+    if (!g.ok) return set_error(GEPI_ERR_CUDA, "cudaSetDevice failed");
+    GEPI_TRY(ensure_tables(pl));
+    GEPI_TRY(ensure_scan_buffers(pl, k));
+    std::memset(tops, 0, sizeof(gepi_result) * (size_t)k);
+
+    const int T = popc_tile_snps();
+    std::vector<int2> tiles;
+    build_tiles(a0, a0 + na, b0, b0 + nb, T, true, tiles);
+    GEPI_TRY(upload_tiles(pl, tiles));
+    GEPI_TRY(ensure_events(pl, 4));
+    gepi_scan_stats &S = pl->stats;
+    S = gepi_scan_stats{};
+    S.method = GEPI_METHOD_POPC;
+    S.tile_snps = T;
+    S.tiles = tiles.size();
+    {
+        // pairs (s, t), t < s, s in A, t in B; and SNPs in both ranges
+        const int64_t ia0 = a0, ia1 = (int64_t)a0 + na, ib0 = b0, ib1 = (int64_t)b0 + nb;
+        uint64_t pairs = 0;
+        for (int64_t s = ia0; s < ia1; ++s) {
+            const int64_t hi = std::min<int64_t>(s, ib1);
+            if (hi > ib0) pairs += (uint64_t)(hi - ib0);
+        }
+        S.snp_pairs = pairs;
+        const int64_t lo = std::max(ia0, ib0), hi = std::min(ia1, ib1);
+        S.diag_snps = hi > lo ? (uint64_t)(hi - lo) : 0;
+    }
+    GEPI_CUDA(cudaEventRecord(pl->ev[0], pl->stream));
+
+    ScanState init{};
+    init.tau_key = 0ull;
+    init.theta = 0.f;
+    init.lp_thr = INFINITY;
+    *pl->h_state = init;
+    GEPI_CUDA(cudaMemcpyAsync(pl->d_state, pl->h_state, sizeof(ScanState), cudaMemcpyHostToDevice,
+                              pl->stream));
+
+    const float lp_margin = 2e-6f * pl->lf_max + 1e-3f;
+    int cur = 0;
+    ScanCtx ctx;
+    ctx.T = pl->d_T;
+    ctx.F = pl->F;
+    ctx.lf = pl->d_lf;
+    ctx.lf32 = pl->d_lf32;
+    ctx.objective = par->objective;
+    ctx.cap = pl->cap;
+    ctx.st = pl->d_state;
+
+    const size_t ntiles = tiles.size();
+    const double tests_per_tile = 20.0 * T * T;
+    const uint32_t budget = pl->cap / 2;
+    const double pilot_tests = par->objective == GEPI_ENTROPY ? pl->cap / 4.0 : 1.0 * (1 << 16);
+    size_t batch = (size_t)std::max(1.0, std::floor(pilot_tests / tests_per_tile));
+    size_t t = 0;
+    uint32_t count = 0;
+    int retries = 0;
+    while (t < ntiles) {
+        const size_t nbt = std::min(batch, ntiles - t);
+        ctx.cand = pl->d_cand[cur];
+        GEPI_CUDA(cudaEventRecord(pl->ev[2], pl->stream));
+        GEPI_CUDA(launch_popc_tiles(pl->d_planes, pl->Wp, pl->W0, pl->d_tiles + t, (int)nbt, a0,
+                                    a0 + na, b0, b0 + nb, ctx, nullptr, pl->stream));
+        GEPI_CUDA(cudaEventRecord(pl->ev[3], pl->stream));
+        GEPI_CUDA(cudaMemcpyAsync(pl->h_state, pl->d_state, sizeof(ScanState),
+                                  cudaMemcpyDeviceToHost, pl->stream));
+        GEPI_CUDA(cudaStreamSynchronize(pl->stream));
+        {
+            float ms = 0.f;
+            GEPI_CUDA(cudaEventElapsedTime(&ms, pl->ev[2], pl->ev[3]));
+            S.count_ms += ms;
+            S.max_count_ms = std::max<double>(S.max_count_ms, ms);
+            S.count_launches += 1;
+        }
+        if (pl->h_state->overflow) {
+            // Tighten with everything captured (a valid lower bound), drop this
+            // batch's partial appends, retry it in halves.  Only more than
+            // `cap` exactly tied candidates can keep overflowing a 1-tile batch.
+            if (++retries > 64)
+                return set_error(GEPI_ERR_LIMIT, "candidate buffer keeps overflowing (massive ties)");
+            S.overflows += 1;
+            S.other_launches += kSelectLaunches;
+            GEPI_CUDA(run_select_compact(pl->d_cand[cur], pl->d_cand[cur ^ 1], pl->d_state,
+                                         pl->d_sel, pl->cap, (uint32_t)k, (int)pl->cap, count,
+                                         par->objective, lp_margin, pl->num_sms, pl->stream));
+            cur ^= 1;
+            GEPI_CUDA(cudaMemcpyAsync(pl->h_state, pl->d_state, sizeof(ScanState),
+                                      cudaMemcpyDeviceToHost, pl->stream));
+            GEPI_CUDA(cudaStreamSynchronize(pl->stream));
+            count = pl->h_state->count;
+            batch = std::max<size_t>(1, nbt / 2);
+            if (par->verbose)
+                std::fprintf(stderr, "gepi: candidate overflow, batch -> %zu tiles\n", batch);
+            continue;
+        }
+        const uint32_t appended = pl->h_state->count - count;
+        count = pl->h_state->count;
+        t += nbt;
+        retries = 0;
+        S.batches += 1;
+        if (count > budget && t < ntiles) {
+            S.other_launches += kSelectLaunches;
+            GEPI_CUDA(run_select_compact(pl->d_cand[cur], pl->d_cand[cur ^ 1], pl->d_state,
+                                         pl->d_sel, pl->cap, (uint32_t)k, -1, 0xFFFFFFFFu,
+                                         par->objective, lp_margin, pl->num_sms, pl->stream));
+            cur ^= 1;
+            GEPI_CUDA(cudaMemcpyAsync(pl->h_state, pl->d_state, sizeof(ScanState),
+                                      cudaMemcpyDeviceToHost, pl->stream));
+            GEPI_CUDA(cudaStreamSynchronize(pl->stream));
+            count = pl->h_state->count;
+        }
+        // Next batch: as many tiles as the remaining budget allows at the
+        // append rate just observed (an over-estimate once tau has risen),
+        // growing at most 8x per step.
+        const double rate = std::max(1.0, (double)appended) / (double)nbt;
+        const double room = (double)budget - (double)count;
+        double nb_next = room > 0 ? room / rate : 1.0;
+        nb_next = std::min(nb_next, 8.0 * (double)nbt);
+        batch = (size_t)std::max(1.0, nb_next);
+        if (par->verbose)
+            std::fprintf(stderr, "gepi: %zu/%zu tiles, %u candidates, next batch %zu\n", t, ntiles,
+                         count, batch);
+    }
+    if (count > (uint32_t)k) {
+        S.other_launches += kSelectLaunches;
+        GEPI_CUDA(run_select_compact(pl->d_cand[cur], pl->d_cand[cur ^ 1], pl->d_state, pl->d_sel,
+                                     pl->cap, (uint32_t)k, -1, 0xFFFFFFFFu, par->objective,
+                                     lp_margin, pl->num_sms, pl->stream));
+        cur ^= 1;
+        GEPI_CUDA(cudaMemcpyAsync(pl->h_state, pl->d_state, sizeof(ScanState),
+                                  cudaMemcpyDeviceToHost, pl->stream));
+        GEPI_CUDA(cudaStreamSynchronize(pl->stream));
+        count = pl->h_state->count;
+    }
+    GEPI_CUDA(cudaEventRecord(pl->ev[1], pl->stream));
+    std::vector<Cand> host(count);
+    if (count)
+        GEPI_CUDA(cudaMemcpyAsync(host.data(), pl->d_cand[cur], (size_t)count * sizeof(Cand),
+                                  cudaMemcpyDeviceToHost, pl->stream));
+    GEPI_CUDA(cudaStreamSynchronize(pl->stream));
+    {
+        float ms = 0.f;
+        GEPI_CUDA(cudaEventElapsedTime(&ms, pl->ev[0], pl->ev[1]));
+        S.scan_ms = ms;
+        S.candidates = count;
+    }
+    const size_t keep = std::min<size_t>(host.size(), (size_t)k);
+    std::partial_sort(host.begin(), host.begin() + keep, host.end(), cand_better);
+    for (size_t i = 0; i < keep; ++i) {
+        const Cand &c = host[i];
+        gepi_result &r = tops[i];
+        r.sA = c.rA;
+        r.sB = c.rBfun >> 3;
+        r.fun = (char)(c.rBfun & 7);
+        for (int j = 0; j < 4; ++j) r.n[j] = c.n[j];
+        r.ent = (float)(-value_of_key(c.key));
+    }
+    return GEPI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *gepi_status_string(gepi_status s) {
+    switch (s) {
+    case GEPI_OK: return "ok";
+    case GEPI_ERR_ARG: return "invalid argument";
+    case GEPI_ERR_IO: return "i/o error";
+    case GEPI_ERR_FORMAT: return "format error";
+    case GEPI_ERR_CUDA: return "CUDA error";
+    case GEPI_ERR_OOM: return "out of device memory";
+    case GEPI_ERR_NOCLASS: return "phenotype class 1 or 2 is empty";
+    case GEPI_ERR_TIMEOUT: return "device wait timed out";
+    case GEPI_ERR_UNSUPPORTED: return "unsupported";
+    case GEPI_ERR_LIMIT: return "request beyond a documented limit";
+    }
+    return "unknown status";
+}
+
+const char *gepi_last_error(void) { return g_last_error.c_str(); }
+
+int gepi_abi_version(void) { return GEPI_ABI_VERSION; }
+
+gepi_status gepi_planes_from_bed(const uint8_t *bed, size_t bed_bytes, int n_bim_snps,
+                                 int n_samples, const int32_t *phenotype, int device,
+                                 gepi_planes **out) {
+    clear_error();
+    if (!bed || !phenotype || !out || n_bim_snps <= 0 || n_samples <= 0)
+        return set_error(GEPI_ERR_ARG, "gepi_planes_from_bed: bad argument");
+    *out = nullptr;
+    const size_t bps = ((size_t)n_samples + 3) / 4;
+    if (bed_bytes < 3 || bed[0] != 0x6c || bed[1] != 0x1b)
+        return set_error(GEPI_ERR_FORMAT, ".bed: Incorrect Magic");
+    if (bed_bytes != 3 + (size_t)n_bim_snps * bps)
+        return set_error(GEPI_ERR_FORMAT, ".bed: size " + std::to_string(bed_bytes) +
+                                              " different than expected " +
+                                              std::to_string(3 + (size_t)n_bim_snps * bps));
+    std::vector<int> c0, c1;
+    for (int i = 0; i < n_samples; ++i) {
+        if (phenotype[i] == 1) c0.push_back(i);
+        else if (phenotype[i] == 2) c1.push_back(i);
+    }
+    if (c0.empty() || c1.empty()) return set_error(GEPI_ERR_NOCLASS, "Error in class mask data");
+    DeviceGuard g(device);
+    if (!g.ok) return set_error(GEPI_ERR_CUDA, "cudaSetDevice failed");
+    gepi_planes *pl = new gepi_planes();
+    gepi_status st = planes_alloc(pl, device, n_bim_snps, (int)c0.size(), (int)c1.size());
+    uint8_t *d_bed = nullptr;
+    int32_t *d_perm = nullptr;
+    auto fail = [&](gepi_status s) {
+        if (d_bed) cudaFree(d_bed);
+        if (d_perm) cudaFree(d_perm);
+        planes_free(pl);
+        delete pl;
+        return s;
+    };
+    if (st != GEPI_OK) return fail(st);
+    std::vector<int32_t> perm;
+    build_perm(c0, c1, pl->W0, pl->Wp, perm);
+    const size_t payload = bed_bytes - 3;
+    if ((st = check_mem(payload + perm.size() * 4, ".bed staging")) != GEPI_OK) return fail(st);
+    if (cudaMalloc(&d_bed, payload) != cudaSuccess || cudaMalloc(&d_perm, perm.size() * 4) != cudaSuccess)
+        return fail(set_error(GEPI_ERR_OOM, "cudaMalloc .bed staging failed"));
+    cudaError_t e = cudaMemcpyAsync(d_bed, bed + 3, payload, cudaMemcpyHostToDevice, pl->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_perm, perm.data(), perm.size() * 4, cudaMemcpyHostToDevice, pl->stream);
+    if (e == cudaSuccess)
+        e = launch_decode_bed(d_bed, bps, n_bim_snps, d_perm, pl->Wp, pl->d_planes, pl->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(pl->stream);
+    if (e != cudaSuccess)
+        return fail(set_error(GEPI_ERR_CUDA, std::string("decode: ") + cudaGetErrorString(e)));
+    cudaFree(d_bed);
+    cudaFree(d_perm);
+    *out = pl;
+    return GEPI_OK;
+}
+
+gepi_status gepi_planes_from_rows(const uint64_t *bits, const uint64_t *valid, int n_rows,
+                                  int n_words, const uint64_t *mask1, const uint64_t *mask2,
+                                  int device, gepi_planes **out) {
+    clear_error();
+    if (!bits || !valid || !mask1 || !mask2 || !out || n_rows <= 0 || (n_rows & 1) || n_words <= 0)
+        return set_error(GEPI_ERR_ARG, "gepi_planes_from_rows: bad argument");
+    *out = nullptr;
+    const int n_snps = n_rows / 2;
+    for (int s = 0; s < n_snps; ++s)
+        if (std::memcmp(valid + (size_t)(2 * s) * n_words, valid + (size_t)(2 * s + 1) * n_words,
+                        (size_t)n_words * 8) != 0)
+            return set_error(GEPI_ERR_FORMAT, "valid rows of allele pair " + std::to_string(s) +
+                                                  " differ");
+    std::vector<int> c0, c1;
+    for (int i = 0; i < n_words * 64; ++i) {
+        const uint64_t bit = 1ull << (i & 63);
+        const bool in0 = mask1[i >> 6] & bit, in1 = mask2[i >> 6] & bit;
+        if (in0 && in1) return set_error(GEPI_ERR_FORMAT, "sample in both class masks");
+        if (in0) c0.push_back(i);
+        if (in1) c1.push_back(i);
+    }
+    if (c0.empty() || c1.empty()) return set_error(GEPI_ERR_NOCLASS, "Error in class mask data");
+    DeviceGuard g(device);
+    if (!g.ok) return set_error(GEPI_ERR_CUDA, "cudaSetDevice failed");
+    gepi_planes *pl = new gepi_planes();
+    gepi_status st = planes_alloc(pl, device, n_snps, (int)c0.size(), (int)c1.size());
+    uint64_t *d_bits = nullptr, *d_valid = nullptr;
+    int32_t *d_perm = nullptr;
+    auto fail = [&](gepi_status s) {
+        if (d_bits) cudaFree(d_bits);
+        if (d_valid) cudaFree(d_valid);
+        if (d_perm) cudaFree(d_perm);
+        planes_free(pl);
+        delete pl;
+        return s;
+    };
+    if (st != GEPI_OK) return fail(st);
+    std::vector<int32_t> perm;
+    build_perm(c0, c1, pl->W0, pl->Wp, perm);
+    const size_t rb = (size_t)n_rows * n_words * 8;
+    if ((st = check_mem(2 * rb + perm.size() * 4, "row staging")) != GEPI_OK) return fail(st);
+    if (cudaMalloc(&d_bits, rb) != cudaSuccess || cudaMalloc(&d_valid, rb) != cudaSuccess ||
+        cudaMalloc(&d_perm, perm.size() * 4) != cudaSuccess)
+        return fail(set_error(GEPI_ERR_OOM, "cudaMalloc row staging failed"));
+    cudaError_t e = cudaMemcpyAsync(d_bits, bits, rb, cudaMemcpyHostToDevice, pl->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_valid, valid, rb, cudaMemcpyHostToDevice, pl->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_perm, perm.data(), perm.size() * 4, cudaMemcpyHostToDevice, pl->stream);
+    if (e == cudaSuccess)
+        e = launch_decode_rows(d_bits, d_valid, n_words, n_snps, d_perm, pl->Wp, pl->d_planes,
+                               pl->stream, pl->num_sms);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(pl->stream);
+    if (e != cudaSuccess)
+        return fail(set_error(GEPI_ERR_CUDA, std::string("decode rows: ") + cudaGetErrorString(e)));
+    cudaFree(d_bits);
+    cudaFree(d_valid);
+    cudaFree(d_perm);
+    *out = pl;
+    return GEPI_OK;
+}
+
+void gepi_planes_destroy(gepi_planes *pl) {
+    if (!pl) return;
+    planes_free(pl);
+    delete pl;
+}
+
+int gepi_planes_num_snps(const gepi_planes *pl) { return pl ? pl->n_snps : 0; }
+
+gepi_status gepi_planes_class_sizes(const gepi_planes *pl, int *n0, int *n1) {
+    if (!pl) return set_error(GEPI_ERR_ARG, "null planes");
+    if (n0) *n0 = pl->S0;
+    if (n1) *n1 = pl->S1;
+    return GEPI_OK;
+}
+
+gepi_status gepi_scan(gepi_planes *pl, const gepi_params *par, gepi_result *tops, int k) {
+    if (!pl) return set_error(GEPI_ERR_ARG, "null planes");
+    return scan_impl(pl, par, 0, pl->n_snps, 0, pl->n_snps, tops, k);
+}
+
+gepi_status gepi_scan_range(gepi_planes *pl, const gepi_params *par, int a0, int na, int b0,
+                            int nb, gepi_result *tops, int k) {
+    return scan_impl(pl, par, a0, na, b0, nb, tops, k);
+}
+
+gepi_status gepi_pair_counts(gepi_planes *pl, int method, int a0, int na, int b0, int nb,
+                             uint32_t *out) {
+    clear_error();
+    if (!pl || !out || na <= 0 || nb <= 0 || a0 < 0 || b0 < 0 || a0 + na > pl->n_snps ||
+        b0 + nb > pl->n_snps)
+        return set_error(GEPI_ERR_ARG, "gepi_pair_counts: bad argument");
+    if (method != GEPI_METHOD_POPC && method != GEPI_METHOD_AUTO)
+        return set_error(GEPI_ERR_UNSUPPORTED, "tensor-core counting not available in this build");
+    DeviceGuard g(pl->device);
+    if (!g.ok) return set_error(GEPI_ERR_CUDA, "cudaSetDevice failed");
+    std::vector<int2> tiles;
+    build_tiles(a0, a0 + na, b0, b0 + nb, popc_tile_snps(), false, tiles);
+    GEPI_TRY(upload_tiles(pl, tiles));
+    const size_t bytes = (size_t)na * nb * 18 * 4;
+    GEPI_TRY(check_mem(bytes, "pair counts"));
+    uint32_t *d_out = nullptr;
+    GEPI_CUDA(cudaMalloc(&d_out, bytes));
+    ScanCtx ctx{};
+    cudaError_t e = launch_popc_tiles(pl->d_planes, pl->Wp, pl->W0, pl->d_tiles, (int)tiles.size(),
+                                      a0, a0 + na, b0, b0 + nb, ctx, d_out, pl->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, bytes, cudaMemcpyDeviceToHost, pl->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(pl->stream);
+    cudaFree(d_out);
+    if (e != cudaSuccess)
+        return set_error(GEPI_ERR_CUDA, std::string("pair counts: ") + cudaGetErrorString(e));
+    return GEPI_OK;
+}
+
+gepi_status gepi_last_scan_stats(const gepi_planes *pl, gepi_scan_stats *out) {
+    if (!pl || !out) return set_error(GEPI_ERR_ARG, "gepi_last_scan_stats: bad argument");
+    *out = pl->stats;
+    return GEPI_OK;
+}
+
+gepi_status gepi_process_gpu_1(const uint64_t *bits, const uint64_t *valid, int n_rows,
+                               int n_words, const uint64_t *mask1, const uint64_t *mask2,
+                               gepi_result *tops, const gepi_params *par) {
+    if (!par || !tops) return set_error(GEPI_ERR_ARG, "gepi_process_gpu_1: bad argument");
+    gepi_planes *pl = nullptr;
+    GEPI_TRY(gepi_planes_from_rows(bits, valid, n_rows, n_words, mask1, mask2, par->gpu_num, &pl));
+    gepi_status s = gepi_scan(pl, par, tops, par->topmost);
+    gepi_planes_destroy(pl);
+    return s;
+}
+
+}  // extern "C"

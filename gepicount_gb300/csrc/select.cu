@@ -1,0 +1,169 @@
+// Device top-k machinery replacing the per-batch thrust::sort_by_key, the
+// D2H of every count and the host streaming merge
+// (src/kernels/kernel1.cu:448, misc1.cu:205-264).
+//
+// Counting kernels append every test whose exact key is >= tau_key to a
+// candidate buffer.  When the buffer grows past its budget, a radix select
+// finds the k-th largest key (8 passes of 8-bit digits), tau_key is raised to
+// it and the buffer is compacted to keys >= tau_key (ties at the k-th place are
+// kept).  Every test with key >= the final k-th key is therefore present at the
+// end, and the host sorts the survivors by (key desc, rA, rB, fun).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+
+#include "device.cuh"
+
+namespace gepi {
+
+struct SelState {
+    unsigned long long prefix, mask;
+    uint32_t krem;     // rank still to locate inside the current bucket (0 = no select)
+    uint32_t n;        // entries examined
+    uint32_t ncompact; // entries kept by compaction
+    uint32_t pad;
+    uint32_t hist[256];
+};
+
+__global__ void sel_init_kernel(const ScanState *st, SelState *sel, uint32_t cap, uint32_t k,
+                                int n_override) {
+    if (threadIdx.x == 0) {
+        uint32_t n = n_override >= 0 ? (uint32_t)n_override : st->count;
+        if (n > cap) n = cap;
+        sel->n = n;
+        sel->krem = (n >= k && k > 0) ? k : 0u;
+        sel->prefix = 0ull;
+        sel->mask = 0ull;
+        sel->ncompact = 0u;
+    }
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) sel->hist[i] = 0u;
+}
+
+__global__ void sel_hist_kernel(const Cand *__restrict__ cand, SelState *sel, int shift) {
+    __shared__ uint32_t h[256];
+    if (sel->krem == 0) return;
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0u;
+    __syncthreads();
+    const uint32_t n = sel->n;
+    const unsigned long long prefix = sel->prefix, mask = sel->mask;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        unsigned long long key = cand[i].key;
+        if ((key & mask) == prefix) atomicAdd(&h[(key >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 256; i += blockDim.x)
+        if (h[i]) atomicAdd(&sel->hist[i], h[i]);
+}
+
+// One warp: walk buckets from the largest digit down to find the one holding
+// the krem-th largest key, fix that digit, clear the histogram.
+__global__ void sel_pick_kernel(SelState *sel, int shift) {
+    if (sel->krem == 0) return;
+    const int lane = threadIdx.x;
+    // lane L owns buckets 255-8L .. 248-8L (descending)
+    uint32_t c[8], tot = 0;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        c[j] = sel->hist[255 - 8 * lane - j];
+        tot += c[j];
+    }
+    // exclusive prefix over lanes (descending bucket order)
+    uint32_t incl = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    const uint32_t excl = incl - tot;
+    const uint32_t k = sel->krem;
+    const bool mine = excl < k && k <= incl;
+    const unsigned ball = __ballot_sync(0xffffffffu, mine);
+    const int owner = __ffs(ball) - 1;
+    if (lane == owner) {
+        uint32_t run = excl;
+        int b = 0;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            if (run + c[j] >= k) {
+                b = 255 - 8 * lane - j;
+                break;
+            }
+            run += c[j];
+        }
+        sel->krem = k - run;
+        sel->prefix |= (unsigned long long)b << shift;
+        sel->mask |= 255ull << shift;
+    }
+    __syncwarp();
+    for (int i = lane; i < 256; i += 32) sel->hist[i] = 0u;
+}
+
+// Raise tau_key to the selected key and derive the float bounds.
+//   entropy: theta = (2^I - 1) * (1 - 2^-10), I the selected mutual information
+//   Fisher : lp_thr = ln(p) + margin, p = 10^-v for the selected v = -log10 p
+__global__ void sel_apply_kernel(ScanState *st, const SelState *sel, int objective,
+                                 float lp_margin) {
+    if (sel->krem == 0) return;
+    unsigned long long key = sel->prefix;
+    if (key <= st->tau_key) return;
+    st->tau_key = key;
+    double v = value_of_key(key);
+    if (objective == 0) {
+        double th = (exp2(v) - 1.0) * (1.0 - 1.0 / 1024.0);
+        st->theta = th > 0.0 ? __double2float_rd(th) : 0.0f;
+    } else {
+        double lp = -v * 2.302585092994045684 + (double)lp_margin;
+        st->lp_thr = lp < 0.0 ? __double2float_ru(lp) : 0.0f;
+    }
+}
+
+__global__ void compact_kernel(const Cand *__restrict__ in, Cand *__restrict__ out,
+                               const ScanState *st, SelState *sel, uint32_t n_limit) {
+    const unsigned long long tau = st->tau_key;
+    uint32_t n = sel->n;
+    if (n > n_limit) n = n_limit;
+    const int lane = threadIdx.x & 31;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        bool keep = false;
+        Cand c;
+        if (i < n) {
+            c = in[i];
+            keep = c.key >= tau;
+        }
+        const unsigned ball = __ballot_sync(0xffffffffu, keep);
+        uint32_t off = 0;
+        if (lane == 0 && ball) off = atomicAdd(&sel->ncompact, (uint32_t)__popc(ball));
+        off = __shfl_sync(0xffffffffu, off, 0);
+        if (keep) out[off + __popc(ball & ((1u << lane) - 1u))] = c;
+    }
+}
+
+__global__ void set_count_kernel(ScanState *st, const SelState *sel) {
+    st->count = sel->ncompact;
+    st->overflow = 0u;
+}
+
+// k-th largest key of the first min(count, cap) candidates (or n_override) ->
+// tau_key, then compaction of the first n_compact candidates into `out`.
+cudaError_t run_select_compact(Cand *in, Cand *out, ScanState *st, void *sel_raw, uint32_t cap,
+                               uint32_t k, int n_override, uint32_t n_compact, int objective,
+                               float lp_margin, int num_sms, cudaStream_t stream) {
+    SelState *sel = static_cast<SelState *>(sel_raw);
+    sel_init_kernel<<<1, 256, 0, stream>>>(st, sel, cap, k, n_override);
+    const int grid = num_sms * 4;
+    for (int shift = 56; shift >= 0; shift -= 8) {
+        sel_hist_kernel<<<grid, 256, 0, stream>>>(in, sel, shift);
+        sel_pick_kernel<<<1, 32, 0, stream>>>(sel, shift);
+    }
+    sel_apply_kernel<<<1, 1, 0, stream>>>(st, sel, objective, lp_margin);
+    // compaction reads sel->n (= entries examined); limit to n_compact
+    compact_kernel<<<grid, 256, 0, stream>>>(in, out, st, sel, n_compact);
+    set_count_kernel<<<1, 1, 0, stream>>>(st, sel);
+    return cudaGetLastError();
+}
+
+size_t sel_state_bytes() { return sizeof(SelState); }
+
+}  // namespace gepi

@@ -1,0 +1,222 @@
+/*
+ * gepi.h -- C ABI of the GB300-native pairwise Boolean epistasis scan.
+ *
+ * This is the drop-in boundary for gEpiCount's `proc_gpu` path.  Every entry
+ * point takes plain pointers and sizes, returns a gepi_status, and never
+ * throws.  Reference interfaces replaced (paths are inside the gEpiCount
+ * project):
+ *
+ *   process_gpu_1(PlinkReader<ui8>*, InteractionResult*, const _paramP1&)
+ *       src/proc_gpu.h:271, src/kernels/kernel1.cu:508-511
+ *       -> gepi_process_gpu_1()  (same inputs as plain arrays, same output)
+ *   InteractionResult                 inc/gEpiCount.h:75-82  -> gepi_result
+ *   struct _paramP1                   inc/gEpiCount.h:116-132 -> gepi_params
+ *   BinaryFunction / FitnessFunction  inc/gEpiCount.h:58-73
+ *   float fisher_pval(int,int,int,int)  inc/gEpiCount.h:137-139,
+ *       src/misc/fisher_p.c:52-76     -> gepi_fisher_pval()
+ *   BinPlinkReader::checkConsistency/readData
+ *       src/reader/BinPlinkReader.h:58-244 -> gepi_plink_open() (host parse)
+ *       + gepi_planes_from_bed() (2-bit decode on the device)
+ *   allocSendData_device  src/kernels/setup1.h:72-102 -> gepi_planes_from_rows()
+ *
+ * Threading: a handle (gepi_planes) may be used by one host thread at a time.
+ * All calls are synchronous on return unless stated otherwise.
+ */
+#ifndef GEPI_H_
+#define GEPI_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GEPI_ABI_VERSION 1
+
+typedef enum gepi_status {
+    GEPI_OK = 0,
+    GEPI_ERR_ARG = 1,          /* invalid argument (null pointer, bad size, ...)     */
+    GEPI_ERR_IO = 2,           /* file missing / unreadable                          */
+    GEPI_ERR_FORMAT = 3,       /* bad .bed magic / size mismatch / unparsable text   */
+    GEPI_ERR_CUDA = 4,         /* CUDA runtime error (message via gepi_last_error)   */
+    GEPI_ERR_OOM = 5,          /* device memory admission failed                     */
+    GEPI_ERR_NOCLASS = 6,      /* phenotype class 1 or 2 has no sample               */
+    GEPI_ERR_TIMEOUT = 7,      /* a bounded device wait ran out                      */
+    GEPI_ERR_UNSUPPORTED = 8,  /* option not available on this device / build       */
+    GEPI_ERR_LIMIT = 9         /* request beyond a documented maximum                */
+} gepi_status;
+
+/* Boolean functions, same values as BinaryFunction (inc/gEpiCount.h:58-66). */
+enum { GEPI_AND = 0, GEPI_NAND = 1, GEPI_ANDN = 2, GEPI_NANDN = 3, GEPI_XOR = 4 };
+/* Objective, same values as FitnessFunction (inc/gEpiCount.h:68-73). */
+enum { GEPI_ENTROPY = 0, GEPI_FISHER = 1 };
+/* Counting method. */
+enum { GEPI_METHOD_AUTO = 0, GEPI_METHOD_POPC = 1, GEPI_METHOD_TENSOR = 2 };
+
+/* One ranked interaction.  Byte layout identical to InteractionResult
+ * (inc/gEpiCount.h:75-82, sizeof 48, int4 aligned at offset 16):
+ *   sA, sB : allele-row indices (row 2s = .bim column-5 allele carrier,
+ *            row 2s+1 = column-6 allele carrier), sB <= sA
+ *   n      : {w = on count class 1 (controls), x = on count class 2 (cases),
+ *             y = valid count class 1,          z = valid count class 2}
+ *   ent    : objective, ascending = best.  Entropy: -I(F;C) in bits.
+ *            Fisher: log10 of the two-sided p-value.
+ *   fun    : GEPI_AND .. GEPI_XOR */
+typedef struct gepi_result {
+    int32_t sA;
+    int32_t sB;
+    int32_t _pad0[2];
+    int32_t n[4];
+    float ent;
+    char fun;
+    char _pad1[11];
+} gepi_result;
+
+/* Scan parameters: the subset of struct _paramP1 (inc/gEpiCount.h:116-132)
+ * that changes results, plus the new knobs. */
+typedef struct gepi_params {
+    int32_t gpu_num;        /* -G  : CUDA device ordinal                           */
+    int32_t topmost;        /* -N  : length of the ranked list                     */
+    int32_t objective;      /* -f  : GEPI_ENTROPY / GEPI_FISHER                     */
+    int32_t method;         /* GEPI_METHOD_*                                        */
+    int32_t verbose;        /* 0 silent, 1 progress lines on stderr                 */
+    int32_t reserved[7];
+} gepi_params;
+
+/* Opaque device-resident genotype bit-planes (one cohort). */
+typedef struct gepi_planes gepi_planes;
+
+/* Host-side PLINK fileset, parsed with BinPlinkReader semantics. */
+typedef struct gepi_plink gepi_plink;
+
+/* ---- status / version ---------------------------------------------------- */
+const char *gepi_status_string(gepi_status s);
+/* Last error message of the calling thread ("" if none). */
+const char *gepi_last_error(void);
+int gepi_abi_version(void);
+
+/* ---- host PLINK reader (replaces BinPlinkReader/PlinkReader host parsing) -- */
+/* Parses BASE.fam / BASE.bim and maps BASE.bed (checkConsistency semantics:
+ * magic 6c 1b, size == (rows/2)*ceil(samples/4)+3).  Rows = 2 x .bim lines. */
+gepi_status gepi_plink_open(const char *base, gepi_plink **out);
+void gepi_plink_close(gepi_plink *p);
+int gepi_plink_num_rows(const gepi_plink *p);        /* numSNPs(): 2 x .bim lines */
+int gepi_plink_num_samples(const gepi_plink *p);     /* numSamples()              */
+int gepi_plink_elements_snp(const gepi_plink *p);    /* elementsSNP(): 64-bit words */
+const uint8_t *gepi_plink_bed(const gepi_plink *p, size_t *nbytes); /* whole .bed */
+const int32_t *gepi_plink_phenotypes(const gepi_plink *p); /* .fam column 6       */
+/* .fam info of sample i: name (first field), sex, phenotype. */
+gepi_status gepi_plink_sample_info(const gepi_plink *p, int i, const char **name, int *sex,
+                                   int *phenotype);
+/* .bim info of allele row r: id, allele char, chromosome, position. */
+gepi_status gepi_plink_row_info(const gepi_plink *p, int row, const char **id,
+                                char *allele, int *chr, int *pos);
+/* Host decode to the reference's row-major ui8 bit-planes (BitData/ValidData,
+ * BinPlinkReader.h:101-244) and class masks (PlinkReader.h:408-440); for the
+ * process_gpu_1 view and for tests.  Arrays are rows x words, words =
+ * elementsSNP(); masks have `words` entries. */
+gepi_status gepi_plink_decode_rows(const gepi_plink *p, uint64_t *bits, uint64_t *valid,
+                                   uint64_t *mask1, uint64_t *mask2);
+
+/* ---- device genotype planes ---------------------------------------------- */
+/* Upload a whole .bed file image (header included) and decode it on the device
+ * into class-sorted bit-planes.  phenotype[i] is .fam column 6 of sample i;
+ * samples with phenotype 1 form class 0 (controls, CLASS0), phenotype 2 class 1
+ * (cases, CLASS1); all other samples are left out of every count. */
+gepi_status gepi_planes_from_bed(const uint8_t *bed, size_t bed_bytes, int n_bim_snps,
+                                 int n_samples, const int32_t *phenotype, int device,
+                                 gepi_planes **out);
+/* Build planes from the reference reader's host arrays (BitData, ValidData:
+ * rows x words ui8, row-major; class masks mask1 (phenotype 1) and mask2
+ * (phenotype 2), `words` entries each).  n_rows must be even. */
+gepi_status gepi_planes_from_rows(const uint64_t *bits, const uint64_t *valid, int n_rows,
+                                  int n_words, const uint64_t *mask1, const uint64_t *mask2,
+                                  int device, gepi_planes **out);
+void gepi_planes_destroy(gepi_planes *pl);
+int gepi_planes_num_snps(const gepi_planes *pl);
+/* Samples per class (class 0 = phenotype 1, class 1 = phenotype 2). */
+gepi_status gepi_planes_class_sizes(const gepi_planes *pl, int *n0, int *n1);
+
+/* ---- the scan ------------------------------------------------------------ */
+/* All-pairs scan over allele rows rB <= rA of 5 Boolean functions; writes the
+ * `k` best results, ascending by ent with ties broken by (sA, sB, fun)
+ * ascending.  Slots beyond the number of tests with a non-zero association
+ * are zero-filled (the reference's zeroed tops, gEpiCount.cpp:81-82). */
+gepi_status gepi_scan(gepi_planes *pl, const gepi_params *par, gepi_result *tops, int k);
+
+/* Range request: SNP ranges [a0, a0+na) x [b0, b0+nb) (.bim SNP indices).
+ * Tests every allele-row pair (rA, rB) with rA in the A range, rB in the B
+ * range and rB <= rA, once.  The whole-genome scan is a0=b0=0, na=nb=N. */
+gepi_status gepi_scan_range(gepi_planes *pl, const gepi_params *par, int a0, int na,
+                            int b0, int nb, gepi_result *tops, int k);
+
+/* Per-SNP-pair Gram counts, for verification: for every s in [a0,a0+na),
+ * t in [b0,b0+nb) writes 18 uint32 at out[((s-a0)*nb + (t-b0))*18]:
+ * class c (0,1) x planes (p,q) in {A-carrier row, a-carrier row, valid}^2,
+ * index c*9 + p*3 + q, counting samples of class c with plane p of SNP s and
+ * plane q of SNP t both set.  method: GEPI_METHOD_POPC or _TENSOR. */
+gepi_status gepi_pair_counts(gepi_planes *pl, int method, int a0, int na, int b0, int nb,
+                             uint32_t *out);
+
+/* Timing and work counters of the last gepi_scan / gepi_scan_range on `pl`,
+ * measured with CUDA events on the library's stream. */
+typedef struct gepi_scan_stats {
+    double scan_ms;           /* device time from first to last launch of the scan      */
+    double count_ms;          /* summed device time of the counting launches            */
+    double max_count_ms;      /* longest counting launch                                */
+    int32_t count_launches;   /* counting-kernel launches (one per batch)               */
+    int32_t other_launches;   /* select / compaction launches                           */
+    int32_t batches;          /* batches completed                                      */
+    int32_t overflows;        /* batches retried after a candidate-buffer overflow      */
+    uint64_t snp_pairs;       /* SNP pairs s > t tested (pair-tests)                    */
+    uint64_t diag_snps;       /* SNPs whose same-SNP allele-row pairs were tested        */
+    uint64_t tiles;           /* SNP tile pairs processed                               */
+    uint64_t candidates;      /* candidates left for the final host sort                */
+    int32_t method;           /* GEPI_METHOD_POPC or GEPI_METHOD_TENSOR actually used   */
+    int32_t tile_snps;        /* SNPs per tile side                                     */
+} gepi_scan_stats;
+gepi_status gepi_last_scan_stats(const gepi_planes *pl, gepi_scan_stats *out);
+
+/* ---- drop-in for the reference's process_gpu_1 ----------------------------- */
+/* Same inputs as process_gpu_1 reads from its PlinkReader (BitData, ValidData,
+ * numSNPs() = n_rows, elementsSNP() = n_words, classData(1|2)->mask()), same
+ * output: tops[par->topmost] filled ascending.  tops must be zeroed by the
+ * caller as gEpiCount.cpp:81-82 does. */
+gepi_status gepi_process_gpu_1(const uint64_t *bits, const uint64_t *valid, int n_rows,
+                               int n_words, const uint64_t *mask1, const uint64_t *mask2,
+                               gepi_result *tops, const gepi_params *par);
+
+/* ---- host scoring helpers -------------------------------------------------- */
+/* Two-sided Fisher exact test, log10(p) as float; replaces fisher_pval()
+ * (src/misc/fisher_p.c:52-76), argument order (n11, n12, n21, n22). */
+float gepi_fisher_pval(int n11, int n12, int n21, int n22);
+/* Same test in double. */
+double gepi_fisher_log10p(int n11, int n12, int n21, int n22);
+
+/* ---- seeded synthetic PLINK data -------------------------------------------- */
+typedef struct gepi_synth_spec {
+    int32_t n_snps;          /* .bim lines                                          */
+    int32_t n_cases;         /* phenotype 2                                         */
+    int32_t n_controls;      /* phenotype 1                                         */
+    double maf_lo, maf_hi;   /* per-SNP minor allele frequency ~ U(maf_lo, maf_hi)  */
+    double missing;          /* i.i.d. missing-call probability                     */
+    int32_t n_planted;       /* interacting SNP pairs with a case-risk effect        */
+    double odds_ratio;       /* planted effect size                                 */
+    uint64_t seed;
+} gepi_synth_spec;
+
+/* Size in bytes of the .bed image gepi_synth_bed writes. */
+size_t gepi_synth_bed_bytes(const gepi_synth_spec *spec);
+/* Writes the .bed image (header included), phenotype[n_cases+n_controls]
+ * (1 or 2) and, if planted != NULL, planted[2*n_planted] SNP indices. */
+gepi_status gepi_synth_bed(const gepi_synth_spec *spec, uint8_t *bed, int32_t *phenotype,
+                           int32_t *planted);
+/* Writes BASE.bed/.bim/.fam for the same data. */
+gepi_status gepi_synth_write(const gepi_synth_spec *spec, const char *base);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GEPI_H_ */

@@ -1,0 +1,219 @@
+"""GPU parity: the CUDA scan through the C ABI against the CPU oracle.
+
+Integer work (Gram counts, contingency counts, row/function indices, the
+ranked order) must be bit-exact.  Entropy scores are bit-exact too: both sides
+rank by the same fixed-point key and round it to float the same way.  Fisher
+p-values must agree within 1e-9 relative (|d ln p| <= 1e-9).
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+
+import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+FISHER_RTOL = 1e-9  # on p: |d ln p| <= 1e-9
+
+
+def make_planes(gepi, spec_kw, tmp_path, name="c"):
+    spec = gepi.SynthSpec(**spec_kw)
+    base = str(tmp_path / name)
+    gepi.synth_write(spec, base)
+    fs = H.read_fileset(base)
+    rows = H.decode_rows(fs)
+    pl = gepi.Planes.from_bed(fs.bed, fs.n_lines, fs.pheno)
+    return pl, rows, fs, base
+
+
+def items_of(tops):
+    return [(int(t["sA"]), int(t["sB"]), int(t["fun"])) for t in tops]
+
+
+def assert_same_topk(got, want):
+    assert got.shape == want.shape
+    for i in range(got.size):
+        g, w = got[i], want[i]
+        gi = (int(g["sA"]), int(g["sB"]), int(g["fun"]), tuple(int(v) for v in g["n"]))
+        wi = (int(w["sA"]), int(w["sB"]), int(w["fun"]), tuple(int(v) for v in w["n"]))
+        assert gi == wi, f"rank {i}: gpu {gi} oracle {wi}"
+        assert np.float32(g["ent"]).tobytes() == np.float32(w["ent"]).tobytes(), (
+            f"rank {i}: ent {g['ent']!r} vs {w['ent']!r}")
+
+
+SHAPES = [
+    dict(n_snps=33, n_cases=31, n_controls=32, missing=0.02, seed=63),     # 63 samples
+    dict(n_snps=64, n_cases=32, n_controls=32, missing=0.02, seed=64),     # 64
+    dict(n_snps=65, n_cases=33, n_controls=32, missing=0.10, seed=65),     # 65
+    dict(n_snps=70, n_cases=100, n_controls=29, missing=0.05, seed=129),   # class pad
+    dict(n_snps=40, n_cases=1, n_controls=1, missing=0.0, seed=2),         # 1 + 1 samples
+    dict(n_snps=45, n_cases=700, n_controls=1500, missing=0.3, seed=7),    # >1 K chunk
+]
+
+
+@pytest.mark.parametrize("kw", SHAPES, ids=[f"s{k['n_cases'] + k['n_controls']}" for k in SHAPES])
+def test_pair_counts_bit_exact(gepi, tmp_path, kw):
+    pl, rows, fs, _ = make_planes(gepi, kw, tmp_path)
+    N = fs.n_lines
+    got = pl.pair_counts(0, N, 0, N)
+    want = H.oracle_pair_gram(rows, 0, N, 0, N)
+    assert np.array_equal(got, want)
+    # an unaligned sub-rectangle crossing tile boundaries
+    a0, na, b0, nb = 3, min(N - 3, 37), 1, min(N - 1, 33)
+    got = pl.pair_counts(a0, na, b0, nb)
+    assert np.array_equal(got, H.oracle_pair_gram(rows, a0, na, b0, nb))
+    pl.close()
+
+
+def test_rows_path_matches_bed_path(gepi, tmp_path):
+    kw = dict(n_snps=50, n_cases=90, n_controls=77, missing=0.04, seed=21)
+    pl, rows, fs, _ = make_planes(gepi, kw, tmp_path)
+    bits, valid, m1, m2 = rows
+    pr = gepi.Planes.from_rows(bits, valid, m1, m2)
+    assert pr.class_sizes() == pl.class_sizes() == (77, 90)
+    assert np.array_equal(pr.pair_counts(0, 50, 0, 50), pl.pair_counts(0, 50, 0, 50))
+    pr.close()
+    pl.close()
+
+
+@pytest.mark.parametrize("name", ["cfg1", "s63", "s64", "s65", "s129", "miss50", "cfg2_small"])
+def test_scan_entropy_matches_oracle_and_gold(gepi, tmp_path, name):
+    doc = H.load_golden(name)
+    base = H.golden_input(doc, str(tmp_path))
+    fs = H.read_fileset(base)
+    rows = H.decode_rows(fs)
+    k = doc["k"]
+    with gepi.Planes.from_bed(fs.bed, fs.n_lines, fs.pheno) as pl:
+        got = pl.scan(k)
+    want, keys, nranked = H.oracle_topk(rows, k)
+    assert_same_topk(got, want)
+    if nranked >= k:
+        gold = doc["rows"]
+        gold_items = [(r["sA"], r["sB"], r["fun"]) for r in gold]
+        gold_keys = [k_ for k_, _ in H.exact_keys(rows, gold_items)]
+        probs = H.compare_ranked(items_of(got), [-float(v) for v in keys], gold_items, gold_keys,
+                                 k, rtol=2e-5)
+        assert not probs, probs[:5]
+
+
+def test_scan_is_deterministic(gepi, tmp_path):
+    kw = dict(n_snps=300, n_cases=400, n_controls=350, missing=0.02, seed=77)
+    pl, rows, fs, _ = make_planes(gepi, kw, tmp_path)
+    a = pl.scan(500)
+    b = pl.scan(500)
+    assert a.tobytes() == b.tobytes()
+    pl.close()
+
+
+@pytest.mark.parametrize("cap", ["4096", "20000"])
+def test_scan_exact_under_candidate_overflow(gepi, tmp_path, cap, monkeypatch):
+    """A tiny candidate buffer forces overflow, select, compaction and batch
+    retries; the result must stay exact."""
+    kw = dict(n_snps=200, n_cases=150, n_controls=170, missing=0.03, seed=31)
+    pl, rows, fs, _ = make_planes(gepi, kw, tmp_path)
+    monkeypatch.setenv("GEPI_DEBUG_CAP", cap)
+    got = pl.scan(300)
+    monkeypatch.delenv("GEPI_DEBUG_CAP")
+    want, _, _ = H.oracle_topk(rows, 300)
+    assert_same_topk(got, want)
+    pl.close()
+
+
+def test_k_beyond_ranked_tests_zero_pads(gepi, tmp_path):
+    kw = dict(n_snps=3, n_cases=4, n_controls=3, missing=0.0, seed=12)
+    pl, rows, fs, _ = make_planes(gepi, kw, tmp_path)
+    k = 100  # 5 * 6 * 7 / 2 = 105 tests, many with zero association
+    got = pl.scan(k)
+    want, _, nranked = H.oracle_topk(rows, k)
+    assert nranked < k
+    assert_same_topk(got, want)
+    assert all(int(t["sA"]) == 0 and int(t["n"][2]) == 0 for t in got[nranked:])
+    pl.close()
+
+
+@pytest.mark.parametrize("rng_", [(0, 40, 0, 40), (40, 60, 5, 50), (90, 30, 0, 120), (7, 1, 7, 1)])
+def test_scan_range_matches_oracle(gepi, tmp_path, rng_):
+    kw = dict(n_snps=120, n_cases=160, n_controls=140, missing=0.02, seed=41)
+    pl, rows, fs, _ = make_planes(gepi, kw, tmp_path)
+    a0, na, b0, nb = rng_
+    got = pl.scan_range(a0, na, b0, nb, 200)
+    want, _, _ = H.oracle_topk_range(rows, 2 * a0, 2 * (a0 + na), 2 * b0, 2 * (b0 + nb), 200)
+    assert_same_topk(got, want)
+    pl.close()
+
+
+def test_process_gpu_1_dropin(gepi, tmp_path):
+    """process_gpu_1 with the reference reader's host arrays."""
+    spec = gepi.SynthSpec(n_snps=150, n_cases=120, n_controls=130, missing=0.02, seed=55)
+    base = str(tmp_path / "p")
+    gepi.synth_write(spec, base)
+    r = gepi.BinPlinkReader(base)
+    assert r.checkConsistency() and r.readData()
+    par = gepi.Params(topmost=250)
+    tops = np.zeros(250, dtype=gepi.RESULT_DTYPE)
+    gepi.process_gpu_1(r, tops, par)
+    want, _, _ = H.oracle_topk((r.BitData(), r.ValidData(), r.classMask(1), r.classMask(2)), 250)
+    assert_same_topk(tops, want)
+
+
+@pytest.mark.parametrize("kw", [
+    dict(n_snps=60, n_cases=70, n_controls=65, missing=0.02, seed=81),
+    dict(n_snps=40, n_cases=300, n_controls=420, missing=0.05, n_planted=2, seed=82),
+])
+def test_scan_fisher_matches_oracle(gepi, tmp_path, kw):
+    pl, rows, fs, _ = make_planes(gepi, kw, tmp_path)
+    k = 150
+    got = pl.scan(k, objective=gepi.FISHER)
+    want, keys, nranked = H.oracle_topk(rows, k, objective=1)
+    assert nranked >= k
+    # values: every returned test re-scored by the oracle within tolerance
+    items = items_of(got)
+    ex = H.exact_keys(rows, items, objective=1)
+    worst = 0.0
+    for t, (key, n) in zip(got, ex):
+        assert tuple(int(v) for v in t["n"]) == n
+        want_l10 = -key
+        d = abs(float(t["ent"]) - want_l10)
+        assert d <= 2e-7 * abs(want_l10) + 1e-30  # float rounding of the output
+    # ranked lists identical up to near-ties within the Fisher tolerance
+    got_keys = [k_ for k_, _ in ex]
+    probs = H.compare_ranked(items, got_keys, items_of(want), [-float(v) for v in keys], k,
+                             rtol=FISHER_RTOL * 10)
+    assert not probs, probs[:5]
+    pl.close()
+
+
+def test_config2_scale_properties(gepi):
+    """BASELINE config 2 (20,000 SNPs x 4,000 samples, 3 planted pairs, top
+    1,000): size-independent checks -- every returned count and key is the
+    oracle's, the list is sorted under the tie-break, and no sampled test beats
+    the k-th entry without being listed."""
+    spec = gepi.SynthSpec(n_snps=20000, n_cases=2000, n_controls=2000, maf_lo=0.01, maf_hi=0.5,
+                          missing=0.01, n_planted=3, odds_ratio=2.0, seed=1002)
+    bed, ph, planted = gepi.synth_bed(spec)
+    fs = H.Fileset(bed=bed, pheno=ph, n_lines=spec.n_snps, bim=[])
+    rows = H.decode_rows(fs)
+    k = 1000
+    with gepi.Planes.from_bed(bed, spec.n_snps, ph) as pl:
+        got = pl.scan(k)
+    items = items_of(got)
+    ex = H.exact_keys(rows, items)
+    keys = []
+    for t, (key, n) in zip(got, ex):
+        assert tuple(int(v) for v in t["n"]) == n
+        assert np.float32(-key) == np.float32(t["ent"])
+        keys.append(key)
+    order = sorted(range(k), key=lambda i: (-keys[i], items[i]))
+    assert order == list(range(k))
+    kth = keys[-1]
+    listed = set(items)
+    rs = np.random.default_rng(5)
+    R = 2 * spec.n_snps
+    sample = []
+    for _ in range(20000):
+        a, b = sorted(int(v) for v in rs.integers(0, R, size=2))
+        sample.append((b, a, int(rs.integers(0, 5))))
+    for (key, _), it in zip(H.exact_keys(rows, sample), sample):
+        assert key < kth or it in listed or key == kth

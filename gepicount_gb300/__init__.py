@@ -25,7 +25,7 @@ import numpy as np
 
 __all__ = [
     "GepiError", "RESULT_DTYPE", "FUNC_NAMES", "Params", "BinPlinkReader", "Planes",
-    "process_gpu_1", "fisher_pval", "fisher_log10p", "SynthSpec", "synth_bed", "synth_write",
+    "process_gpu_1", "process_gpu_1_noalloc", "fisher_pval", "fisher_log10p", "SynthSpec", "synth_bed", "synth_write",
     "library_path", "lib",
 ]
 
@@ -126,6 +126,7 @@ def lib():
     L.gepi_pair_counts.argtypes = [P, i32, i32, i32, i32, i32, P]
     L.gepi_process_gpu_1.argtypes = [P, P, i32, i32, P, P, P, ctypes.POINTER(_Params)]
     L.gepi_last_scan_stats.argtypes = [P, ctypes.POINTER(_ScanStats)]
+    L.gepi_process_gpu_1_noalloc.argtypes = [P, P, i32, i32, P, P, P, ctypes.POINTER(_Params)]
     L.gepi_fisher_pval.argtypes = [i32, i32, i32, i32]
     L.gepi_fisher_pval.restype = ctypes.c_float
     L.gepi_fisher_log10p.argtypes = [i32, i32, i32, i32]
@@ -137,7 +138,7 @@ def lib():
     for f in ("gepi_plink_open", "gepi_plink_row_info", "gepi_plink_decode_rows",
               "gepi_planes_from_bed", "gepi_planes_from_rows", "gepi_planes_class_sizes",
               "gepi_scan", "gepi_scan_range", "gepi_pair_counts", "gepi_process_gpu_1",
-              "gepi_last_scan_stats",
+              "gepi_last_scan_stats", "gepi_process_gpu_1_noalloc",
               "gepi_synth_bed", "gepi_synth_write"):
         getattr(L, f).restype = i32
     _lib = L
@@ -365,6 +366,21 @@ def process_gpu_1(pr: BinPlinkReader, tops: np.ndarray, par: Params) -> None:
         raise GepiError(1, "reader has no data (call readData first)")
     _check(lib().gepi_process_gpu_1(_ptr(bits), _ptr(valid), bits.shape[0], bits.shape[1],
                                     _ptr(m1), _ptr(m2), _ptr(tops), ctypes.byref(par._c())))
+
+
+def process_gpu_1_noalloc(pr: BinPlinkReader, tops: np.ndarray, par: Params) -> None:
+    """process_gpu_1 for hosts that cannot allocate device memory: every
+    device buffer comes from the library's fixed 32 MiB scratch array (see
+    gepi_process_gpu_1_noalloc in include/gepi.h for limits and sharing)."""
+    if tops.dtype != RESULT_DTYPE or tops.size < par.topmost:
+        raise GepiError(1, "tops must be a RESULT_DTYPE array of length >= topmost")
+    bits, valid = pr.BitData(), pr.ValidData()
+    m1, m2 = pr.classMask(1), pr.classMask(2)
+    if bits is None or m1 is None or m2 is None:
+        raise GepiError(1, "reader has no data (call readData first)")
+    _check(lib().gepi_process_gpu_1_noalloc(_ptr(bits), _ptr(valid), bits.shape[0],
+                                            bits.shape[1], _ptr(m1), _ptr(m2), _ptr(tops),
+                                            ctypes.byref(par._c())))
 
 
 def fisher_pval(n11: int, n12: int, n21: int, n22: int) -> float:

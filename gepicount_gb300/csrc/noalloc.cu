@@ -1,0 +1,396 @@
+// gepi_process_gpu_1_noalloc: the process_gpu_1 scan for callers that cannot
+// allocate device memory.
+//
+// Some hosts own every byte of GPU memory through their own pool or caching
+// allocator (a framework plugin, a database operator, a process that must not
+// grow its footprint after start-up) and forbid cudaMalloc/cudaFree from
+// libraries they load.  This entry point serves them: the caller passes the
+// same host inputs and host output as gepi_process_gpu_1, and every device
+// buffer the scan needs -- uploaded rows, class permutation, genotype planes,
+// scoring tables, tile list, candidate buffers, scan state, output records --
+// is carved from ONE file-scope device array, g_noalloc_scratch, of
+// kNoAllocScratchBytes (32 MiB).  Every GPU that loads the library holds that
+// array until the process exits.  No cudaMalloc, cudaFree, cudaMallocHost,
+// stream or event creation and no host heap allocation happen on this path:
+// tables and the class permutation are built by kernels, the final ranking is
+// done on the device, and only the k result records are copied back.
+//
+// Limits: the inputs, planes and tables must fit the array next to the
+// candidate buffers (two buffers of kNoAllocCap = 65,536 records), and
+// k <= kNoAllocCap / 4; larger requests return GEPI_ERR_LIMIT before any
+// device work.
+//
+// Set-up: the first call on a device, with that device current, looks up the
+// array's device address with cudaGetSymbolAddress (the host-side symbol is
+// only a stand-in and must not be passed to a kernel).  Make that first call
+// before any stream capture.
+//
+// Sharing: every call on a device uses the same array and finds the previous
+// call's contents there; the call initialises everything it reads (scan state,
+// select state, planes, tables, output records).  Calls that overlap on the
+// same GPU (from several host threads) race on the array and must be
+// serialised by the caller.  Work is issued on the legacy default stream and
+// the call returns after it completes.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+
+#include "common.h"
+#include "device.cuh"
+#include "tables.h"
+
+namespace gepi {
+
+cudaError_t launch_decode_rows(const uint64_t *bits, const uint64_t *valid, int nw, int n_snps,
+                               const int32_t *perm, int Wp, uint32_t *planes,
+                               cudaStream_t stream, int num_sms);
+cudaError_t launch_popc_tiles(const uint32_t *planes, int Wp, int W0, const int2 *tiles,
+                              int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
+                              uint32_t *dump, cudaStream_t stream);
+cudaError_t run_select_compact(Cand *in, Cand *out, ScanState *st, void *sel, uint32_t cap,
+                               uint32_t k, int n_override, uint32_t n_compact, int objective,
+                               float lp_margin, int num_sms, cudaStream_t stream);
+size_t sel_state_bytes();
+int popc_tile_snps();
+
+constexpr size_t kNoAllocScratchBytes = 32ull << 20;
+constexpr uint32_t kNoAllocCap = 65536;
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace {
+
+std::mutex g_setup_mu;
+unsigned char *g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of the scratch array on `dev` (looked up once per device).
+gepi_status scratch_address(int dev, unsigned char **out) {
+    if (dev < 0 || dev >= kMaxDevices) return set_error(GEPI_ERR_ARG, "device ordinal out of range");
+    std::lock_guard<std::mutex> lk(g_setup_mu);
+    if (!g_scratch_ptr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess)
+            return set_error(GEPI_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        g_scratch_ptr[dev] = static_cast<unsigned char *>(p);
+    }
+    *out = g_scratch_ptr[dev];
+    return GEPI_OK;
+}
+
+// Bump allocator over the scratch array (offsets only; nothing is allocated).
+struct Carve {
+    size_t used = 0;
+    size_t take(size_t bytes) {
+        size_t off = used;
+        used += (bytes + 255) & ~size_t(255);
+        return off;
+    }
+};
+
+// Same integer log2 as the host table builder (tables.cpp): 64 fraction bits
+// by repeated squaring of the Q1.63 mantissa, truncating each square.
+__device__ uint64_t na_log2_fixed(uint64_t n, int F) {
+    if (n <= 1) return 0;
+    const int e = 63 - __clzll((long long)n);
+    uint64_t x = n << (63 - e);
+    uint64_t frac = 0;
+    for (int i = 1; i <= 64; ++i) {
+        const uint64_t hi = __umul64hi(x, x), lo = x * x;
+        if (hi >> 63) {
+            x = hi;
+            frac |= 1ull << (64 - i);
+        } else {
+            x = (hi << 1) | (lo >> 63);
+        }
+    }
+    const uint64_t r = (frac >> (64 - F)) + ((frac >> (63 - F)) & 1ull);
+    return ((uint64_t)e << F) + r;
+}
+
+__global__ void na_tables_kernel(uint64_t *T, double *lf, float *lf32, int nmax, int F) {
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n <= nmax; n += gridDim.x * blockDim.x) {
+        T[n] = (uint64_t)n * na_log2_fixed((uint64_t)n, F);
+        const double v = lgamma((double)n + 1.0);
+        lf[n] = v;
+        lf32[n] = (float)v;
+    }
+}
+
+// Class-sorted permutation from the two class masks (one block): slot j of
+// class 0 is the j-th sample (in file order) of mask1, class 1 starts at
+// word W0; every other slot is -1.
+__global__ void na_perm_kernel(const uint64_t *m1, const uint64_t *m2, int nw, int W0, int Wp,
+                               int32_t *perm) {
+    __shared__ int base[2][1024];
+    const int nslots = Wp * 32;
+    for (int i = threadIdx.x; i < nslots; i += blockDim.x) perm[i] = -1;
+    const int per = (nw + blockDim.x - 1) / blockDim.x;
+    const int w0 = threadIdx.x * per, w1 = min(nw, w0 + per);
+    int c0 = 0, c1 = 0;
+    for (int w = w0; w < w1; ++w) {
+        c0 += __popcll(m1[w]);
+        c1 += __popcll(m2[w]);
+    }
+    base[0][threadIdx.x] = c0;
+    base[1][threadIdx.x] = c1;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int a = 0, b = 0;
+        for (int t = 0; t < (int)blockDim.x; ++t) {
+            int va = base[0][t], vb = base[1][t];
+            base[0][t] = a;
+            base[1][t] = b;
+            a += va;
+            b += vb;
+        }
+    }
+    __syncthreads();
+    int s0 = base[0][threadIdx.x], s1 = W0 * 32 + base[1][threadIdx.x];
+    for (int w = w0; w < w1; ++w) {
+        uint64_t a = m1[w], b = m2[w];
+        while (a) {
+            const int bit = __ffsll((long long)a) - 1;
+            perm[s0++] = w * 64 + bit;
+            a &= a - 1;
+        }
+        while (b) {
+            const int bit = __ffsll((long long)b) - 1;
+            perm[s1++] = w * 64 + bit;
+            b &= b - 1;
+        }
+    }
+}
+
+// Lower-triangle tile list (A tile i >= B tile j), row-major like the
+// allocating path.
+__global__ void na_tiles_kernel(int2 *tiles, int nt) {
+    const long long total = (long long)nt * (nt + 1) / 2;
+    for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < total;
+         l += (long long)gridDim.x * blockDim.x) {
+        int i = (int)((sqrt(8.0 * (double)l + 1.0) - 1.0) * 0.5);
+        while ((long long)i * (i + 1) / 2 > l) --i;
+        while ((long long)(i + 1) * (i + 2) / 2 <= l) ++i;
+        tiles[l] = make_int2(i, (int)(l - (long long)i * (i + 1) / 2));
+    }
+}
+
+__device__ __forceinline__ bool na_better(const Cand &a, const Cand &b) {
+    if (a.key != b.key) return a.key > b.key;
+    if (a.rA != b.rA) return a.rA < b.rA;
+    return a.rBfun < b.rBfun;
+}
+
+// Final ranking on the device: the rank of each survivor is the number of
+// survivors that beat it under (key desc, sA, sB, fun); ranks < k are written
+// as result records, slots with no survivor are zeroed.
+__global__ void na_rank_kernel(const Cand *cand, const ScanState *st, int k, gepi_result *out) {
+    const uint32_t n = min(st->count, kNoAllocCap);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < k; i += gridDim.x * blockDim.x)
+        if ((uint32_t)i >= n) {
+            gepi_result z;
+            memset(&z, 0, sizeof z);
+            out[i] = z;
+        }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const Cand c = cand[i];
+        uint32_t rank = 0;
+        for (uint32_t j = 0; j < n; ++j) rank += na_better(cand[j], c) ? 1u : 0u;
+        if (rank < (uint32_t)k) {
+            gepi_result r;
+            memset(&r, 0, sizeof r);
+            r.sA = c.rA;
+            r.sB = c.rBfun >> 3;
+            r.fun = (char)(c.rBfun & 7);
+            for (int q = 0; q < 4; ++q) r.n[q] = c.n[q];
+            r.ent = (float)(-value_of_key(c.key));
+            out[rank] = r;
+        }
+    }
+}
+
+}  // namespace
+}  // namespace gepi
+
+using namespace gepi;
+
+extern "C" gepi_status gepi_process_gpu_1_noalloc(const uint64_t *bits, const uint64_t *valid,
+                                                  int n_rows, int n_words, const uint64_t *mask1,
+                                                  const uint64_t *mask2, gepi_result *tops,
+                                                  const gepi_params *par) {
+    clear_error();
+    if (!bits || !valid || !mask1 || !mask2 || !tops || !par || n_rows <= 0 || (n_rows & 1) ||
+        n_words <= 0)
+        return set_error(GEPI_ERR_ARG, "gepi_process_gpu_1_noalloc: bad argument");
+    const int k = par->topmost;
+    if (k <= 0) return set_error(GEPI_ERR_ARG, "gepi_process_gpu_1_noalloc: topmost <= 0");
+    if (par->objective != GEPI_ENTROPY && par->objective != GEPI_FISHER)
+        return set_error(GEPI_ERR_ARG, "gepi_process_gpu_1_noalloc: unknown objective");
+    if (par->method == GEPI_METHOD_TENSOR)
+        return set_error(GEPI_ERR_UNSUPPORTED, "gepi_process_gpu_1_noalloc: popcount counting only");
+    const int n_snps = n_rows / 2;
+    for (int s = 0; s < n_snps; ++s)
+        if (std::memcmp(valid + (size_t)(2 * s) * n_words, valid + (size_t)(2 * s + 1) * n_words,
+                        (size_t)n_words * 8) != 0)
+            return set_error(GEPI_ERR_FORMAT, "valid rows of an allele pair differ");
+    int S0 = 0, S1 = 0;
+    for (int w = 0; w < n_words; ++w) {
+        if (mask1[w] & mask2[w]) return set_error(GEPI_ERR_FORMAT, "sample in both class masks");
+        S0 += __builtin_popcountll(mask1[w]);
+        S1 += __builtin_popcountll(mask2[w]);
+    }
+    if (S0 == 0 || S1 == 0) return set_error(GEPI_ERR_NOCLASS, "Error in class mask data");
+    const int W0 = ((S0 + kClassPadSamples - 1) / kClassPadSamples) * (kClassPadSamples / 32);
+    const int W1 = ((S1 + kClassPadSamples - 1) / kClassPadSamples) * (kClassPadSamples / 32);
+    const int Wp = W0 + W1;
+    const int nmax = S0 + S1;
+    const int T = popc_tile_snps();
+    const int nt = (n_snps + T - 1) / T;
+    const long long ntiles = (long long)nt * (nt + 1) / 2;
+
+    // Lay out the scratch array; reject requests that do not fit.
+    Carve cv;
+    const size_t o_state = cv.take(sizeof(ScanState));
+    const size_t o_sel = cv.take(sel_state_bytes());
+    const size_t o_cand0 = cv.take((size_t)kNoAllocCap * sizeof(Cand));
+    const size_t o_cand1 = cv.take((size_t)kNoAllocCap * sizeof(Cand));
+    const size_t o_out = cv.take((size_t)k * sizeof(gepi_result));
+    const size_t o_m = cv.take(2 * (size_t)n_words * 8);
+    const size_t o_bits = cv.take((size_t)n_rows * n_words * 8);
+    const size_t o_valid = cv.take((size_t)n_rows * n_words * 8);
+    const size_t o_perm = cv.take((size_t)Wp * 32 * 4);
+    const size_t o_planes = cv.take((size_t)n_snps * 3 * Wp * 4);
+    const size_t o_T = cv.take(((size_t)nmax + 1) * 8);
+    const size_t o_lf = cv.take(((size_t)nmax + 1) * 8);
+    const size_t o_lf32 = cv.take(((size_t)nmax + 1) * 4);
+    const size_t o_tiles = cv.take((size_t)ntiles * sizeof(int2));
+    if (k > (int)(kNoAllocCap / 4) || cv.used > kNoAllocScratchBytes)
+        return set_error(GEPI_ERR_LIMIT,
+                         "gepi_process_gpu_1_noalloc: needs " + std::to_string(cv.used) +
+                             " bytes of scratch and k <= " + std::to_string(kNoAllocCap / 4) +
+                             "; the fixed scratch array holds " +
+                             std::to_string(kNoAllocScratchBytes) + " bytes");
+
+    int prev = -1;
+    cudaGetDevice(&prev);
+    if (cudaSetDevice(par->gpu_num) != cudaSuccess)
+        return set_error(GEPI_ERR_CUDA, "cudaSetDevice failed");
+    struct Restore {
+        int d;
+        ~Restore() {
+            if (d >= 0) cudaSetDevice(d);
+        }
+    } restore{prev};
+    unsigned char *base = nullptr;
+    GEPI_TRY(scratch_address(par->gpu_num, &base));
+    int num_sms = 0;
+    GEPI_CUDA(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, par->gpu_num));
+    const cudaStream_t stream = 0;
+
+    ScanState *d_state = reinterpret_cast<ScanState *>(base + o_state);
+    void *d_sel = base + o_sel;
+    Cand *d_cand[2] = {reinterpret_cast<Cand *>(base + o_cand0),
+                       reinterpret_cast<Cand *>(base + o_cand1)};
+    gepi_result *d_out = reinterpret_cast<gepi_result *>(base + o_out);
+    uint64_t *d_m1 = reinterpret_cast<uint64_t *>(base + o_m), *d_m2 = d_m1 + n_words;
+    uint64_t *d_bits = reinterpret_cast<uint64_t *>(base + o_bits);
+    uint64_t *d_valid = reinterpret_cast<uint64_t *>(base + o_valid);
+    int32_t *d_perm = reinterpret_cast<int32_t *>(base + o_perm);
+    uint32_t *d_planes = reinterpret_cast<uint32_t *>(base + o_planes);
+    uint64_t *d_T = reinterpret_cast<uint64_t *>(base + o_T);
+    double *d_lf = reinterpret_cast<double *>(base + o_lf);
+    float *d_lf32 = reinterpret_cast<float *>(base + o_lf32);
+    int2 *d_tiles = reinterpret_cast<int2 *>(base + o_tiles);
+
+    // Inputs, tables, permutation, planes, tile list.
+    const size_t rb = (size_t)n_rows * n_words * 8;
+    GEPI_CUDA(cudaMemcpy(d_bits, bits, rb, cudaMemcpyHostToDevice));
+    GEPI_CUDA(cudaMemcpy(d_valid, valid, rb, cudaMemcpyHostToDevice));
+    GEPI_CUDA(cudaMemcpy(d_m1, mask1, (size_t)n_words * 8, cudaMemcpyHostToDevice));
+    GEPI_CUDA(cudaMemcpy(d_m2, mask2, (size_t)n_words * 8, cudaMemcpyHostToDevice));
+    const int F = tfix_bits(nmax);
+    na_tables_kernel<<<num_sms, 256, 0, stream>>>(d_T, d_lf, d_lf32, nmax, F);
+    GEPI_CUDA(cudaGetLastError());
+    na_perm_kernel<<<1, 1024, 0, stream>>>(d_m1, d_m2, n_words, W0, Wp, d_perm);
+    GEPI_CUDA(cudaGetLastError());
+    GEPI_CUDA(launch_decode_rows(d_bits, d_valid, n_words, n_snps, d_perm, Wp, d_planes, stream,
+                                 num_sms));
+    na_tiles_kernel<<<num_sms, 256, 0, stream>>>(d_tiles, nt);
+    GEPI_CUDA(cudaGetLastError());
+
+    ScanState st{};
+    st.tau_key = 0ull;
+    st.theta = 0.f;
+    st.lp_thr = INFINITY;
+    GEPI_CUDA(cudaMemcpy(d_state, &st, sizeof st, cudaMemcpyHostToDevice));
+
+    ScanCtx ctx;
+    ctx.T = d_T;
+    ctx.F = F;
+    ctx.lf = d_lf;
+    ctx.lf32 = d_lf32;
+    ctx.objective = par->objective;
+    ctx.cap = kNoAllocCap;
+    ctx.st = d_state;
+    const float lp_margin = 2e-6f * (float)std::lgamma((double)nmax + 1.0) + 1e-3f;
+
+    // Adaptive batches over the tile list, as in the allocating scan.
+    const double tests_per_tile = 20.0 * T * T;
+    const uint32_t budget = kNoAllocCap / 2;
+    const double pilot = par->objective == GEPI_ENTROPY ? kNoAllocCap / 4.0 : 4096.0;
+    size_t batch = (size_t)std::max(1.0, std::floor(pilot / tests_per_tile));
+    size_t t = 0;
+    uint32_t count = 0;
+    int cur = 0, retries = 0;
+    while (t < (size_t)ntiles) {
+        const size_t nbt = std::min(batch, (size_t)ntiles - t);
+        ctx.cand = d_cand[cur];
+        GEPI_CUDA(launch_popc_tiles(d_planes, Wp, W0, d_tiles + t, (int)nbt, 0, n_snps, 0, n_snps,
+                                    ctx, nullptr, stream));
+        GEPI_CUDA(cudaMemcpy(&st, d_state, sizeof st, cudaMemcpyDeviceToHost));
+        if (st.overflow) {
+            if (++retries > 64)
+                return set_error(GEPI_ERR_LIMIT, "candidate buffer keeps overflowing (massive ties)");
+            GEPI_CUDA(run_select_compact(d_cand[cur], d_cand[cur ^ 1], d_state, d_sel, kNoAllocCap,
+                                         (uint32_t)k, (int)kNoAllocCap, count, par->objective,
+                                         lp_margin, num_sms, stream));
+            cur ^= 1;
+            GEPI_CUDA(cudaMemcpy(&st, d_state, sizeof st, cudaMemcpyDeviceToHost));
+            count = st.count;
+            batch = std::max<size_t>(1, nbt / 2);
+            continue;
+        }
+        const uint32_t appended = st.count - count;
+        count = st.count;
+        t += nbt;
+        retries = 0;
+        if (count > budget && t < (size_t)ntiles) {
+            GEPI_CUDA(run_select_compact(d_cand[cur], d_cand[cur ^ 1], d_state, d_sel, kNoAllocCap,
+                                         (uint32_t)k, -1, 0xFFFFFFFFu, par->objective, lp_margin,
+                                         num_sms, stream));
+            cur ^= 1;
+            GEPI_CUDA(cudaMemcpy(&st, d_state, sizeof st, cudaMemcpyDeviceToHost));
+            count = st.count;
+        }
+        const double rate = std::max(1.0, (double)appended) / (double)nbt;
+        const double room = (double)budget - (double)count;
+        double nb_next = room > 0 ? room / rate : 1.0;
+        nb_next = std::min(nb_next, 8.0 * (double)nbt);
+        batch = (size_t)std::max(1.0, nb_next);
+    }
+    if (count > (uint32_t)k) {
+        GEPI_CUDA(run_select_compact(d_cand[cur], d_cand[cur ^ 1], d_state, d_sel, kNoAllocCap,
+                                     (uint32_t)k, -1, 0xFFFFFFFFu, par->objective, lp_margin,
+                                     num_sms, stream));
+        cur ^= 1;
+    }
+    na_rank_kernel<<<num_sms, 256, 0, stream>>>(d_cand[cur], d_state, k, d_out);
+    GEPI_CUDA(cudaGetLastError());
+    GEPI_CUDA(cudaMemcpy(tops, d_out, (size_t)k * sizeof(gepi_result), cudaMemcpyDeviceToHost));
+    return GEPI_OK;
+}

@@ -187,6 +187,22 @@ gepi_status gepi_process_gpu_1(const uint64_t *bits, const uint64_t *valid, int 
                                int n_words, const uint64_t *mask1, const uint64_t *mask2,
                                gepi_result *tops, const gepi_params *par);
 
+/* Same inputs, output and results as gepi_process_gpu_1, for callers that
+ * cannot allocate device memory (their GPU memory is owned by a pool or a
+ * framework that forbids cudaMalloc/cudaFree in libraries it loads).  It
+ * allocates nothing: all device scratch comes from one fixed 32 MiB array in
+ * device memory (held by every GPU that loads the library until exit).
+ * Requests whose rows, planes, tables and tile list do not fit next to the
+ * 2 x 65,536-record candidate buffers, or with topmost > 16,384, return
+ * GEPI_ERR_LIMIT before any device work.  The first call on a device looks up
+ * the array's device address; make it before any stream capture.  Calls share
+ * the array: overlapping calls on one GPU race and must be serialised.
+ * Popcount counting only.  This entry point has no counterpart in the
+ * reference. */
+gepi_status gepi_process_gpu_1_noalloc(const uint64_t *bits, const uint64_t *valid, int n_rows,
+                                       int n_words, const uint64_t *mask1, const uint64_t *mask2,
+                                       gepi_result *tops, const gepi_params *par);
+
 /* ---- host scoring helpers -------------------------------------------------- */
 /* Two-sided Fisher exact test, log10(p) as float; replaces fisher_pval()
  * (src/misc/fisher_p.c:52-76), argument order (n11, n12, n21, n22). */

@@ -236,6 +236,17 @@ def run_ours(args, cfg):
         wall = time.perf_counter() - t0
     dev_ms = sum(s["scan_ms"] for s in stats)
     pairs_per_scan = stats[0]["snp_pairs"]
+    # The plain popcount kernel on the same resident planes (the metric's "vs plain kernel").
+    plain = None
+    if args.plain_steps > 0 and stats[0]["method"] != g.METHOD_POPC:
+        planes.scan(k, method=g.METHOD_POPC)
+        pms = []
+        for _ in range(args.plain_steps):
+            planes.scan(k, method=g.METHOD_POPC)
+            pms.append(planes.last_stats()["scan_ms"])
+        pmean = sum(pms) / len(pms)
+        plain = {"value": world * pairs_per_scan / (pmean / 1000.0), "ms_per_step": pmean,
+                 "steps": len(pms)}
     # max over ranks of the device time
     if world > 1:
         import torch.distributed as dist
@@ -258,8 +269,9 @@ def run_ours(args, cfg):
     peaks, peak_kind = measured_peaks()
     achieved = ops_per_launch / avg_launch_s / 1e12
     peak = float(peaks.get("bf16_tflops", 1900.0))
+    kname = "tc_tile_kernel" if stats[0]["method"] == g.METHOD_TENSOR else "popc_tile_kernel"
     roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak, "traffic": None, "kernel": "popc_tile_kernel",
+            "frac": achieved / peak, "traffic": None, "kernel": kname,
             "peak_source": f"{peak_kind} dense bf16 (burst)",
             "work": "2 x 9 x samples ops per SNP pair (0/1 Gram), per launch",
             "avg_launch_ms": avg_launch_s * 1e3, "launches": nlaunch}
@@ -297,7 +309,7 @@ def run_ours(args, cfg):
             "scaling": "weak", "vs_baseline": None, "dtype": "u32",
             "data": "synthetic (seeded generator, HWE, planted pairs)",
             "config": {"workload": describe(args.config, cfg), "n_snps": spec.n_snps,
-                       "n_samples": n_samples, "k": k, "method": args.method,
+                       "n_samples": n_samples, "k": k, "method": ["auto", "popc", "tensor"][stats[0]["method"]] if args.method == "auto" else args.method,
                        "pair_tests_per_step": pairs_per_scan,
                        "boolean_tests_per_step": 5 * (2 * spec.n_snps) * (2 * spec.n_snps + 1) // 2,
                        "l2": "inputs larger than L2 (genotype planes "
@@ -306,6 +318,8 @@ def run_ours(args, cfg):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(nbytes),
                     "d2h_bytes_per_step": int(d2h), "seconds_per_step": e2e_t},
             "gpu_launches": launches,
+            "plain_kernel": plain,
+            "vs_plain": (value / plain["value"]) if plain else None,
             "roofline": roof,
             "cpu_baseline": cpu,
             "wall_s": wall,
@@ -330,6 +344,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--plain-steps", type=int, default=2,
+                    help="timed scans of the plain popcount kernel for vs_plain (0 = skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     cfg = CONFIGS[args.config]

@@ -18,28 +18,17 @@
 #include <cstdint>
 
 #include "device.cuh"
+#include "tile_common.cuh"
 
 namespace gepi {
 
-constexpr int kPopcTile = 32;
-constexpr int kPopcKC = 32;                  // words per K chunk
-constexpr int kPopcStride = kPopcKC + 4;     // padded smem row pitch (words)
-constexpr int kPopcRows = kPopcTile * 3;     // plane rows per operand
-constexpr int kPopcStages = 3;
+constexpr int kPopcTile = kTileSnps;
+constexpr int kPopcKC = kTileKC;
+constexpr int kPopcStride = kTileStride;
+constexpr int kPopcRows = kTileRows;
+constexpr int kPopcStages = kTileStages;
 constexpr int kPopcThreads = 256;
-constexpr size_t kPopcSmem = (size_t)kPopcStages * 2 * kPopcRows * kPopcStride * 4;
-
-__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src, int src_bytes) {
-    unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(gmem_src),
-                 "r"(src_bytes)
-                 : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
-}
+constexpr size_t kPopcSmem = kTileSmem;
 
 // Two consecutive words (h = word pair index in the chunk) of one class.
 template <int CLS>
@@ -87,21 +76,7 @@ __global__ void __launch_bounds__(kPopcThreads, 2)
     const uint32_t *gB = planes + (size_t)sB0 * 3 * Wp;
 
     auto load_stage = [&](int chunk, int stage) {
-        uint32_t *sA = smem + (size_t)stage * 2 * kPopcRows * kPopcStride;
-        uint32_t *sB = sA + kPopcRows * kPopcStride;
-        const int wbase = chunk * kPopcKC;
-        constexpr int per_op = kPopcRows * (kPopcKC / 4);
-#pragma unroll
-        for (int c = tid; c < 2 * per_op; c += kPopcThreads) {
-            const int op = c >= per_op;
-            const int rem = c - op * per_op;
-            const int row = rem >> 3, q = rem & 7;
-            const int w = wbase + 4 * q;
-            const bool ok = (row < (op ? nBr : nAr)) && (w < Wp);
-            const uint32_t *g = (op ? gB : gA) + (size_t)row * Wp + w;
-            uint32_t *d = (op ? sB : sA) + row * kPopcStride + 4 * q;
-            cp_async16(d, ok ? g : planes, ok ? 16 : 0);
-        }
+        load_tile_stage<kPopcThreads>(smem, planes, gA, gB, nAr, nBr, Wp, chunk, stage, tid);
     };
 
     uint32_t acc[2][2][2][9];

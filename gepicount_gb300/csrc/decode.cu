@@ -8,6 +8,11 @@
 // class 0 (phenotype 1) comes first, then class 1 (phenotype 2), each padded to
 // a multiple of 128 samples; samples of any other phenotype are dropped.
 //
+// Bit order inside a 32-sample word is nibble-transposed: sample slot k of the
+// word sits at bit 8*(k%4) + k/4.  Popcount counting is blind to the order;
+// the tensor-core counting form uses it to turn 4 consecutive samples into the
+// 4 bytes of an 8-bit MMA operand register with one shift and one AND.
+//
 // HBM-bound: reads N * ceil(S/4) bytes, writes 3 * N * Wp * 4 bytes.
 #include <cuda_runtime.h>
 
@@ -19,8 +24,9 @@ namespace gepi {
 
 // One CTA decodes `spc` consecutive SNPs whose .bed rows are staged in shared
 // memory.  Each warp produces 32 consecutive output words of one SNP at a time:
-// iteration j ballots the three plane bits of slot (w0 + j)*32 + lane; lane j
-// keeps word j, then the warp stores 32 words per plane, coalesced.
+// iteration j ballots the three plane bits of word w0 + j, lane L carrying slot
+// 4*(L%8) + L/8 of that word (bit L); lane j keeps word j, then the warp stores
+// 32 words per plane, coalesced.
 __global__ void decode_bed_kernel(const uint8_t *__restrict__ bed, size_t bps, int n_snps,
                                   const int32_t *__restrict__ perm, int Wp, int spc,
                                   uint32_t *__restrict__ planes) {
@@ -32,6 +38,7 @@ __global__ void decode_bed_kernel(const uint8_t *__restrict__ bed, size_t bps, i
     for (size_t i = threadIdx.x; i < tot; i += blockDim.x) srow[i] = __ldg(src + i);
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const int slot = 4 * (lane & 7) + (lane >> 3);  // slot whose bit is `lane`
     const int nchunks = (Wp + 31) / 32;
     for (int job = warp; job < nchunks * ns; job += nwarp) {
         const int si = job / nchunks, ch = job - si * nchunks;
@@ -41,7 +48,7 @@ __global__ void decode_bed_kernel(const uint8_t *__restrict__ bed, size_t bps, i
         for (int j = 0; j < 32; ++j) {
             const int w = w0 + j;
             if (w >= Wp) break;  // uniform across the warp
-            const int sample = __ldg(perm + (size_t)w * 32 + lane);
+            const int sample = __ldg(perm + (size_t)w * 32 + slot);
             int code = 1;
             if (sample >= 0) code = (row[sample >> 2] >> ((sample & 3) * 2)) & 3;
             const uint32_t A = __ballot_sync(0xffffffffu, code == 0 || code == 2);
@@ -72,6 +79,7 @@ __global__ void decode_rows_kernel(const uint64_t *__restrict__ bits,
                                    const int32_t *__restrict__ perm, int Wp,
                                    uint32_t *__restrict__ planes) {
     const int lane = threadIdx.x & 31;
+    const int slot = 4 * (lane & 7) + (lane >> 3);  // slot whose bit is `lane`
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarp = (gridDim.x * blockDim.x) >> 5;
     const int nchunks = (Wp + 31) / 32;
@@ -84,7 +92,7 @@ __global__ void decode_rows_kernel(const uint64_t *__restrict__ bits,
         for (int j = 0; j < 32; ++j) {
             const int w = w0 + j;
             if (w >= Wp) break;
-            const int sample = __ldg(perm + (size_t)w * 32 + lane);
+            const int sample = __ldg(perm + (size_t)w * 32 + slot);
             bool A = false, a = false, V = false;
             if (sample >= 0) {
                 const int k = sample >> 6;

@@ -7,7 +7,7 @@
 //   p = 2 : valid (non-missing) call
 // row (3s + p), words [0, W0) hold class-0 samples (phenotype 1) in file order,
 // words [W0, W0+W1) class-1 samples (phenotype 2); each class is zero-padded
-// to a multiple of 128 samples.  Row pitch Wp = W0 + W1 words (16 B multiple).
+// to a multiple of 256 samples.  Row pitch Wp = W0 + W1 words (32 B multiple).
 //
 // For SNP pair (s, t) and class c the kernels produce the 9 Gram counts
 // G[p*3+q] = popcount(plane_p(s) & plane_q(t)) over class-c words.  For allele
@@ -24,7 +24,7 @@
 namespace gepi {
 
 constexpr int kNumFuncs = 5;
-constexpr int kClassPadSamples = 128;
+constexpr int kClassPadSamples = 256;  // one tensor-core pipeline chunk
 
 // Candidate record appended by the epilogue (32 bytes).
 struct __align__(16) Cand {
@@ -42,8 +42,9 @@ struct ScanState {
     float lp_thr;                // Fisher bound: reject when log P(obs) > lp_thr (nats)
     uint32_t count;              // appended candidates (may exceed cap)
     uint32_t overflow;           // set when count went past cap
-    uint32_t exact_evals;        // tests that reached the exact path
-    uint32_t pad;
+    float tau_f;                 // entropy: tau as mutual information in bits, rounded down
+    int kerr;                    // non-zero: a counting kernel gave up a bounded wait
+    double tau_val;              // tau as a value (I bits or -log10 p); -inf: none yet
 };
 
 struct ScanCtx {
@@ -224,21 +225,32 @@ __device__ __forceinline__ void append_candidate(const ScanCtx &ctx, double valu
     ctx.cand[idx] = c;
 }
 
-// Exact evaluation of one test that passed the bound; appends if it ranks.
+// Exact evaluation of one test that passed the bounds; appends if it ranks.
+// Entropy rejects with one FP64 multiply against tau before the division.
 static __device__ __noinline__ void exact_test(const ScanCtx &ctx, int rA, int rB, int fun, int w,
                                         int x, int y, int z) {
     long long d = (long long)w * z - (long long)x * y;
     if (d == 0) return;
-    atomicAdd(&ctx.st->exact_evals, 1u);
     double value;
     if (ctx.objective == 0) {
-        value = exact_mi(ctx.T, ctx.F, w, x, y, z);
+        const int m = y + z, xx = w + x;
+        const uint64_t *T = ctx.T;
+        const uint64_t num = __ldg(T + m) + __ldg(T + w) + __ldg(T + (y - w)) + __ldg(T + x) +
+                             __ldg(T + (z - x)) - __ldg(T + xx) - __ldg(T + (m - xx)) -
+                             __ldg(T + y) - __ldg(T + z);
+        const double lhs = (double)(long long)num;
+        // num * 2^-F / m >= tau  <=>  num >= tau * m * 2^F (checked with 1e-12 slack)
+        if (lhs < ctx.st->tau_val * (double)m * scalbn(1.0, ctx.F) * (1.0 - 1e-12)) return;
+        value = scalbn(lhs, -ctx.F) / (double)m;
     } else {
         // print order (w, y-w, x, z-x); value = -log10 p
         value = -fisher_lnp(ctx.lf, w, y - w, x, z - x) * 0.43429448190325182765;
     }
     append_candidate(ctx, value, rA, rB, fun, w, x, y, z);
 }
+
+// n * log2(n) in FP32 (0 for n <= 1).
+__device__ __forceinline__ float tlog2f(float n) { return n > 1.f ? n * __log2f(n) : 0.f; }
 
 // Scores every test of SNP pair (s >= t) from the Gram counts of both classes
 // (G0 class 0, G1 class 1; float holding exact integers).  Row pairs (2s+i,
@@ -249,6 +261,8 @@ static __device__ __noinline__ void exact_test(const ScanCtx &ctx, int rA, int r
 // is dropped when (|D| + e)^2 < theta * Q, theta = (2^tau - 1)(1 - 2^-10) and e
 // bounding the float rounding of D.
 // Bound (Fisher): p >= P(obs); dropped when log P(obs) > lp_thr.
+// Entropy survivors then meet an FP32 estimate of m*I with an error margin,
+// and only tests within that margin of tau reach the exact integer key.
 __device__ __forceinline__ void score_tests(const ScanCtx &ctx, const float *G0,
                                             const float *G1, int s, int t, float theta,
                                             float lp_thr) {
@@ -256,6 +270,8 @@ __device__ __forceinline__ void score_tests(const ScanCtx &ctx, const float *G0,
     const float m = y + z;
     const float yz = y * z;
     const bool diag = (s == t);
+    // Pair-level terms of the FP32 entropy estimate (stage 2), made on demand.
+    float Tm = -1.f, Ty = 0.f, Tz = 0.f;
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
 #pragma unroll
@@ -290,6 +306,23 @@ __device__ __forceinline__ void score_tests(const ScanCtx &ctx, const float *G0,
                                __ldg(L + iz) - __ldg(L + (iy + iz)) - __ldg(L + iw) -
                                __ldg(L + (iy - iw)) - __ldg(L + ix) - __ldg(L + (iz - ix));
                     pass = lp <= lp_thr;
+                }
+                if (pass && ctx.objective == 0) {
+                    // Stage 2: m*I in FP32 from __log2f (relative error of each
+                    // n*log2(n) <= 2.5 ulp, 8 additions) with a rigorous margin;
+                    // drop when estimate + margin < tau * m.
+                    if (Tm < 0.f) {
+                        Tm = tlog2f(m);
+                        Ty = tlog2f(y);
+                        Tz = tlog2f(z);
+                    }
+                    const float xx = w + x;
+                    const float a = tlog2f(w), b = tlog2f(y - w), c = tlog2f(x), d = tlog2f(z - x);
+                    const float e = tlog2f(xx), g = tlog2f(m - xx);
+                    const float est = ((Tm + a) + (b + c)) + d - (e + g) - (Ty + Tz);
+                    const float tm = ctx.st->tau_f * m;
+                    const float mag = Tm + a + b + c + d + e + g + Ty + Tz + fabsf(tm);
+                    pass = est + (2e-6f * mag + 1e-3f) >= tm;
                 }
                 if (pass)
                     exact_test(ctx, 2 * s + i, 2 * t + j, f, (int)w, (int)x, (int)y, (int)z);

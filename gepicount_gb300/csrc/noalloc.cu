@@ -167,8 +167,7 @@ __global__ void na_perm_kernel(const uint64_t *m1, const uint64_t *m2, int nw, i
     }
 }
 
-// Lower-triangle tile list (A tile i >= B tile j), row-major like the
-// allocating path.
+// Lower-triangle tile list (A tile i >= B tile j), row-major.
 __global__ void na_tiles_kernel(int2 *tiles, int nt) {
     const long long total = (long long)nt * (nt + 1) / 2;
     for (long long l = blockIdx.x * (long long)blockDim.x + threadIdx.x; l < total;
@@ -327,6 +326,8 @@ extern "C" gepi_status gepi_process_gpu_1_noalloc(const uint64_t *bits, const ui
     st.tau_key = 0ull;
     st.theta = 0.f;
     st.lp_thr = INFINITY;
+    st.tau_f = -INFINITY;
+    st.tau_val = -INFINITY;
     GEPI_CUDA(cudaMemcpy(d_state, &st, sizeof st, cudaMemcpyHostToDevice));
 
     ScanCtx ctx;

@@ -32,6 +32,11 @@ cudaError_t launch_decode_rows(const uint64_t *bits, const uint64_t *valid, int 
 cudaError_t launch_popc_tiles(const uint32_t *planes, int Wp, int W0, const int2 *tiles,
                               int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
                               uint32_t *dump, cudaStream_t stream);
+cudaError_t launch_tc_tiles(const uint32_t *planes, int Wp, int W0, const int2 *tiles, int ntiles,
+                            int a0, int a1, int b0, int b1, const ScanCtx &ctx, uint32_t *dump,
+                            int *err, int num_sms, cudaStream_t stream);
+int tc_tile_a_snps();
+int tc_tile_b_snps();
 cudaError_t run_select_compact(Cand *in, Cand *out, ScanState *st, void *sel, uint32_t cap,
                                uint32_t k, int n_override, uint32_t n_compact, int objective,
                                float lp_margin, int num_sms, cudaStream_t stream);
@@ -205,16 +210,28 @@ gepi_status upload_tiles(gepi_planes *pl, const std::vector<int2> &tiles) {
     return GEPI_OK;
 }
 
-// Tile pairs of [a0,a1) x [b0,b1) holding at least one (s, t) with t <= s.
-void build_tiles(int a0, int a1, int b0, int b1, int T, bool triangle, std::vector<int2> &out) {
+// Tile pairs (A tile i of TA SNPs, B tile j of TB SNPs) of [a0,a1) x [b0,b1)
+// holding at least one (s, t) with t <= s (all pairs when !triangle).  The
+// list runs in bands of `band` A tiles: within a band every B tile is visited
+// once for all the band's A tiles, so concurrently running CTAs share B tiles
+// in L2 and each B tile is fetched from HBM about once per band.
+void build_tiles(int a0, int a1, int b0, int b1, int TA, int TB, bool triangle, int band,
+                 std::vector<int2> &out) {
     out.clear();
-    const int nat = (a1 - a0 + T - 1) / T, nbt = (b1 - b0 + T - 1) / T;
-    for (int i = 0; i < nat; ++i) {
-        const int smax = std::min(a0 + i * T + T - 1, a1 - 1);
+    const int nat = (a1 - a0 + TA - 1) / TA, nbt = (b1 - b0 + TB - 1) / TB;
+    if (band < 1) band = 1;
+    for (int i0 = 0; i0 < nat; i0 += band) {
+        const int i1 = std::min(nat, i0 + band);
         for (int j = 0; j < nbt; ++j) {
-            const int tmin = b0 + j * T;
-            if (triangle && tmin > smax) break;
-            out.push_back(make_int2(i, j));
+            const int tmin = b0 + j * TB;
+            bool any = false;
+            for (int i = i0; i < i1; ++i) {
+                const int smax = std::min(a0 + i * TA + TA - 1, a1 - 1);
+                if (triangle && tmin > smax) continue;
+                out.push_back(make_int2(i, j));
+                any = true;
+            }
+            if (triangle && !any) break;
         }
     }
 }
@@ -226,6 +243,12 @@ gepi_status ensure_events(gepi_planes *pl, size_t n) {
         pl->ev.push_back(e);
     }
     return GEPI_OK;
+}
+
+// GEPI_METHOD_AUTO picks the counting form.
+int resolve_method(int m) {
+    if (m == GEPI_METHOD_POPC || m == GEPI_METHOD_TENSOR) return m;
+    return GEPI_METHOD_POPC;
 }
 
 bool cand_better(const Cand &a, const Cand &b) {
@@ -240,8 +263,8 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
     if (!pl || !par || !tops || k <= 0) return set_error(GEPI_ERR_ARG, "gepi_scan: bad argument");
     if (par->objective != GEPI_ENTROPY && par->objective != GEPI_FISHER)
         return set_error(GEPI_ERR_ARG, "gepi_scan: unknown objective");
-    if (par->method == GEPI_METHOD_TENSOR)
-        return set_error(GEPI_ERR_UNSUPPORTED, "tensor-core counting not available in this build");
+    if (par->method < GEPI_METHOD_AUTO || par->method > GEPI_METHOD_TENSOR)
+        return set_error(GEPI_ERR_ARG, "gepi_scan: unknown method");
     if (a0 < 0 || b0 < 0 || na < 0 || nb < 0 || a0 + na > pl->n_snps || b0 + nb > pl->n_snps)
         return set_error(GEPI_ERR_ARG, "gepi_scan: SNP range outside the planes");
     DeviceGuard g(pl->device);
@@ -250,15 +273,18 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
     GEPI_TRY(ensure_scan_buffers(pl, k));
     std::memset(tops, 0, sizeof(gepi_result) * (size_t)k);
 
-    const int T = popc_tile_snps();
+    const int method = resolve_method(par->method);
+    const bool tc = method == GEPI_METHOD_TENSOR;
+    const int TA = tc ? tc_tile_a_snps() : popc_tile_snps();
+    const int TB = tc ? tc_tile_b_snps() : popc_tile_snps();
     std::vector<int2> tiles;
-    build_tiles(a0, a0 + na, b0, b0 + nb, T, true, tiles);
+    build_tiles(a0, a0 + na, b0, b0 + nb, TA, TB, true, 8, tiles);
     GEPI_TRY(upload_tiles(pl, tiles));
     GEPI_TRY(ensure_events(pl, 4));
     gepi_scan_stats &S = pl->stats;
     S = gepi_scan_stats{};
-    S.method = GEPI_METHOD_POPC;
-    S.tile_snps = T;
+    S.method = method;
+    S.tile_snps = TA;
     S.tiles = tiles.size();
     {
         // pairs (s, t), t < s, s in A, t in B; and SNPs in both ranges
@@ -278,6 +304,8 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
     init.tau_key = 0ull;
     init.theta = 0.f;
     init.lp_thr = INFINITY;
+    init.tau_f = -INFINITY;
+    init.tau_val = -INFINITY;
     *pl->h_state = init;
     GEPI_CUDA(cudaMemcpyAsync(pl->d_state, pl->h_state, sizeof(ScanState), cudaMemcpyHostToDevice,
                               pl->stream));
@@ -294,7 +322,7 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
     ctx.st = pl->d_state;
 
     const size_t ntiles = tiles.size();
-    const double tests_per_tile = 20.0 * T * T;
+    const double tests_per_tile = 20.0 * TA * TB;
     const uint32_t budget = pl->cap / 2;
     const double pilot_tests = par->objective == GEPI_ENTROPY ? pl->cap / 4.0 : 1.0 * (1 << 16);
     size_t batch = (size_t)std::max(1.0, std::floor(pilot_tests / tests_per_tile));
@@ -305,8 +333,13 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
         const size_t nbt = std::min(batch, ntiles - t);
         ctx.cand = pl->d_cand[cur];
         GEPI_CUDA(cudaEventRecord(pl->ev[2], pl->stream));
-        GEPI_CUDA(launch_popc_tiles(pl->d_planes, pl->Wp, pl->W0, pl->d_tiles + t, (int)nbt, a0,
-                                    a0 + na, b0, b0 + nb, ctx, nullptr, pl->stream));
+        if (tc)
+            GEPI_CUDA(launch_tc_tiles(pl->d_planes, pl->Wp, pl->W0, pl->d_tiles + t, (int)nbt, a0,
+                                      a0 + na, b0, b0 + nb, ctx, nullptr, &pl->d_state->kerr,
+                                      pl->num_sms, pl->stream));
+        else
+            GEPI_CUDA(launch_popc_tiles(pl->d_planes, pl->Wp, pl->W0, pl->d_tiles + t, (int)nbt,
+                                        a0, a0 + na, b0, b0 + nb, ctx, nullptr, pl->stream));
         GEPI_CUDA(cudaEventRecord(pl->ev[3], pl->stream));
         GEPI_CUDA(cudaMemcpyAsync(pl->h_state, pl->d_state, sizeof(ScanState),
                                   cudaMemcpyDeviceToHost, pl->stream));
@@ -318,6 +351,9 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
             S.max_count_ms = std::max<double>(S.max_count_ms, ms);
             S.count_launches += 1;
         }
+        if (pl->h_state->kerr)
+            return set_error(GEPI_ERR_TIMEOUT, "counting kernel gave up a bounded wait (code " +
+                                                   std::to_string(pl->h_state->kerr) + ")");
         if (pl->h_state->overflow) {
             // Tighten with everything captured (a valid lower bound), drop this
             // batch's partial appends, retry it in halves.  Only more than
@@ -574,25 +610,38 @@ gepi_status gepi_pair_counts(gepi_planes *pl, int method, int a0, int na, int b0
     if (!pl || !out || na <= 0 || nb <= 0 || a0 < 0 || b0 < 0 || a0 + na > pl->n_snps ||
         b0 + nb > pl->n_snps)
         return set_error(GEPI_ERR_ARG, "gepi_pair_counts: bad argument");
-    if (method != GEPI_METHOD_POPC && method != GEPI_METHOD_AUTO)
-        return set_error(GEPI_ERR_UNSUPPORTED, "tensor-core counting not available in this build");
+    if (method < GEPI_METHOD_AUTO || method > GEPI_METHOD_TENSOR)
+        return set_error(GEPI_ERR_ARG, "gepi_pair_counts: unknown method");
     DeviceGuard g(pl->device);
     if (!g.ok) return set_error(GEPI_ERR_CUDA, "cudaSetDevice failed");
+    const bool tc = resolve_method(method) == GEPI_METHOD_TENSOR;
     std::vector<int2> tiles;
-    build_tiles(a0, a0 + na, b0, b0 + nb, popc_tile_snps(), false, tiles);
+    build_tiles(a0, a0 + na, b0, b0 + nb, tc ? tc_tile_a_snps() : popc_tile_snps(),
+                tc ? tc_tile_b_snps() : popc_tile_snps(), false, 8, tiles);
     GEPI_TRY(upload_tiles(pl, tiles));
     const size_t bytes = (size_t)na * nb * 18 * 4;
     GEPI_TRY(check_mem(bytes, "pair counts"));
     uint32_t *d_out = nullptr;
-    GEPI_CUDA(cudaMalloc(&d_out, bytes));
+    int *d_err = nullptr;
+    GEPI_CUDA(cudaMalloc(&d_out, bytes + 256));
+    d_err = reinterpret_cast<int *>(reinterpret_cast<char *>(d_out) + ((bytes + 255) & ~size_t(255)));
     ScanCtx ctx{};
-    cudaError_t e = launch_popc_tiles(pl->d_planes, pl->Wp, pl->W0, pl->d_tiles, (int)tiles.size(),
-                                      a0, a0 + na, b0, b0 + nb, ctx, d_out, pl->stream);
+    int herr = 0;
+    cudaError_t e = cudaMemsetAsync(d_err, 0, sizeof(int), pl->stream);
+    if (e == cudaSuccess)
+        e = tc ? launch_tc_tiles(pl->d_planes, pl->Wp, pl->W0, pl->d_tiles, (int)tiles.size(), a0,
+                                 a0 + na, b0, b0 + nb, ctx, d_out, d_err, pl->num_sms, pl->stream)
+               : launch_popc_tiles(pl->d_planes, pl->Wp, pl->W0, pl->d_tiles, (int)tiles.size(),
+                                   a0, a0 + na, b0, b0 + nb, ctx, d_out, pl->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, bytes, cudaMemcpyDeviceToHost, pl->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, pl->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(pl->stream);
     cudaFree(d_out);
     if (e != cudaSuccess)
         return set_error(GEPI_ERR_CUDA, std::string("pair counts: ") + cudaGetErrorString(e));
+    if (herr)
+        return set_error(GEPI_ERR_TIMEOUT, "counting kernel gave up a bounded wait (code " +
+                                               std::to_string(herr) + ")");
     return GEPI_OK;
 }
 

@@ -109,7 +109,9 @@ __global__ void sel_apply_kernel(ScanState *st, const SelState *sel, int objecti
     if (key <= st->tau_key) return;
     st->tau_key = key;
     double v = value_of_key(key);
+    st->tau_val = v;
     if (objective == 0) {
+        st->tau_f = __double2float_rd(v);
         double th = (exp2(v) - 1.0) * (1.0 - 1.0 / 1024.0);
         st->theta = th > 0.0 ? __double2float_rd(th) : 0.0f;
     } else {

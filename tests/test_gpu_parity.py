@@ -53,18 +53,51 @@ SHAPES = [
 ]
 
 
+METHODS = {"popc": 1, "tensor": 2}
+
+
+@pytest.mark.parametrize("method", sorted(METHODS))
 @pytest.mark.parametrize("kw", SHAPES, ids=[f"s{k['n_cases'] + k['n_controls']}" for k in SHAPES])
-def test_pair_counts_bit_exact(gepi, tmp_path, kw):
+def test_pair_counts_bit_exact(gepi, tmp_path, kw, method):
     pl, rows, fs, _ = make_planes(gepi, kw, tmp_path)
     N = fs.n_lines
-    got = pl.pair_counts(0, N, 0, N)
+    got = pl.pair_counts(0, N, 0, N, method=METHODS[method])
     want = H.oracle_pair_gram(rows, 0, N, 0, N)
     assert np.array_equal(got, want)
     # an unaligned sub-rectangle crossing tile boundaries
     a0, na, b0, nb = 3, min(N - 3, 37), 1, min(N - 1, 33)
-    got = pl.pair_counts(a0, na, b0, nb)
+    got = pl.pair_counts(a0, na, b0, nb, method=METHODS[method])
     assert np.array_equal(got, H.oracle_pair_gram(rows, a0, na, b0, nb))
     pl.close()
+
+
+def test_tensor_counts_exact_at_large_counts(gepi):
+    """FP8 products summed in FP32 stay exact up to the largest counts: all-set
+    and half-set planes over 40,000 samples per class, tensor == popcount."""
+    n_snps, n_samples = 40, 80000
+    nw = n_samples // 64
+    rng = np.random.default_rng(9)
+    bits = np.zeros((2 * n_snps, nw), dtype=np.uint64)
+    valid = np.full((2 * n_snps, nw), np.uint64(0xFFFFFFFFFFFFFFFF), dtype=np.uint64)
+    for s in range(n_snps):
+        kind = s % 4
+        if kind == 0:      # every sample carries both alleles (all three planes set)
+            bits[2 * s] = bits[2 * s + 1] = np.uint64(0xFFFFFFFFFFFFFFFF)
+        elif kind == 1:    # column-5 allele everywhere
+            bits[2 * s] = np.uint64(0xFFFFFFFFFFFFFFFF)
+        else:              # random
+            bits[2 * s] = rng.integers(0, 2**63, size=nw, dtype=np.uint64)
+            bits[2 * s + 1] = ~bits[2 * s] | rng.integers(0, 2**63, size=nw, dtype=np.uint64)
+    m1 = np.zeros(nw, dtype=np.uint64)
+    m2 = np.zeros(nw, dtype=np.uint64)
+    m1[: nw // 2] = np.uint64(0xFFFFFFFFFFFFFFFF)
+    m2[nw // 2:] = np.uint64(0xFFFFFFFFFFFFFFFF)
+    with gepi.Planes.from_rows(bits, valid, m1, m2) as pl:
+        assert pl.class_sizes() == (40000, 40000)
+        p = pl.pair_counts(0, n_snps, 0, n_snps, method=1)
+        t = pl.pair_counts(0, n_snps, 0, n_snps, method=2)
+    assert p.max() == 40000
+    assert np.array_equal(p, t)
 
 
 def test_rows_path_matches_bed_path(gepi, tmp_path):
@@ -78,15 +111,16 @@ def test_rows_path_matches_bed_path(gepi, tmp_path):
     pl.close()
 
 
+@pytest.mark.parametrize("method", sorted(METHODS))
 @pytest.mark.parametrize("name", ["cfg1", "s63", "s64", "s65", "s129", "miss50", "cfg2_small"])
-def test_scan_entropy_matches_oracle_and_gold(gepi, tmp_path, name):
+def test_scan_entropy_matches_oracle_and_gold(gepi, tmp_path, name, method):
     doc = H.load_golden(name)
     base = H.golden_input(doc, str(tmp_path))
     fs = H.read_fileset(base)
     rows = H.decode_rows(fs)
     k = doc["k"]
     with gepi.Planes.from_bed(fs.bed, fs.n_lines, fs.pheno) as pl:
-        got = pl.scan(k)
+        got = pl.scan(k, method=METHODS[method])
     want, keys, nranked = H.oracle_topk(rows, k)
     assert_same_topk(got, want)
     if nranked >= k:
@@ -98,12 +132,13 @@ def test_scan_entropy_matches_oracle_and_gold(gepi, tmp_path, name):
         assert not probs, probs[:5]
 
 
-def test_scan_is_deterministic(gepi, tmp_path):
+def test_scan_is_deterministic_and_method_independent(gepi, tmp_path):
     kw = dict(n_snps=300, n_cases=400, n_controls=350, missing=0.02, seed=77)
     pl, rows, fs, _ = make_planes(gepi, kw, tmp_path)
-    a = pl.scan(500)
-    b = pl.scan(500)
-    assert a.tobytes() == b.tobytes()
+    a = pl.scan(500, method=1)
+    b = pl.scan(500, method=1)
+    c = pl.scan(500, method=2)
+    assert a.tobytes() == b.tobytes() == c.tobytes()
     pl.close()
 
 
@@ -133,12 +168,13 @@ def test_k_beyond_ranked_tests_zero_pads(gepi, tmp_path):
     pl.close()
 
 
+@pytest.mark.parametrize("method", sorted(METHODS))
 @pytest.mark.parametrize("rng_", [(0, 40, 0, 40), (40, 60, 5, 50), (90, 30, 0, 120), (7, 1, 7, 1)])
-def test_scan_range_matches_oracle(gepi, tmp_path, rng_):
+def test_scan_range_matches_oracle(gepi, tmp_path, rng_, method):
     kw = dict(n_snps=120, n_cases=160, n_controls=140, missing=0.02, seed=41)
     pl, rows, fs, _ = make_planes(gepi, kw, tmp_path)
     a0, na, b0, nb = rng_
-    got = pl.scan_range(a0, na, b0, nb, 200)
+    got = pl.scan_range(a0, na, b0, nb, 200, method=METHODS[method])
     want, _, _ = H.oracle_topk_range(rows, 2 * a0, 2 * (a0 + na), 2 * b0, 2 * (b0 + nb), 200)
     assert_same_topk(got, want)
     pl.close()
@@ -197,7 +233,9 @@ def test_config2_scale_properties(gepi):
     rows = H.decode_rows(fs)
     k = 1000
     with gepi.Planes.from_bed(bed, spec.n_snps, ph) as pl:
-        got = pl.scan(k)
+        got = pl.scan(k, method=2)
+        plain = pl.scan(k, method=1)
+    assert got.tobytes() == plain.tobytes()
     items = items_of(got)
     ex = H.exact_keys(rows, items)
     keys = []

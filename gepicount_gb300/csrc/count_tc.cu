@@ -1,39 +1,53 @@
 // tcgen05 pair-count kernel: the per-class plane Gram on the 5th-generation
-// tensor cores (FP8 e4m3 operands, FP32 accumulators in tensor memory), exact,
-// with the fused scoring epilogue of the other counting kernels.
+// tensor cores (packed FP4 E2M1 operands with unit block scales, FP32
+// accumulators in tensor memory), exact, with the fused scoring epilogue of the
+// other counting kernels.
 //
-// A set genotype bit becomes the e4m3 value 2^-6 (byte 0x08); products are
-// 2^-12 and FP32 sums of them are exact, so count = accumulator * 4096.  The
+// A set genotype bit becomes the E2M1 value 1.0 (nibble 0x2) and a clear bit
+// 0; the UE8M0 block scales are all 1.0 (byte 0x7F), so every product is 0 or
+// 1 and the FP32 accumulator holds the count exactly (below 2^24).  The
 // bit-planes stay packed (1 bit per sample) in HBM and L2; CUDA cores expand
-// them on chip, using the nibble-transposed word layout (decode.cu): the four
-// bytes of samples 4t..4t+3 of a word w are ((w >> t) << 3) & 0x08080808.
+// them on chip, four E2M1 words per plane word: word t of the expansion takes
+// bits t, t+4, ..., t+28 into nibbles 0..7.  The sample order inside K is the
+// same for both operands, so the dot product is popcount(a & b).
 //
 // Tile: 40 A SNPs x 32 B SNPs.  MMA M = 128 TMEM lanes: lane quarter q holds A
 // SNPs 10q..10q+9, lane 3i+p of the quarter = plane p of SNP i (lanes 30, 31
-// zero).  MMA N = 96: B row 3j+q = plane q of B SNP j.  K = 32 samples per
-// tcgen05.mma, 8 per 256-sample pipeline chunk (one barrier wait and one
-// commit per 8 MMAs: the issuing thread's wait and commit latency is then
-// hidden behind the 512 tensor cycles of the chunk).
+// zero).  MMA N = 96: B row 3j+q = plane q of B SNP j.  K = 64 samples per
+// tcgen05.mma (kind::mxf4, scale_vec::2X); a pipeline chunk is up to 384
+// samples of one class (6 MMAs, one barrier wait and one commit).
 //
-// Tensor memory (512 columns, one CTA per SM): two accumulator buffers of
-// 192 columns (class 0 at +0, class 1 at +96) and two A stages of 64 columns
-// (256 fp8 per lane).  Shared memory: two B stages of 96 rows x 256 bytes in
-// the SWIZZLE_NONE K-major core-matrix layout (8 rows x 16 B cores, k-group
-// stride 128 B, row-group stride 2048 B).
+// Data path per chunk: TMA (cp.async.bulk.tensor, 2-D map over the plane
+// rows) lands the packed bits of the tile's 120 A rows and 96 B rows (48 bytes
+// each) in a shared-memory ring; producer warps expand them, A into tensor
+// memory (tcgen05.st), B into shared memory; one thread issues the MMAs.  The
+// producers never wait on global memory.
 //
-// Warp roles (17 warps, persistent CTA striding over the tile list):
+// Tensor memory (512 columns, one CTA per SM): two accumulator buffers of 192
+// columns (class 0 at +0, class 1 at +96), two A stages of 48 columns (384
+// E2M1 per lane) and 32 columns of scale factors (all 0x7F).  Shared memory:
+// two B stages of 96 rows x 192 bytes in the SWIZZLE_NONE K-major
+// core-matrix layout (8 rows x 16 B cores, k-group stride 128 B, row-group
+// stride 1536 B), the packed ring and the epilogue exchange rows.
+//
+// Warp roles (18 warps, persistent CTA striding over the tile list):
 //   producers  two groups, warps 0-3 and 8-11, take alternate chunks (one
-//              stage each); in a chunk each warp writes A for its TMEM lane
-//              quarter by tcgen05.st and 6 of the 768 B words by st.shared
+//              A/B stage each); thread u of a group expands packed A row
+//              30q+lane (lane < 30) and packed B row u (u < 96)
 //   epilogue   warps 4-7 and 12-15 (two per lane quarter, each half of the B
 //              SNPs): drain an accumulator buffer per tile (tcgen05.ld),
 //              exchange the three A planes of a SNP through shared memory and
 //              score every SNP pair (score_tests)
-//   MMA        warp 16, one thread: 8 x tcgen05.mma per chunk, commits
-// mbarriers: full[s] (4 producer warps) / empty[s] (tcgen05.commit) per stage,
-// dfull[b] (commit) / dempty[b] (8 epilogue warps) per accumulator buffer.
-// Every wait is bounded by a clock budget; on expiry the kernel records an
-// error, drains its own MMAs, frees its tensor memory and returns.
+//   MMA        warp 16, one thread: up to 6 x tcgen05.mma per chunk, commits
+//   TMA        warp 17, one thread: two tensor loads per chunk
+// mbarriers: pfull[j] (TMA transaction bytes) / pempty[j] (4 producer warps)
+// per ring slot, full[s] (4 producer warps) / empty[s] (tcgen05.commit) per
+// stage, dfull[b] (commit) / dempty[b] (8 epilogue warps) per accumulator
+// buffer.  Every wait is bounded by a clock budget; on expiry the kernel
+// records an error, drains its own MMAs and tensor loads, frees its tensor
+// memory and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -44,27 +58,40 @@ namespace gepi {
 
 constexpr int kTcASnps = 40;
 constexpr int kTcBSnps = 32;
+constexpr int kTcARows = 3 * kTcASnps;             // 120
 constexpr int kTcN = 3 * kTcBSnps;                 // 96
-constexpr int kTcChunkWords = 8;                   // 256 samples per stage (8 MMAs)
-constexpr int kTcStages = 2;
+constexpr int kTcChunkWords = 12;                  // 384 samples per chunk (6 MMAs of K = 64)
+constexpr int kTcStages = 2;                       // A/B operand stages, one per producer group
+constexpr int kTcPStages = 6;                      // packed ring depth
 constexpr int kTcLbo = 128;                        // k-group stride (bytes)
-constexpr int kTcSbo = kTcChunkWords * 2 * kTcLbo;   // 8-row group stride: 2,048 bytes
-constexpr int kTcBStageBytes = (kTcN / 8) * kTcSbo;  // 24,576
+constexpr int kTcSbo = kTcChunkWords * kTcLbo;     // 8-row group stride: 1,536 bytes
+constexpr int kTcBStageBytes = (kTcN / 8) * kTcSbo;  // 18,432
+constexpr int kTcPABytes = kTcARows * kTcChunkWords * 4;  // 5,760
+constexpr int kTcPBBytes = kTcN * kTcChunkWords * 4;      // 4,608
+constexpr int kTcPStageBytes = kTcPABytes + kTcPBBytes;   // 10,368
 constexpr int kTcXStride = 49;                     // epilogue exchange row pitch (floats)
-constexpr int kTcThreads = 17 * 32;
+constexpr int kTcThreads = 18 * 32;
 constexpr int kTcMmaWarp = 16;
+constexpr int kTcTmaWarp = 17;
 constexpr int kTcEpiWarps = 8;
 constexpr uint32_t kTcCols = 512;
 constexpr uint32_t kTcDCols = 2 * kTcN;            // one accumulator buffer
 constexpr uint32_t kTcACol = 2 * kTcDCols;         // 384: first A stage
-constexpr uint32_t kTcAStageCols = kTcChunkWords * 8;  // 64 columns (256 fp8 per lane)
-constexpr uint32_t kTcIdesc =
-    (1u << 4) | ((uint32_t)(kTcN >> 3) << 17) | ((uint32_t)(128 >> 4) << 24);  // f32 += e4m3*e4m3
-constexpr size_t kTcSmemUsed =
-    kTcStages * (size_t)kTcBStageBytes + (size_t)kTcEpiWarps * 32 * kTcXStride * 4;
-constexpr size_t kTcSmem = 116 * 1024;             // > half an SM: one CTA (and TMEM owner) per SM
+constexpr uint32_t kTcAStageCols = kTcChunkWords * 4;  // 48 columns (384 E2M1 per lane)
+constexpr uint32_t kTcSfCol = kTcACol + kTcStages * kTcAStageCols;  // 480: scale factors
+constexpr uint32_t kTcIdesc = (1u << 7) | (1u << 10)           // A, B = E2M1
+                              | ((uint32_t)(kTcN >> 3) << 17)  // N
+                              | (1u << 23)                     // scales UE8M0
+                              | ((uint32_t)(128 >> 4) << 24);  // M
+constexpr size_t kTcPOff = kTcStages * (size_t)kTcBStageBytes;               // packed ring
+constexpr size_t kTcXOff = kTcPOff + kTcPStages * (size_t)kTcPStageBytes;    // exchange rows
+constexpr size_t kTcSmem = kTcXOff + (size_t)kTcEpiWarps * 32 * kTcXStride * 4;
+static_assert(kTcSfCol + 32 <= kTcCols, "tensor memory budget");
 constexpr long long kTcWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
-static_assert(kTcSmemUsed <= kTcSmem, "smem layout");
+static_assert(kTcPStageBytes % 128 == 0 && kTcPABytes % 128 == 0 && kTcPOff % 128 == 0,
+              "TMA destinations 128-byte aligned");
+static_assert(kTcSmem > 114 * 1024 && kTcSmem <= 227 * 1024,
+              "more than half an SM: one CTA (and tensor-memory owner) per SM");
 
 __device__ __forceinline__ uint32_t su32(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -88,6 +115,21 @@ __device__ __forceinline__ bool mbar_try(uint64_t *b, uint32_t parity) {
         : "r"(su32(b)), "r"(parity)
         : "memory");
     return done != 0;
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)), "r"(bytes)
+                 : "memory");
+}
+
+// 2-D tensor load of one box into shared memory, completion on mbarrier `b`.
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
+                                            uint64_t *b) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
+        "%3}], [%4];" ::"r"(su32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(su32(b))
+        : "memory");
 }
 
 // Warp-uniform bounded wait: lane 0 polls, the verdict is broadcast.
@@ -129,11 +171,13 @@ __device__ __forceinline__ uint64_t tc_bdesc(uint32_t saddr) {
            ((uint64_t)(kTcSbo >> 4) << 32) | (1ull << 46);
 }
 
-__device__ __forceinline__ void tc_mma(uint32_t d, uint32_t a, uint64_t bdesc, uint32_t acc) {
+__device__ __forceinline__ void tc_mma(uint32_t d, uint32_t a, uint64_t bdesc, uint32_t sf,
+                                       uint32_t acc) {
     asm volatile(
-        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-        " tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], [%1], %2, %3, p;\n}\n" ::"r"(d),
-        "r"(a), "l"(bdesc), "r"(kTcIdesc), "r"(acc));
+        "{\n .reg .pred p;\n setp.ne.b32 p, %5, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::mxf4.block_scale.scale_vec::2X [%0], [%1], %2, %3, [%4], "
+        "[%4], p;\n}\n" ::"r"(d),
+        "r"(a), "l"(bdesc), "r"(kTcIdesc), "r"(sf), "r"(acc));
 }
 
 __device__ __forceinline__ void tc_commit(uint64_t *b) {
@@ -142,20 +186,16 @@ __device__ __forceinline__ void tc_commit(uint64_t *b) {
         : "memory");
 }
 
-// 32 samples (one nibble-transposed word) -> 8 registers of 4 e4m3 bytes.
+// 32 samples (one plane word) -> 4 registers of 8 E2M1 nibbles (1.0 or 0).
 __device__ __forceinline__ void expand_word(uint32_t w, uint32_t *o) {
-    constexpr uint32_t M = 0x08080808u;
-    o[0] = (w << 3) & M;
-    o[1] = (w << 2) & M;
-    o[2] = (w << 1) & M;
-    o[3] = w & M;
-    o[4] = (w >> 1) & M;
-    o[5] = (w >> 2) & M;
-    o[6] = (w >> 3) & M;
-    o[7] = (w >> 4) & M;
+    constexpr uint32_t M = 0x22222222u;
+    o[0] = (w << 1) & M;
+    o[1] = w & M;
+    o[2] = (w >> 1) & M;
+    o[3] = (w >> 2) & M;
 }
 
-__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&r)[32]) {
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t *r) {
     asm volatile(
         "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
         "%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
@@ -164,6 +204,16 @@ __device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&r)[32
         "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]),
         "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]),
         "r"(r[29]), "r"(r[30]), "r"(r[31])
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t *r) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+        "%14,%15,%16};" ::"r"(taddr),
+        "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+        "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]),
+        "r"(r[15])
         : "memory");
 }
 
@@ -187,22 +237,58 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&r)[8]) {
         : "memory");
 }
 
+// Bounded wait used on the way out: ignores the abort flag (the copies or MMAs
+// it waits for are this CTA's own and must land before the CTA exits).
+__device__ __forceinline__ void mbar_drain(uint64_t *b, uint32_t parity) {
+    if (mbar_try(b, parity)) return;
+    const long long t0 = clock64();
+    while (!mbar_try(b, parity) && clock64() - t0 < kTcWaitCycles) {
+    }
+}
+
+// Chunk c of a tile: class 0 owns chunks [0, n0) over words [0, W0), class 1
+// chunks [n0, n0 + n1) over words [W0, Wp); the last chunk of a class may be
+// short (its box reaches into the next class or past the row, which the MMAs
+// of the chunk do not read).
+struct ChunkMap {
+    int n0, nchunks, W0, W1;
+    __device__ __forceinline__ int start(int c) const {
+        return c < n0 ? kTcChunkWords * c : W0 + kTcChunkWords * (c - n0);
+    }
+    __device__ __forceinline__ int mmas(int c) const {  // K = 64 samples = 2 words per MMA
+        const int rem = c < n0 ? W0 - kTcChunkWords * c : W1 - kTcChunkWords * (c - n0);
+        return (rem < kTcChunkWords ? rem : kTcChunkWords) >> 1;
+    }
+};
+
 template <bool DUMP>
 __global__ void __launch_bounds__(kTcThreads, 1)
-    tc_tile_kernel(const uint32_t *__restrict__ planes, int Wp, int W0,
-                   const int2 *__restrict__ tiles, int ntiles, int a0, int a1, int b0, int b1,
-                   ScanCtx ctx, uint32_t *__restrict__ dump, int *err) {
+    tc_tile_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+                   int Wp, int W0, const int2 *__restrict__ tiles, int ntiles, int a0, int a1, int b0,
+                   int b1, ScanCtx ctx, uint32_t *__restrict__ dump, int *err) {
     extern __shared__ __align__(1024) unsigned char tc_smem[];
-    __shared__ uint64_t full_bar[kTcStages], empty_bar[kTcStages], dfull_bar[2], dempty_bar[2],
-        fin_bar;
+    __shared__ uint64_t pfull_bar[kTcPStages], pempty_bar[kTcPStages], full_bar[kTcStages],
+        empty_bar[kTcStages], dfull_bar[2], dempty_bar[2], fin_bar;
     __shared__ uint32_t tmem_slot;
     __shared__ int abort_flag;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int nchunks = Wp / kTcChunkWords;
-    const int csplit = W0 / kTcChunkWords;  // chunks of class 0
+    ChunkMap cm;
+    cm.W0 = W0;
+    cm.W1 = Wp - W0;
+    cm.n0 = (W0 + kTcChunkWords - 1) / kTcChunkWords;
+    cm.nchunks = cm.n0 + (cm.W1 + kTcChunkWords - 1) / kTcChunkWords;
+    const int nchunks = cm.nchunks;
+    const int my_tiles = (int)blockIdx.x < ntiles
+                             ? (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x
+                             : 0;
+    const int total = my_tiles * nchunks;  // this CTA's (tile, chunk) sequence, walked flat
 
     if (tid == 0) {
+        for (int j = 0; j < kTcPStages; ++j) {
+            mbar_init(&pfull_bar[j], 1);
+            mbar_init(&pempty_bar[j], 4);
+        }
         for (int s = 0; s < kTcStages; ++s) {
             mbar_init(&full_bar[s], 4);
             mbar_init(&empty_bar[s], 1);
@@ -227,96 +313,113 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     tc_fence_after();
     const uint32_t tbase = tmem_slot;
     volatile int *vabort = &abort_flag;
+    if (warp < 4) {
+        // unit block scales (UE8M0 1.0) over all lanes of the scale-factor columns
+        uint32_t r[32];
+#pragma unroll
+        for (int k = 0; k < 32; ++k) r[k] = 0x7F7F7F7Fu;
+        tmem_st32(tbase + ((uint32_t)(32 * warp) << 16) + kTcSfCol, r);
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
 
     if (warp < 4 || (warp >= 8 && warp < 12)) {
         // ---------------- producers ----------------
         const int q = warp & 3;             // TMEM lane quarter
         const int grp = warp >= 8;          // producer group: chunks of parity grp
-        const int u = q * 32 + lane;        // 0..127 within the group
-        const int ai = 10 * q + lane / 3, ap = lane % 3;
-        const bool arow = lane < 30;
-        constexpr int kBW = kTcN * kTcChunkWords / 128;  // B words per thread: 6
-        int bn[kBW], bw[kBW];
-#pragma unroll
-        for (int m = 0; m < kBW; ++m) {
-            const int wi = u + 128 * m;     // consecutive lanes: consecutive B rows
-            bn[m] = wi % kTcN;
-            bw[m] = wi / kTcN;
-        }
-        // The CTA's (tile, chunk) sequence is walked flat; this group takes
-        // every other chunk and loads its next chunk ahead.
-        const int my_tiles = blockIdx.x < (unsigned)ntiles
-                                 ? (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x
-                                 : 0;
-        const int total = my_tiles * nchunks;
-        struct Words {
-            uint4 a0, a1;
-            uint32_t b[kBW];
-        };
-        auto load = [&](int idx, Words &w) {
-            w.a0 = w.a1 = make_uint4(0, 0, 0, 0);
-#pragma unroll
-            for (int m = 0; m < kBW; ++m) w.b[m] = 0;
-            if (idx >= total) return;
-            const int k = idx / nchunks, c = idx - k * nchunks;
-            const int2 tl = tiles[blockIdx.x + k * gridDim.x];
-            const int sa = a0 + tl.x * kTcASnps + ai;
-            if (arow && sa < a1) {
-                const uint4 *g = reinterpret_cast<const uint4 *>(planes + ((size_t)sa * 3 + ap) * Wp +
-                                                                 kTcChunkWords * c);
-                w.a0 = __ldg(g);
-                w.a1 = __ldg(g + 1);
-            }
-            const int sb0 = b0 + tl.y * kTcBSnps;
-#pragma unroll
-            for (int m = 0; m < kBW; ++m) {
-                const int sb = sb0 + bn[m] / 3;
-                if (sb < b1)
-                    w.b[m] = __ldg(planes + ((size_t)sb * 3 + bn[m] % 3) * Wp + kTcChunkWords * c + bw[m]);
-            }
-        };
-        Words cur, nxt;
-        load(grp, cur);
+        const int u = q * 32 + lane;        // B row of this thread (u < 96)
+        const bool arow = lane < 30, brow = u < kTcN;
+        const uint32_t s = (uint32_t)grp;   // this group's A/B stage
+        const uint32_t ta = tbase + ((uint32_t)(32 * q) << 16) + kTcACol + s * kTcAStageCols;
+        unsigned char *bst = tc_smem + (size_t)s * kTcBStageBytes + (u >> 3) * kTcSbo + (u & 7) * 16;
         for (int idx = grp; idx < total; idx += 2) {
-            load(idx + 2, nxt);
-            const uint32_t gc = (uint32_t)idx;
-            const uint32_t s = gc % kTcStages;
-            if (!mbar_wait_warp(&empty_bar[s], ((gc / kTcStages) & 1) ^ 1, vabort, err, 1)) break;
-            tc_fence_after();
-            const uint32_t ta = tbase + ((uint32_t)(32 * q) << 16) + kTcACol + s * kTcAStageCols;
-            {
-                uint32_t r[32];
-                expand_word(cur.a0.x, r);
-                expand_word(cur.a0.y, r + 8);
-                expand_word(cur.a0.z, r + 16);
-                expand_word(cur.a0.w, r + 24);
-                tmem_st32(ta, r);
-            }
-            {
-                uint32_t r[32];
-                expand_word(cur.a1.x, r);
-                expand_word(cur.a1.y, r + 8);
-                expand_word(cur.a1.z, r + 16);
-                expand_word(cur.a1.w, r + 24);
-                tmem_st32(ta + 32, r);
-            }
-            unsigned char *stage = tc_smem + (size_t)s * kTcBStageBytes;
+            const uint32_t j = (uint32_t)idx % kTcPStages;
+            if (!mbar_wait_warp(&pfull_bar[j], ((uint32_t)idx / kTcPStages) & 1, vabort, err, 5)) break;
+            const unsigned char *pk = tc_smem + kTcPOff + (size_t)j * kTcPStageBytes;
+            uint4 pa[3], pb[3];
 #pragma unroll
-            for (int m = 0; m < kBW; ++m) {
-                uint32_t o[8];
-                expand_word(cur.b[m], o);
-                unsigned char *st = stage + (bn[m] >> 3) * kTcSbo + (2 * bw[m]) * kTcLbo + (bn[m] & 7) * 16;
-                *reinterpret_cast<uint4 *>(st) = make_uint4(o[0], o[1], o[2], o[3]);
-                *reinterpret_cast<uint4 *>(st + kTcLbo) = make_uint4(o[4], o[5], o[6], o[7]);
+            for (int m = 0; m < 3; ++m) pa[m] = pb[m] = make_uint4(0, 0, 0, 0);
+            if (arow) {
+                const uint4 *r = reinterpret_cast<const uint4 *>(pk + (30 * q + lane) * (kTcChunkWords * 4));
+#pragma unroll
+                for (int m = 0; m < 3; ++m) pa[m] = r[m];
+            }
+            if (brow) {
+                const uint4 *r =
+                    reinterpret_cast<const uint4 *>(pk + kTcPABytes + u * (kTcChunkWords * 4));
+#pragma unroll
+                for (int m = 0; m < 3; ++m) pb[m] = r[m];
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&pempty_bar[j]);
+            if (!mbar_wait_warp(&empty_bar[s], (((uint32_t)idx / kTcStages) & 1) ^ 1, vabort, err, 1))
+                break;
+            tc_fence_after();
+            {
+                uint32_t r[48];
+#pragma unroll
+                for (int m = 0; m < 3; ++m) {
+                    expand_word(pa[m].x, r + 16 * m);
+                    expand_word(pa[m].y, r + 16 * m + 4);
+                    expand_word(pa[m].z, r + 16 * m + 8);
+                    expand_word(pa[m].w, r + 16 * m + 12);
+                }
+                tmem_st32(ta, r);
+                tmem_st16(ta + 32, r + 32);
+            }
+            if (brow) {
+#pragma unroll
+                for (int m = 0; m < 3; ++m) {
+                    const uint32_t w4[4] = {pb[m].x, pb[m].y, pb[m].z, pb[m].w};
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        uint32_t o[4];
+                        expand_word(w4[e], o);
+                        *reinterpret_cast<uint4 *>(bst + (4 * m + e) * kTcLbo) =
+                            make_uint4(o[0], o[1], o[2], o[3]);
+                    }
+                }
             }
             asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&full_bar[s]);
-            cur = nxt;
             if (__any_sync(0xffffffffu, *vabort != 0)) break;
         }
+    } else if (warp == kTcTmaWarp) {
+        // ---------------- TMA issuer ----------------
+        if (lane == 0) {
+            asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_a)) : "memory");
+            asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_b)) : "memory");
+            int issued = 0;
+            int2 tl = make_int2(0, 0), tl_next = make_int2(0, 0);
+            if (my_tiles > 0) tl_next = tiles[blockIdx.x];
+            int k = -1, c = nchunks;
+            for (int idx = 0; idx < total; ++idx) {
+                if (++c >= nchunks) {
+                    c = 0;
+                    ++k;
+                    tl = tl_next;
+                    if (k + 1 < my_tiles) tl_next = tiles[blockIdx.x + (k + 1) * gridDim.x];
+                }
+                const uint32_t j = (uint32_t)idx % kTcPStages;
+                if (!mbar_wait(&pempty_bar[j], (((uint32_t)idx / kTcPStages) & 1) ^ 1, vabort, err, 6))
+                    break;
+                unsigned char *pk = tc_smem + kTcPOff + (size_t)j * kTcPStageBytes;
+                const int x = cm.start(c);
+                mbar_expect_tx(&pfull_bar[j], kTcPStageBytes);
+                tma_load_2d(pk, &map_a, x, 3 * (a0 + tl.x * kTcASnps), &pfull_bar[j]);
+                tma_load_2d(pk + kTcPABytes, &map_b, x, 3 * (b0 + tl.y * kTcBSnps), &pfull_bar[j]);
+                issued = idx + 1;
+            }
+            // every tensor load this thread issued lands before the CTA exits
+            for (int idx = issued > kTcPStages ? issued - kTcPStages : 0; idx < issued; ++idx)
+                mbar_drain(&pfull_bar[idx % kTcPStages], ((uint32_t)idx / kTcPStages) & 1);
+        }
+        __syncwarp();
     } else if (warp == kTcMmaWarp) {
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
@@ -324,6 +427,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
             for (int st = 0; st < kTcStages; ++st)
                 bdesc[st] = tc_bdesc(su32(tc_smem + (size_t)st * kTcBStageBytes));
+            const uint32_t sf = tbase + kTcSfCol;
             uint32_t gc = 0, lt = 0;
             bool ok = true;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++lt) {
@@ -333,19 +437,21 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 const uint32_t dbuf = tbase + b * kTcDCols;
                 for (int c = 0; c < nchunks; ++c, ++gc) {
                     const uint32_t s = gc % kTcStages;
+                    const int nm = cm.mmas(c);
+                    const uint32_t d = dbuf + (c < cm.n0 ? 0u : (uint32_t)kTcN);
+                    const uint32_t acc0 = (c == 0 || c == cm.n0) ? 0u : 1u;
+                    const uint32_t a = tbase + kTcACol + s * kTcAStageCols;
+                    const uint64_t bd = bdesc[s];
                     if (!mbar_wait(&full_bar[s], (gc / kTcStages) & 1, vabort, err, 3)) {
                         ok = false;
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t d = dbuf + (c < csplit ? 0u : (uint32_t)kTcN);
-                    const uint32_t acc0 = (c == 0 || c == csplit) ? 0u : 1u;
-                    const uint32_t a = tbase + kTcACol + s * kTcAStageCols;
-                    const uint64_t bd = bdesc[s];
-                    // k-group pair kk starts 2*kk*LBO = 256 B further: +16 in the address field
+                    // MMA kk reads A columns 8kk.. and the k-group pair 2kk (256 B further
+                    // each: +16 in the descriptor's address field)
 #pragma unroll
-                    for (int kk = 0; kk < kTcChunkWords; ++kk)
-                        tc_mma(d, a + kk * 8, bd + (uint64_t)(16 * kk), kk == 0 ? acc0 : 1u);
+                    for (int kk = 0; kk < kTcChunkWords / 2; ++kk)
+                        if (kk < nm) tc_mma(d, a + kk * 8, bd + (uint64_t)(16 * kk), sf, kk == 0 ? acc0 : 1u);
                     tc_commit(&empty_bar[s]);
                 }
                 if (!ok) break;
@@ -353,9 +459,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
             // drain every MMA this thread issued before tensor memory is freed
             tc_commit(&fin_bar);
-            const long long t0 = clock64();
-            while (!mbar_try(&fin_bar, 0) && clock64() - t0 < kTcWaitCycles) {
-            }
+            mbar_drain(&fin_bar, 0);
         }
         __syncwarp();
     } else {
@@ -363,8 +467,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const int q = warp & 3;
         const int eh = warp >= 12;  // which half of the B SNPs
         const int ew = q + 4 * eh;  // 0..7
-        float *xb = reinterpret_cast<float *>(tc_smem + kTcStages * (size_t)kTcBStageBytes) +
-                    (size_t)ew * 32 * kTcXStride;
+        float *xb = reinterpret_cast<float *>(tc_smem + kTcXOff) + (size_t)ew * 32 * kTcXStride;
         const int i = lane / 3, p = lane % 3;
         const float theta = DUMP ? 0.f : ctx.st->theta;
         const float lp_thr = DUMP ? 0.f : ctx.st->lp_thr;
@@ -398,8 +501,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                             uint32_t *o = dump + ((size_t)(sA - a0) * (b1 - b0) + (sBt - b0)) * 18;
 #pragma unroll
                             for (int qq = 0; qq < 3; ++qq) {
-                                o[p * 3 + qq] = (uint32_t)(__uint_as_float(v0[3 * jl + qq]) * 4096.f);
-                                o[9 + p * 3 + qq] = (uint32_t)(__uint_as_float(v1[3 * jl + qq]) * 4096.f);
+                                o[p * 3 + qq] = (uint32_t)__uint_as_float(v0[3 * jl + qq]);
+                                o[9 + p * 3 + qq] = (uint32_t)__uint_as_float(v1[3 * jl + qq]);
                             }
                         }
                     }
@@ -408,8 +511,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 float *row = xb + lane * kTcXStride;
 #pragma unroll
                 for (int k = 0; k < 24; ++k) {
-                    row[k] = __uint_as_float(v0[k]) * 4096.f;
-                    row[24 + k] = __uint_as_float(v1[k]) * 4096.f;
+                    row[k] = __uint_as_float(v0[k]);
+                    row[24 + k] = __uint_as_float(v1[k]);
                 }
                 __syncwarp();
                 if (lane < 30 && sA < a1) {
@@ -441,25 +544,60 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
 }
 
-cudaError_t launch_tc_tiles(const uint32_t *planes, int Wp, int W0, const int2 *tiles, int ntiles,
-                            int a0, int a1, int b0, int b1, const ScanCtx &ctx, uint32_t *dump,
-                            int *err, int num_sms, cudaStream_t stream) {
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+// Plane rows as a 2-D uint32 tensor [nrows][Wp]; box = one chunk of `box_rows` rows.
+bool plane_map(CUtensorMap *m, const uint32_t *planes, int Wp, int nrows, int box_rows) {
+    auto enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)Wp, (cuuint64_t)nrows};
+    const cuuint64_t strides[1] = {(cuuint64_t)Wp * 4};
+    const cuuint32_t box[2] = {(cuuint32_t)kTcChunkWords, (cuuint32_t)box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<uint32_t *>(planes), dims, strides,
+               box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+cudaError_t launch_tc_tiles(const uint32_t *planes, int Wp, int W0, int nrows, const int2 *tiles,
+                            int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
+                            uint32_t *dump, int *err, int num_sms, cudaStream_t stream) {
     if (ntiles <= 0) return cudaSuccess;
-    if ((Wp % kTcChunkWords) || (W0 % kTcChunkWords)) return cudaErrorInvalidValue;
+    // class starts and chunk starts on 16-byte TMA boundaries, whole K = 64 MMAs
+    if ((W0 & 3) || (Wp & 3) || W0 <= 0 || Wp <= W0 || (reinterpret_cast<uintptr_t>(planes) & 15))
+        return cudaErrorInvalidValue;
+    CUtensorMap map_a, map_b;
+    if (!plane_map(&map_a, planes, Wp, nrows, kTcARows) || !plane_map(&map_b, planes, Wp, nrows, kTcN))
+        return cudaErrorInvalidValue;
     const int grid = ntiles < num_sms ? ntiles : num_sms;
     cudaError_t e;
     if (dump) {
         e = cudaFuncSetAttribute(tc_tile_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)kTcSmem);
         if (e != cudaSuccess) return e;
-        tc_tile_kernel<true><<<grid, kTcThreads, kTcSmem, stream>>>(planes, Wp, W0, tiles, ntiles, a0,
-                                                                    a1, b0, b1, ctx, dump, err);
+        tc_tile_kernel<true><<<grid, kTcThreads, kTcSmem, stream>>>(map_a, map_b, Wp, W0, tiles, ntiles,
+                                                                    a0, a1, b0, b1, ctx, dump, err);
     } else {
         e = cudaFuncSetAttribute(tc_tile_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)kTcSmem);
         if (e != cudaSuccess) return e;
-        tc_tile_kernel<false><<<grid, kTcThreads, kTcSmem, stream>>>(planes, Wp, W0, tiles, ntiles,
-                                                                     a0, a1, b0, b1, ctx, nullptr, err);
+        tc_tile_kernel<false><<<grid, kTcThreads, kTcSmem, stream>>>(
+            map_a, map_b, Wp, W0, tiles, ntiles, a0, a1, b0, b1, ctx, nullptr, err);
     }
     return cudaGetLastError();
 }

@@ -24,7 +24,7 @@
 namespace gepi {
 
 constexpr int kNumFuncs = 5;
-constexpr int kClassPadSamples = 256;  // one tensor-core pipeline chunk
+constexpr int kClassPadSamples = 256;  // class blocks: whole 16-byte TMA steps and K = 64 MMAs
 
 // Candidate record appended by the epilogue (32 bytes).
 struct __align__(16) Cand {

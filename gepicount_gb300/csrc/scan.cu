@@ -32,9 +32,9 @@ cudaError_t launch_decode_rows(const uint64_t *bits, const uint64_t *valid, int 
 cudaError_t launch_popc_tiles(const uint32_t *planes, int Wp, int W0, const int2 *tiles,
                               int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
                               uint32_t *dump, cudaStream_t stream);
-cudaError_t launch_tc_tiles(const uint32_t *planes, int Wp, int W0, const int2 *tiles, int ntiles,
-                            int a0, int a1, int b0, int b1, const ScanCtx &ctx, uint32_t *dump,
-                            int *err, int num_sms, cudaStream_t stream);
+cudaError_t launch_tc_tiles(const uint32_t *planes, int Wp, int W0, int nrows, const int2 *tiles,
+                            int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
+                            uint32_t *dump, int *err, int num_sms, cudaStream_t stream);
 int tc_tile_a_snps();
 int tc_tile_b_snps();
 cudaError_t run_select_compact(Cand *in, Cand *out, ScanState *st, void *sel, uint32_t cap,
@@ -119,8 +119,10 @@ gepi_status planes_alloc(gepi_planes *pl, int device, int n_snps, int S0, int S1
     pl->n_snps = n_snps;
     pl->S0 = S0;
     pl->S1 = S1;
-    pl->W0 = ((S0 + kClassPadSamples - 1) / kClassPadSamples) * (kClassPadSamples / 32);
-    pl->W1 = ((S1 + kClassPadSamples - 1) / kClassPadSamples) * (kClassPadSamples / 32);
+    // every class gets at least one padded block, so an empty class still has
+    // (all-zero) words for the counting kernels to sum
+    pl->W0 = std::max(1, (S0 + kClassPadSamples - 1) / kClassPadSamples) * (kClassPadSamples / 32);
+    pl->W1 = std::max(1, (S1 + kClassPadSamples - 1) / kClassPadSamples) * (kClassPadSamples / 32);
     pl->Wp = pl->W0 + pl->W1;
     GEPI_CUDA(cudaDeviceGetAttribute(&pl->num_sms, cudaDevAttrMultiProcessorCount, device));
     GEPI_CUDA(cudaStreamCreateWithFlags(&pl->stream, cudaStreamNonBlocking));
@@ -334,9 +336,9 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
         ctx.cand = pl->d_cand[cur];
         GEPI_CUDA(cudaEventRecord(pl->ev[2], pl->stream));
         if (tc)
-            GEPI_CUDA(launch_tc_tiles(pl->d_planes, pl->Wp, pl->W0, pl->d_tiles + t, (int)nbt, a0,
-                                      a0 + na, b0, b0 + nb, ctx, nullptr, &pl->d_state->kerr,
-                                      pl->num_sms, pl->stream));
+            GEPI_CUDA(launch_tc_tiles(pl->d_planes, pl->Wp, pl->W0, 3 * pl->n_snps,
+                                      pl->d_tiles + t, (int)nbt, a0, a0 + na, b0, b0 + nb, ctx,
+                                      nullptr, &pl->d_state->kerr, pl->num_sms, pl->stream));
         else
             GEPI_CUDA(launch_popc_tiles(pl->d_planes, pl->Wp, pl->W0, pl->d_tiles + t, (int)nbt,
                                         a0, a0 + na, b0, b0 + nb, ctx, nullptr, pl->stream));
@@ -629,8 +631,9 @@ gepi_status gepi_pair_counts(gepi_planes *pl, int method, int a0, int na, int b0
     int herr = 0;
     cudaError_t e = cudaMemsetAsync(d_err, 0, sizeof(int), pl->stream);
     if (e == cudaSuccess)
-        e = tc ? launch_tc_tiles(pl->d_planes, pl->Wp, pl->W0, pl->d_tiles, (int)tiles.size(), a0,
-                                 a0 + na, b0, b0 + nb, ctx, d_out, d_err, pl->num_sms, pl->stream)
+        e = tc ? launch_tc_tiles(pl->d_planes, pl->Wp, pl->W0, 3 * pl->n_snps, pl->d_tiles,
+                                 (int)tiles.size(), a0, a0 + na, b0, b0 + nb, ctx, d_out, d_err,
+                                 pl->num_sms, pl->stream)
                : launch_popc_tiles(pl->d_planes, pl->Wp, pl->W0, pl->d_tiles, (int)tiles.size(),
                                    a0, a0 + na, b0, b0 + nb, ctx, d_out, pl->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, bytes, cudaMemcpyDeviceToHost, pl->stream);

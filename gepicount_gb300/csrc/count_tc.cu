@@ -17,11 +17,15 @@
 // tcgen05.mma (kind::mxf4, scale_vec::2X); a pipeline chunk is up to 384
 // samples of one class (6 MMAs, one barrier wait and one commit).
 //
-// Data path per chunk: TMA (cp.async.bulk.tensor, 2-D map over the plane
-// rows) lands the packed bits of the tile's 120 A rows and 96 B rows (48 bytes
-// each) in a shared-memory ring; producer warps expand them, A into tensor
-// memory (tcgen05.st), B into shared memory; one thread issues the MMAs.  The
-// producers never wait on global memory.
+// Operand layout in HBM (built once per plane set by tc_relayout_kernel): the
+// plane words cut into 12-word (384-sample) blocks, block-major --
+// blk[(b * rows_pad + row) * 12 + w] -- with class 0 in blocks [0, n0) and
+// class 1 in [n0, n0 + n1), a short last block of a class zero-filled and
+// rows_pad - 3 * n_snps zero rows at the end.  A chunk of a tile is then two
+// contiguous runs (120 A rows x 48 B, 96 B rows x 48 B) that the bulk-copy
+// engine (cp.async.bulk) lands in a shared-memory ring; producer warps expand
+// them, A into tensor memory (tcgen05.st), B into shared memory; one thread
+// issues the MMAs.  No thread waits on global memory.
 //
 // Tensor memory (512 columns, one CTA per SM): two accumulator buffers of 192
 // columns (class 0 at +0, class 1 at +96), two A stages of 48 columns (384
@@ -31,23 +35,23 @@
 // stride 1536 B), the packed ring and the epilogue exchange rows.
 //
 // Warp roles (18 warps, persistent CTA striding over the tile list):
-//   producers  two groups, warps 0-3 and 8-11, take alternate chunks (one
-//              A/B stage each); thread u of a group expands packed A row
-//              30q+lane (lane < 30) and packed B row u (u < 96)
+//   producers  warps 0-3 and 8-11 share every chunk: warps q and q+8 (lane
+//              quarter q) expand words 0-5 and 6-11 of packed A row 30q+lane
+//              (lane < 30) and of packed B row 32q+lane (q < 3); stages
+//              alternate between chunks
 //   epilogue   warps 4-7 and 12-15 (two per lane quarter, each half of the B
 //              SNPs): drain an accumulator buffer per tile (tcgen05.ld),
 //              exchange the three A planes of a SNP through shared memory and
-//              score every SNP pair (score_tests)
+//              score every SNP pair (stage-1 bit mask, survivors refined
+//              out of line)
 //   MMA        warp 16, one thread: up to 6 x tcgen05.mma per chunk, commits
-//   TMA        warp 17, one thread: two tensor loads per chunk
-// mbarriers: pfull[j] (TMA transaction bytes) / pempty[j] (4 producer warps)
-// per ring slot, full[s] (4 producer warps) / empty[s] (tcgen05.commit) per
+//   TMA        warp 17, one thread: two bulk copies per chunk
+// mbarriers: pfull[j] (copy transaction bytes) / pempty[j] (8 producer warps)
+// per ring slot, full[s] (8 producer warps) / empty[s] (tcgen05.commit) per
 // stage, dfull[b] (commit) / dempty[b] (8 epilogue warps) per accumulator
 // buffer.  Every wait is bounded by a clock budget; on expiry the kernel
 // records an error, drains its own MMAs and tensor loads, frees its tensor
 // memory and returns.
-#include <cuda.h>
-#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -61,7 +65,7 @@ constexpr int kTcBSnps = 32;
 constexpr int kTcARows = 3 * kTcASnps;             // 120
 constexpr int kTcN = 3 * kTcBSnps;                 // 96
 constexpr int kTcChunkWords = 12;                  // 384 samples per chunk (6 MMAs of K = 64)
-constexpr int kTcStages = 2;                       // A/B operand stages, one per producer group
+constexpr int kTcStages = 2;                       // A/B operand stages
 constexpr int kTcPStages = 6;                      // packed ring depth
 constexpr int kTcLbo = 128;                        // k-group stride (bytes)
 constexpr int kTcSbo = kTcChunkWords * kTcLbo;     // 8-row group stride: 1,536 bytes
@@ -71,6 +75,7 @@ constexpr int kTcPBBytes = kTcN * kTcChunkWords * 4;      // 4,608
 constexpr int kTcPStageBytes = kTcPABytes + kTcPBBytes;   // 10,368
 constexpr int kTcXStride = 49;                     // epilogue exchange row pitch (floats)
 constexpr int kTcThreads = 18 * 32;
+constexpr int kTcProducerWarps = 8;
 constexpr int kTcMmaWarp = 16;
 constexpr int kTcTmaWarp = 17;
 constexpr int kTcEpiWarps = 8;
@@ -122,13 +127,12 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *b, uint32_t bytes) {
                  : "memory");
 }
 
-// 2-D tensor load of one box into shared memory, completion on mbarrier `b`.
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y,
-                                            uint64_t *b) {
+// Bulk copy of `bytes` contiguous bytes into shared memory, completion on mbarrier `b`.
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *b) {
     asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
-        "%3}], [%4];" ::"r"(su32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(su32(b))
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            su32(dst)),
+        "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(su32(b))
         : "memory");
 }
 
@@ -217,6 +221,12 @@ __device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t *r) {
         : "memory");
 }
 
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t *r) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr),
+                 "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7])
+                 : "memory");
+}
+
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
@@ -246,6 +256,89 @@ __device__ __forceinline__ void mbar_drain(uint64_t *b, uint32_t parity) {
     }
 }
 
+// Stage-1 bounds of the 20 tests of an SNP pair (row pairs (2s+i, 2t+j), five
+// functions each) as a bit mask, bit 5 * (2i + j) + f.  Same bounds as
+// score_tests; the tests that pass are refined one by one out of line, which
+// keeps the epilogue's code small (its warps share the instruction cache with
+// the producers).
+template <int OBJ>
+__device__ __forceinline__ uint32_t tc_stage1(const ScanCtx &ctx, const float *G0, const float *G1,
+                                              bool diag, float theta, float lp_thr) {
+    const float y = G0[8], z = G1[8];
+    const float m = y + z, yz = y * z;
+    uint32_t mask = 0;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            if (diag && j > i) continue;  // row 2t+j must be <= row 2s+i
+            float on0[5], on1[5];
+            {
+                const float n11 = G0[i * 3 + j], r = G0[i * 3 + 2], c = G0[6 + j];
+                const float n10 = r - n11, n01 = c - n11;
+                on0[0] = n11; on0[1] = n01; on0[2] = n10; on0[3] = y - r - c + n11; on0[4] = n10 + n01;
+            }
+            {
+                const float n11 = G1[i * 3 + j], r = G1[i * 3 + 2], c = G1[6 + j];
+                const float n10 = r - n11, n01 = c - n11;
+                on1[0] = n11; on1[1] = n01; on1[2] = n10; on1[3] = z - r - c + n11; on1[4] = n10 + n01;
+            }
+#pragma unroll
+            for (int f = 0; f < 5; ++f) {
+                const float w = on0[f], x = on1[f];
+                bool pass;
+                if (OBJ == 0) {
+                    const float xx = w + x;
+                    const float Q = xx * (m - xx) * yz;
+                    const float wz = w * z, xy = x * y;
+                    const float D = fabsf(wz - xy) + (wz + xy) * 2.384185791015625e-07f;  // 2^-22
+                    pass = D * D >= theta * Q;
+                } else {
+                    const int iw = (int)w, ix = (int)x, iy = (int)y, iz = (int)z;
+                    const float *L = ctx.lf32;
+                    const float lp = __ldg(L + (iw + ix)) + __ldg(L + (iy + iz - iw - ix)) +
+                                     __ldg(L + iy) + __ldg(L + iz) - __ldg(L + (iy + iz)) -
+                                     __ldg(L + iw) - __ldg(L + (iy - iw)) - __ldg(L + ix) -
+                                     __ldg(L + (iz - ix));
+                    pass = lp <= lp_thr;
+                }
+                mask |= (uint32_t)pass << (5 * (2 * i + j) + f);
+            }
+        }
+    }
+    return mask;
+}
+
+// Stages 2 and 3 of one test that passed stage 1: for entropy the FP32
+// estimate of m*I with its error margin (as in score_tests), then the exact key.
+template <int OBJ>
+static __device__ __noinline__ void tc_refine(const ScanCtx &ctx, int rA, int rB, int f, int w,
+                                              int x, int y, int z) {
+    if (OBJ == 0) {
+        const float fw = (float)w, fx = (float)x, fy = (float)y, fz = (float)z;
+        const float m = fy + fz, xx = fw + fx;
+        const float Tm = tlog2f(m), Ty = tlog2f(fy), Tz = tlog2f(fz);
+        const float a = tlog2f(fw), b = tlog2f(fy - fw), c = tlog2f(fx), d = tlog2f(fz - fx);
+        const float e = tlog2f(xx), g = tlog2f(m - xx);
+        const float est = ((Tm + a) + (b + c)) + d - (e + g) - (Ty + Tz);
+        const float tm = ctx.st->tau_f * m;
+        const float mag = Tm + a + b + c + d + e + g + Ty + Tz + fabsf(tm);
+        if (est + (2e-6f * mag + 1e-3f) < tm) return;
+    }
+    exact_test(ctx, rA, rB, f, w, x, y, z);
+}
+
+// Count of function f (AND, NAND, ANDN, NANDN, XOR) from n11 and the margins.
+__device__ __forceinline__ int fun_count(int n11, int r, int c, int tot, int f) {
+    switch (f) {
+    case 0: return n11;
+    case 1: return c - n11;
+    case 2: return r - n11;
+    case 3: return tot - r - c + n11;
+    default: return r + c - 2 * n11;
+    }
+}
+
 // Chunk c of a tile: class 0 owns chunks [0, n0) over words [0, W0), class 1
 // chunks [n0, n0 + n1) over words [W0, Wp); the last chunk of a class may be
 // short (its box reaches into the next class or past the row, which the MMAs
@@ -261,11 +354,11 @@ struct ChunkMap {
     }
 };
 
-template <bool DUMP>
+template <bool DUMP, int OBJ>
 __global__ void __launch_bounds__(kTcThreads, 1)
-    tc_tile_kernel(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
-                   int Wp, int W0, const int2 *__restrict__ tiles, int ntiles, int a0, int a1, int b0,
-                   int b1, ScanCtx ctx, uint32_t *__restrict__ dump, int *err) {
+    tc_tile_kernel(const uint32_t *__restrict__ blk, int rows_pad, int Wp, int W0,
+                   const int2 *__restrict__ tiles, int ntiles, int a0, int a1, int b0, int b1,
+                   ScanCtx ctx, uint32_t *__restrict__ dump, int *err) {
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     __shared__ uint64_t pfull_bar[kTcPStages], pempty_bar[kTcPStages], full_bar[kTcStages],
         empty_bar[kTcStages], dfull_bar[2], dempty_bar[2], fin_bar;
@@ -287,10 +380,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     if (tid == 0) {
         for (int j = 0; j < kTcPStages; ++j) {
             mbar_init(&pfull_bar[j], 1);
-            mbar_init(&pempty_bar[j], 4);
+            mbar_init(&pempty_bar[j], kTcProducerWarps);
         }
         for (int s = 0; s < kTcStages; ++s) {
-            mbar_init(&full_bar[s], 4);
+            mbar_init(&full_bar[s], kTcProducerWarps);
             mbar_init(&empty_bar[s], 1);
         }
         for (int b = 0; b < 2; ++b) {
@@ -328,27 +421,26 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     if (warp < 4 || (warp >= 8 && warp < 12)) {
         // ---------------- producers ----------------
         const int q = warp & 3;             // TMEM lane quarter
-        const int grp = warp >= 8;          // producer group: chunks of parity grp
-        const int u = q * 32 + lane;        // B row of this thread (u < 96)
-        const bool arow = lane < 30, brow = u < kTcN;
-        const uint32_t s = (uint32_t)grp;   // this group's A/B stage
-        const uint32_t ta = tbase + ((uint32_t)(32 * q) << 16) + kTcACol + s * kTcAStageCols;
-        unsigned char *bst = tc_smem + (size_t)s * kTcBStageBytes + (u >> 3) * kTcSbo + (u & 7) * 16;
-        for (int idx = grp; idx < total; idx += 2) {
-            const uint32_t j = (uint32_t)idx % kTcPStages;
+        const int h = warp >= 8;            // words 6h .. 6h+5 of each row
+        const int u = q * 32 + lane;        // B row of this thread (q < 3)
+        const bool arow = lane < 30, brow = q < 3;
+        const uint32_t ta0 = tbase + ((uint32_t)(32 * q) << 16) + kTcACol + 24 * h;
+        unsigned char *bst0 = tc_smem + (u >> 3) * kTcSbo + (6 * h) * kTcLbo + (u & 7) * 16;
+        for (int idx = 0; idx < total; ++idx) {
+            const uint32_t j = (uint32_t)idx % kTcPStages, s = (uint32_t)idx % kTcStages;
             if (!mbar_wait_warp(&pfull_bar[j], ((uint32_t)idx / kTcPStages) & 1, vabort, err, 5)) break;
-            const unsigned char *pk = tc_smem + kTcPOff + (size_t)j * kTcPStageBytes;
-            uint4 pa[3], pb[3];
+            const unsigned char *pk = tc_smem + kTcPOff + (size_t)j * kTcPStageBytes + 24 * h;
+            uint2 pa[3], pb[3];
 #pragma unroll
-            for (int m = 0; m < 3; ++m) pa[m] = pb[m] = make_uint4(0, 0, 0, 0);
+            for (int m = 0; m < 3; ++m) pa[m] = pb[m] = make_uint2(0, 0);
             if (arow) {
-                const uint4 *r = reinterpret_cast<const uint4 *>(pk + (30 * q + lane) * (kTcChunkWords * 4));
+                const uint2 *r = reinterpret_cast<const uint2 *>(pk + (30 * q + lane) * (kTcChunkWords * 4));
 #pragma unroll
                 for (int m = 0; m < 3; ++m) pa[m] = r[m];
             }
             if (brow) {
-                const uint4 *r =
-                    reinterpret_cast<const uint4 *>(pk + kTcPABytes + u * (kTcChunkWords * 4));
+                const uint2 *r =
+                    reinterpret_cast<const uint2 *>(pk + kTcPABytes + u * (kTcChunkWords * 4));
 #pragma unroll
                 for (int m = 0; m < 3; ++m) pb[m] = r[m];
             }
@@ -358,28 +450,25 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 break;
             tc_fence_after();
             {
-                uint32_t r[48];
+                uint32_t r[24];
 #pragma unroll
                 for (int m = 0; m < 3; ++m) {
-                    expand_word(pa[m].x, r + 16 * m);
-                    expand_word(pa[m].y, r + 16 * m + 4);
-                    expand_word(pa[m].z, r + 16 * m + 8);
-                    expand_word(pa[m].w, r + 16 * m + 12);
+                    expand_word(pa[m].x, r + 8 * m);
+                    expand_word(pa[m].y, r + 8 * m + 4);
                 }
-                tmem_st32(ta, r);
-                tmem_st16(ta + 32, r + 32);
+                const uint32_t ta = ta0 + s * kTcAStageCols;
+                tmem_st16(ta, r);
+                tmem_st8(ta + 16, r + 16);
             }
             if (brow) {
+                unsigned char *bst = bst0 + (size_t)s * kTcBStageBytes;
 #pragma unroll
                 for (int m = 0; m < 3; ++m) {
-                    const uint32_t w4[4] = {pb[m].x, pb[m].y, pb[m].z, pb[m].w};
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) {
-                        uint32_t o[4];
-                        expand_word(w4[e], o);
-                        *reinterpret_cast<uint4 *>(bst + (4 * m + e) * kTcLbo) =
-                            make_uint4(o[0], o[1], o[2], o[3]);
-                    }
+                    uint32_t o[8];
+                    expand_word(pb[m].x, o);
+                    expand_word(pb[m].y, o + 4);
+                    *reinterpret_cast<uint4 *>(bst + (2 * m) * kTcLbo) = make_uint4(o[0], o[1], o[2], o[3]);
+                    *reinterpret_cast<uint4 *>(bst + (2 * m + 1) * kTcLbo) = make_uint4(o[4], o[5], o[6], o[7]);
                 }
             }
             asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
@@ -387,13 +476,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&full_bar[s]);
-            if (__any_sync(0xffffffffu, *vabort != 0)) break;
         }
     } else if (warp == kTcTmaWarp) {
-        // ---------------- TMA issuer ----------------
+        // ---------------- bulk-copy issuer ----------------
         if (lane == 0) {
-            asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_a)) : "memory");
-            asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(&map_b)) : "memory");
             int issued = 0;
             int2 tl = make_int2(0, 0), tl_next = make_int2(0, 0);
             if (my_tiles > 0) tl_next = tiles[blockIdx.x];
@@ -409,13 +495,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 if (!mbar_wait(&pempty_bar[j], (((uint32_t)idx / kTcPStages) & 1) ^ 1, vabort, err, 6))
                     break;
                 unsigned char *pk = tc_smem + kTcPOff + (size_t)j * kTcPStageBytes;
-                const int x = cm.start(c);
+                const uint32_t *base = blk + (size_t)c * rows_pad * kTcChunkWords;
                 mbar_expect_tx(&pfull_bar[j], kTcPStageBytes);
-                tma_load_2d(pk, &map_a, x, 3 * (a0 + tl.x * kTcASnps), &pfull_bar[j]);
-                tma_load_2d(pk + kTcPABytes, &map_b, x, 3 * (b0 + tl.y * kTcBSnps), &pfull_bar[j]);
+                bulk_load(pk, base + (size_t)3 * (a0 + tl.x * kTcASnps) * kTcChunkWords, kTcPABytes,
+                          &pfull_bar[j]);
+                bulk_load(pk + kTcPABytes, base + (size_t)3 * (b0 + tl.y * kTcBSnps) * kTcChunkWords,
+                          kTcPBBytes, &pfull_bar[j]);
                 issued = idx + 1;
             }
-            // every tensor load this thread issued lands before the CTA exits
+            // every copy this thread issued lands before the CTA exits
             for (int idx = issued > kTcPStages ? issued - kTcPStages : 0; idx < issued; ++idx)
                 mbar_drain(&pfull_bar[idx % kTcPStages], ((uint32_t)idx / kTcPStages) & 1);
         }
@@ -527,7 +615,20 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                                 G[pp * 3 + qq] = xb[(3 * i + pp) * kTcXStride + 3 * jl + qq];
                                 G[9 + pp * 3 + qq] = xb[(3 * i + pp) * kTcXStride + 24 + 3 * jl + qq];
                             }
-                        score_tests(ctx, G, G + 9, sA, sBt, theta, lp_thr);
+                        uint32_t mask = tc_stage1<OBJ>(ctx, G, G + 9, sA == sBt, theta, lp_thr);
+                        const int y = (int)G[8], z = (int)G[17];
+                        while (mask) {
+                            const int bit = __ffs(mask) - 1;
+                            mask &= mask - 1;
+                            const int rp = bit / 5, f = bit - 5 * rp, ri = rp >> 1, rj = rp & 1;
+                            const float *g0 = xb + (3 * i) * kTcXStride + 3 * jl;
+                            const int w = fun_count((int)g0[ri * kTcXStride + rj], (int)g0[ri * kTcXStride + 2],
+                                                    (int)g0[2 * kTcXStride + rj], y, f);
+                            const int x = fun_count((int)g0[ri * kTcXStride + 24 + rj],
+                                                    (int)g0[ri * kTcXStride + 24 + 2],
+                                                    (int)g0[2 * kTcXStride + 24 + rj], z, f);
+                            tc_refine<OBJ>(ctx, 2 * sA + ri, 2 * sBt + rj, f, w, x, y, z);
+                        }
                     }
                 }
                 __syncwarp();
@@ -544,60 +645,75 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
 }
 
-namespace {
-
-PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
-        void *p = nullptr;
-        cudaDriverEntryPointQueryResult q{};
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
-                                             &q) != cudaSuccess ||
-            q != cudaDriverEntryPointSuccess)
-            p = nullptr;
-        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    }();
-    return fn;
+// Block-major operand layout (see the file comment).
+__global__ void tc_relayout_kernel(const uint32_t *__restrict__ planes, int Wp, int W0, int nrows,
+                                   int rows_pad, int n0, int nblk, uint32_t *__restrict__ blk) {
+    const size_t total = (size_t)nblk * rows_pad * kTcChunkWords;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
+         i += (size_t)gridDim.x * blockDim.x) {
+        const int w = (int)(i % kTcChunkWords);
+        const size_t br = i / kTcChunkWords;
+        const int row = (int)(br % rows_pad), b = (int)(br / rows_pad);
+        const int start = b < n0 ? kTcChunkWords * b : W0 + kTcChunkWords * (b - n0);
+        const int end = b < n0 ? W0 : Wp;
+        uint32_t v = 0;
+        if (row < nrows && start + w < end) v = planes[(size_t)row * Wp + start + w];
+        blk[i] = v;
+    }
 }
 
-// Plane rows as a 2-D uint32 tensor [nrows][Wp]; box = one chunk of `box_rows` rows.
-bool plane_map(CUtensorMap *m, const uint32_t *planes, int Wp, int nrows, int box_rows) {
-    auto enc = tensor_map_encoder();
-    if (!enc) return false;
-    const cuuint64_t dims[2] = {(cuuint64_t)Wp, (cuuint64_t)nrows};
-    const cuuint64_t strides[1] = {(cuuint64_t)Wp * 4};
-    const cuuint32_t box[2] = {(cuuint32_t)kTcChunkWords, (cuuint32_t)box_rows};
-    const cuuint32_t estr[2] = {1, 1};
-    return enc(m, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<uint32_t *>(planes), dims, strides,
-               box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+void tc_block_shape(int n_snps, int Wp, int W0, int *rows_pad, int *nblk) {
+    const int n0 = (W0 + kTcChunkWords - 1) / kTcChunkWords;
+    const int n1 = (Wp - W0 + kTcChunkWords - 1) / kTcChunkWords;
+    *rows_pad = 3 * n_snps + kTcARows;  // a box starting at any SNP's first row stays inside
+    *nblk = n0 + n1;
 }
 
-}  // namespace
+size_t tc_block_words(int n_snps, int Wp, int W0) {
+    int rows_pad, nblk;
+    tc_block_shape(n_snps, Wp, W0, &rows_pad, &nblk);
+    return (size_t)nblk * rows_pad * kTcChunkWords;
+}
 
-cudaError_t launch_tc_tiles(const uint32_t *planes, int Wp, int W0, int nrows, const int2 *tiles,
+cudaError_t launch_tc_relayout(const uint32_t *planes, int Wp, int W0, int n_snps, uint32_t *blk,
+                               int num_sms, cudaStream_t stream) {
+    int rows_pad, nblk;
+    tc_block_shape(n_snps, Wp, W0, &rows_pad, &nblk);
+    const int n0 = (W0 + kTcChunkWords - 1) / kTcChunkWords;
+    tc_relayout_kernel<<<num_sms * 8, 256, 0, stream>>>(planes, Wp, W0, 3 * n_snps, rows_pad, n0,
+                                                         nblk, blk);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tc_tiles(const uint32_t *blk, int n_snps, int Wp, int W0, const int2 *tiles,
                             int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
                             uint32_t *dump, int *err, int num_sms, cudaStream_t stream) {
     if (ntiles <= 0) return cudaSuccess;
-    // class starts and chunk starts on 16-byte TMA boundaries, whole K = 64 MMAs
-    if ((W0 & 3) || (Wp & 3) || W0 <= 0 || Wp <= W0 || (reinterpret_cast<uintptr_t>(planes) & 15))
+    // whole K = 64 MMAs per class, 16-byte aligned copies
+    if ((W0 & 1) || (Wp & 1) || W0 <= 0 || Wp <= W0 || (reinterpret_cast<uintptr_t>(blk) & 15))
         return cudaErrorInvalidValue;
-    CUtensorMap map_a, map_b;
-    if (!plane_map(&map_a, planes, Wp, nrows, kTcARows) || !plane_map(&map_b, planes, Wp, nrows, kTcN))
-        return cudaErrorInvalidValue;
+    int rows_pad, nblk;
+    tc_block_shape(n_snps, Wp, W0, &rows_pad, &nblk);
     const int grid = ntiles < num_sms ? ntiles : num_sms;
     cudaError_t e;
     if (dump) {
-        e = cudaFuncSetAttribute(tc_tile_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(tc_tile_kernel<true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)kTcSmem);
         if (e != cudaSuccess) return e;
-        tc_tile_kernel<true><<<grid, kTcThreads, kTcSmem, stream>>>(map_a, map_b, Wp, W0, tiles, ntiles,
-                                                                    a0, a1, b0, b1, ctx, dump, err);
+        tc_tile_kernel<true, 0><<<grid, kTcThreads, kTcSmem, stream>>>(
+            blk, rows_pad, Wp, W0, tiles, ntiles, a0, a1, b0, b1, ctx, dump, err);
+    } else if (ctx.objective == 0) {
+        e = cudaFuncSetAttribute(tc_tile_kernel<false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kTcSmem);
+        if (e != cudaSuccess) return e;
+        tc_tile_kernel<false, 0><<<grid, kTcThreads, kTcSmem, stream>>>(
+            blk, rows_pad, Wp, W0, tiles, ntiles, a0, a1, b0, b1, ctx, nullptr, err);
     } else {
-        e = cudaFuncSetAttribute(tc_tile_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(tc_tile_kernel<false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)kTcSmem);
         if (e != cudaSuccess) return e;
-        tc_tile_kernel<false><<<grid, kTcThreads, kTcSmem, stream>>>(
-            map_a, map_b, Wp, W0, tiles, ntiles, a0, a1, b0, b1, ctx, nullptr, err);
+        tc_tile_kernel<false, 1><<<grid, kTcThreads, kTcSmem, stream>>>(
+            blk, rows_pad, Wp, W0, tiles, ntiles, a0, a1, b0, b1, ctx, nullptr, err);
     }
     return cudaGetLastError();
 }

@@ -32,9 +32,12 @@ cudaError_t launch_decode_rows(const uint64_t *bits, const uint64_t *valid, int 
 cudaError_t launch_popc_tiles(const uint32_t *planes, int Wp, int W0, const int2 *tiles,
                               int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
                               uint32_t *dump, cudaStream_t stream);
-cudaError_t launch_tc_tiles(const uint32_t *planes, int Wp, int W0, int nrows, const int2 *tiles,
+cudaError_t launch_tc_tiles(const uint32_t *blk, int n_snps, int Wp, int W0, const int2 *tiles,
                             int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
                             uint32_t *dump, int *err, int num_sms, cudaStream_t stream);
+cudaError_t launch_tc_relayout(const uint32_t *planes, int Wp, int W0, int n_snps, uint32_t *blk,
+                               int num_sms, cudaStream_t stream);
+size_t tc_block_words(int n_snps, int Wp, int W0);
 int tc_tile_a_snps();
 int tc_tile_b_snps();
 cudaError_t run_select_compact(Cand *in, Cand *out, ScanState *st, void *sel, uint32_t cap,
@@ -60,6 +63,7 @@ struct gepi_planes {
     int device = 0, num_sms = 0;
     int n_snps = 0, S0 = 0, S1 = 0, W0 = 0, W1 = 0, Wp = 0;
     uint32_t *d_planes = nullptr;
+    uint32_t *d_tc_blocks = nullptr;  // block-major copy for the tensor-core kernel (lazy)
     cudaStream_t stream = nullptr;
     uint64_t *d_T = nullptr;
     int F = 0;
@@ -137,6 +141,7 @@ void planes_free(gepi_planes *pl) {
     DeviceGuard g(pl->device);
     if (pl->stream) cudaStreamSynchronize(pl->stream);
     dfree(pl->d_planes);
+    dfree(pl->d_tc_blocks);
     dfree(pl->d_T);
     dfree(pl->d_lf);
     dfree(pl->d_lf32);
@@ -217,6 +222,18 @@ gepi_status upload_tiles(gepi_planes *pl, const std::vector<int2> &tiles) {
 // list runs in bands of `band` A tiles: within a band every B tile is visited
 // once for all the band's A tiles, so concurrently running CTAs share B tiles
 // in L2 and each B tile is fetched from HBM about once per band.
+// The tensor-core kernel reads the planes in 384-sample blocks, block-major;
+// the copy is made on first use and kept with the plane set.
+gepi_status ensure_tc_blocks(gepi_planes *pl) {
+    if (pl->d_tc_blocks) return GEPI_OK;
+    const size_t bytes = tc_block_words(pl->n_snps, pl->Wp, pl->W0) * 4;
+    GEPI_TRY(check_mem(bytes, "tensor-core operand blocks"));
+    GEPI_CUDA(cudaMalloc(&pl->d_tc_blocks, bytes));
+    GEPI_CUDA(launch_tc_relayout(pl->d_planes, pl->Wp, pl->W0, pl->n_snps, pl->d_tc_blocks,
+                                 pl->num_sms, pl->stream));
+    return GEPI_OK;
+}
+
 void build_tiles(int a0, int a1, int b0, int b1, int TA, int TB, bool triangle, int band,
                  std::vector<int2> &out) {
     out.clear();
@@ -277,6 +294,7 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
 
     const int method = resolve_method(par->method);
     const bool tc = method == GEPI_METHOD_TENSOR;
+    if (tc) GEPI_TRY(ensure_tc_blocks(pl));
     const int TA = tc ? tc_tile_a_snps() : popc_tile_snps();
     const int TB = tc ? tc_tile_b_snps() : popc_tile_snps();
     std::vector<int2> tiles;
@@ -336,7 +354,7 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
         ctx.cand = pl->d_cand[cur];
         GEPI_CUDA(cudaEventRecord(pl->ev[2], pl->stream));
         if (tc)
-            GEPI_CUDA(launch_tc_tiles(pl->d_planes, pl->Wp, pl->W0, 3 * pl->n_snps,
+            GEPI_CUDA(launch_tc_tiles(pl->d_tc_blocks, pl->n_snps, pl->Wp, pl->W0,
                                       pl->d_tiles + t, (int)nbt, a0, a0 + na, b0, b0 + nb, ctx,
                                       nullptr, &pl->d_state->kerr, pl->num_sms, pl->stream));
         else
@@ -617,6 +635,7 @@ gepi_status gepi_pair_counts(gepi_planes *pl, int method, int a0, int na, int b0
     DeviceGuard g(pl->device);
     if (!g.ok) return set_error(GEPI_ERR_CUDA, "cudaSetDevice failed");
     const bool tc = resolve_method(method) == GEPI_METHOD_TENSOR;
+    if (tc) GEPI_TRY(ensure_tc_blocks(pl));
     std::vector<int2> tiles;
     build_tiles(a0, a0 + na, b0, b0 + nb, tc ? tc_tile_a_snps() : popc_tile_snps(),
                 tc ? tc_tile_b_snps() : popc_tile_snps(), false, 8, tiles);
@@ -631,7 +650,7 @@ gepi_status gepi_pair_counts(gepi_planes *pl, int method, int a0, int na, int b0
     int herr = 0;
     cudaError_t e = cudaMemsetAsync(d_err, 0, sizeof(int), pl->stream);
     if (e == cudaSuccess)
-        e = tc ? launch_tc_tiles(pl->d_planes, pl->Wp, pl->W0, 3 * pl->n_snps, pl->d_tiles,
+        e = tc ? launch_tc_tiles(pl->d_tc_blocks, pl->n_snps, pl->Wp, pl->W0, pl->d_tiles,
                                  (int)tiles.size(), a0, a0 + na, b0, b0 + nb, ctx, d_out, d_err,
                                  pl->num_sms, pl->stream)
                : launch_popc_tiles(pl->d_planes, pl->Wp, pl->W0, pl->d_tiles, (int)tiles.size(),

@@ -126,6 +126,9 @@ def lib():
     L.gepi_pair_counts.argtypes = [P, i32, i32, i32, i32, i32, P]
     L.gepi_process_gpu_1.argtypes = [P, P, i32, i32, P, P, P, ctypes.POINTER(_Params)]
     L.gepi_last_scan_stats.argtypes = [P, ctypes.POINTER(_ScanStats)]
+    L.gepi_planes_autotune.argtypes = [P, ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_float),
+                                       ctypes.POINTER(ctypes.c_float)]
+    L.gepi_tensor_peak_tflops.argtypes = [i32, ctypes.POINTER(ctypes.c_double)]
     L.gepi_process_gpu_1_noalloc.argtypes = [P, P, i32, i32, P, P, P, ctypes.POINTER(_Params)]
     L.gepi_fisher_pval.argtypes = [i32, i32, i32, i32]
     L.gepi_fisher_pval.restype = ctypes.c_float
@@ -138,7 +141,8 @@ def lib():
     for f in ("gepi_plink_open", "gepi_plink_row_info", "gepi_plink_decode_rows",
               "gepi_planes_from_bed", "gepi_planes_from_rows", "gepi_planes_class_sizes",
               "gepi_scan", "gepi_scan_range", "gepi_pair_counts", "gepi_process_gpu_1",
-              "gepi_last_scan_stats", "gepi_process_gpu_1_noalloc",
+              "gepi_last_scan_stats", "gepi_process_gpu_1_noalloc", "gepi_planes_autotune",
+              "gepi_tensor_peak_tflops",
               "gepi_synth_bed", "gepi_synth_write"):
         getattr(L, f).restype = i32
     _lib = L
@@ -332,6 +336,15 @@ class Planes:
         _check(lib().gepi_pair_counts(self._h, method, a0, na, b0, nb, _ptr(out)))
         return out
 
+    def autotune(self) -> dict:
+        """The counting method METHOD_AUTO uses on these planes, with the two
+        kernels' timings on the tuning triangle (tuned on first use)."""
+        m = ctypes.c_int32()
+        tp, tt = ctypes.c_float(), ctypes.c_float()
+        _check(lib().gepi_planes_autotune(self._h, ctypes.byref(m), ctypes.byref(tp),
+                                          ctypes.byref(tt)))
+        return {"method": m.value, "popc_ms": tp.value, "tensor_ms": tt.value}
+
     def last_stats(self) -> dict:
         """Device timings and counters of the last scan on these planes."""
         st = _ScanStats()
@@ -381,6 +394,13 @@ def process_gpu_1_noalloc(pr: BinPlinkReader, tops: np.ndarray, par: Params) -> 
     _check(lib().gepi_process_gpu_1_noalloc(_ptr(bits), _ptr(valid), bits.shape[0],
                                             bits.shape[1], _ptr(m1), _ptr(m2), _ptr(tops),
                                             ctypes.byref(par._c())))
+
+
+def tensor_peak_tflops(device: int = 0) -> float:
+    """Dense kind::mxf4 tensor-core rate of `device` (TFLOP/s), measured now."""
+    v = ctypes.c_double()
+    _check(lib().gepi_tensor_peak_tflops(device, ctypes.byref(v)))
+    return v.value
 
 
 def fisher_pval(n11: int, n12: int, n21: int, n22: int) -> float:

@@ -54,6 +54,7 @@
 // memory and returns.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "device.cuh"
@@ -716,6 +717,111 @@ cudaError_t launch_tc_tiles(const uint32_t *blk, int n_snps, int Wp, int W0, con
             blk, rows_pad, Wp, W0, tiles, ntiles, a0, a1, b0, b1, ctx, nullptr, err);
     }
     return cudaGetLastError();
+}
+
+// Dense kind::mxf4 MMA rate of this GPU, the roofline denominator of the
+// tensor-core counting kernel: one CTA per SM issues `iters` back-to-back
+// M=128 x N=256 x K=64 MMAs (A in tensor memory, B in shared memory, unit
+// scales) and waits for them once.
+constexpr uint32_t kTcPeakIdesc = (1u << 7) | (1u << 10) | ((uint32_t)(256 >> 3) << 17) |
+                                  (1u << 23) | ((uint32_t)(128 >> 4) << 24);
+constexpr int kTcPeakSmem = 120 * 1024;  // one CTA per SM
+
+__global__ void __launch_bounds__(128, 1) tc_peak_kernel(int iters, int *err) {
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    __shared__ uint64_t done_bar;
+    __shared__ uint32_t tmem_slot;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int i = tid; i < 8192 / 4; i += blockDim.x)
+        reinterpret_cast<uint32_t *>(tc_smem)[i] = 0x22222222u;  // E2M1 1.0
+    if (tid == 0) {
+        mbar_init(&done_bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         su32(&tmem_slot)),
+                     "r"(kTcCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = tmem_slot;
+    {
+        uint32_t r[32];
+#pragma unroll
+        for (int k = 0; k < 32; ++k) r[k] = 0x7F7F7F7Fu;
+        tmem_st32(tbase + ((uint32_t)(32 * warp) << 16) + kTcSfCol, r);
+#pragma unroll
+        for (int k = 0; k < 32; ++k) r[k] = 0x22222222u;
+        tmem_st32(tbase + ((uint32_t)(32 * warp) << 16) + 256, r);
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+        tc_fence_after();
+        // 256 B rows x 32 B (one K = 64 block): core matrices 128 B apart along K,
+        // 8-row groups 256 B apart
+        const uint64_t bd = (uint64_t)((su32(tc_smem) & 0x3FFFF) >> 4) | ((uint64_t)(128 >> 4) << 16) |
+                            ((uint64_t)(256 >> 4) << 32) | (1ull << 46);
+        const uint32_t sf = tbase + kTcSfCol;
+        for (int i = 0; i < iters; ++i)
+            asm volatile(
+                "{\n .reg .pred p;\n setp.ne.b32 p, %5, 0;\n"
+                " tcgen05.mma.cta_group::1.kind::mxf4.block_scale.scale_vec::2X [%0], [%1], %2, %3, [%4], "
+                "[%4], p;\n}\n" ::"r"(tbase),
+                "r"(tbase + 256), "l"(bd), "r"(kTcPeakIdesc), "r"(sf), "r"(i > 0 ? 1u : 0u));
+        tc_commit(&done_bar);
+        const long long t0 = clock64();
+        while (!mbar_try(&done_bar, 0)) {
+            if (clock64() - t0 > kTcWaitCycles) {
+                atomicExch(err, 7);
+                break;
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(kTcCols)
+                     : "memory");
+    }
+}
+
+// Best of `reps` timed launches; TFLOP/s counting 2 per multiply-accumulate.
+cudaError_t tc_measure_peak(int num_sms, int reps, double *tflops, int *err, cudaStream_t stream) {
+    cudaError_t e = cudaFuncSetAttribute(tc_peak_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         kTcPeakSmem);
+    if (e != cudaSuccess) return e;
+    cudaEvent_t e0, e1;
+    if ((e = cudaEventCreate(&e0)) != cudaSuccess) return e;
+    if ((e = cudaEventCreate(&e1)) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return e;
+    }
+    const int iters = 16384;
+    double best = 0.0;
+    for (int r = 0; r < reps + 1 && e == cudaSuccess; ++r) {
+        cudaEventRecord(e0, stream);
+        tc_peak_kernel<<<num_sms, 128, kTcPeakSmem, stream>>>(iters, err);
+        cudaEventRecord(e1, stream);
+        e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaGetLastError();
+        float ms = 0.f;
+        if (e == cudaSuccess && r > 0 && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess && ms > 0.f) {
+            const double flop = 2.0 * num_sms * (double)iters * 128.0 * 256.0 * 64.0;
+            best = std::max(best, flop / (ms * 1e-3) / 1e12);
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *tflops = best;
+    return e;
 }
 
 int tc_tile_a_snps() { return kTcASnps; }

@@ -38,6 +38,7 @@ cudaError_t launch_tc_tiles(const uint32_t *blk, int n_snps, int Wp, int W0, con
 cudaError_t launch_tc_relayout(const uint32_t *planes, int Wp, int W0, int n_snps, uint32_t *blk,
                                int num_sms, cudaStream_t stream);
 size_t tc_block_words(int n_snps, int Wp, int W0);
+cudaError_t tc_measure_peak(int num_sms, int reps, double *tflops, int *err, cudaStream_t stream);
 int tc_tile_a_snps();
 int tc_tile_b_snps();
 cudaError_t run_select_compact(Cand *in, Cand *out, ScanState *st, void *sel, uint32_t cap,
@@ -61,6 +62,8 @@ using namespace gepi;
 
 struct gepi_planes {
     int device = 0, num_sms = 0;
+    int auto_method = 0;  // AUTO's choice for this plane set (0 = not tuned yet)
+    float tune_ms[2] = {0.f, 0.f};  // autotuner timings: popcount, tensor core
     int n_snps = 0, S0 = 0, S1 = 0, W0 = 0, W1 = 0, Wp = 0;
     uint32_t *d_planes = nullptr;
     uint32_t *d_tc_blocks = nullptr;  // block-major copy for the tensor-core kernel (lazy)
@@ -265,9 +268,84 @@ gepi_status ensure_events(gepi_planes *pl, size_t n) {
 }
 
 // GEPI_METHOD_AUTO picks the counting form.
-int resolve_method(int m) {
-    if (m == GEPI_METHOD_POPC || m == GEPI_METHOD_TENSOR) return m;
-    return GEPI_METHOD_POPC;
+// Device time of one counting-kernel launch over the triangle of SNPs [0, n)
+// with a threshold nothing passes (the steady state of a long scan, where the
+// fused bounds reject almost every test).  The first launch warms up.
+gepi_status time_count_kernel(gepi_planes *pl, bool tc, int n, float *ms) {
+    if (tc) GEPI_TRY(ensure_tc_blocks(pl));
+    std::vector<int2> tiles;
+    const int T0 = tc ? tc_tile_a_snps() : popc_tile_snps();
+    const int T1 = tc ? tc_tile_b_snps() : popc_tile_snps();
+    build_tiles(0, n, 0, n, T0, T1, true, 8, tiles);
+    GEPI_TRY(upload_tiles(pl, tiles));
+    GEPI_TRY(ensure_events(pl, 4));
+    ScanState st{};
+    st.tau_key = ~0ull;
+    st.theta = INFINITY;
+    st.lp_thr = -INFINITY;
+    st.tau_f = INFINITY;
+    st.tau_val = INFINITY;
+    *pl->h_state = st;
+    GEPI_CUDA(cudaMemcpyAsync(pl->d_state, pl->h_state, sizeof(ScanState), cudaMemcpyHostToDevice,
+                              pl->stream));
+    ScanCtx ctx;
+    ctx.T = pl->d_T;
+    ctx.F = pl->F;
+    ctx.lf = pl->d_lf;
+    ctx.lf32 = pl->d_lf32;
+    ctx.objective = GEPI_ENTROPY;
+    ctx.cap = pl->cap;
+    ctx.st = pl->d_state;
+    ctx.cand = pl->d_cand[0];
+    for (int rep = 0; rep < 2; ++rep) {
+        GEPI_CUDA(cudaEventRecord(pl->ev[2], pl->stream));
+        if (tc)
+            GEPI_CUDA(launch_tc_tiles(pl->d_tc_blocks, pl->n_snps, pl->Wp, pl->W0, pl->d_tiles,
+                                      (int)tiles.size(), 0, n, 0, n, ctx, nullptr,
+                                      &pl->d_state->kerr, pl->num_sms, pl->stream));
+        else
+            GEPI_CUDA(launch_popc_tiles(pl->d_planes, pl->Wp, pl->W0, pl->d_tiles, (int)tiles.size(),
+                                        0, n, 0, n, ctx, nullptr, pl->stream));
+        GEPI_CUDA(cudaEventRecord(pl->ev[3], pl->stream));
+    }
+    GEPI_CUDA(cudaMemcpyAsync(pl->h_state, pl->d_state, sizeof(ScanState), cudaMemcpyDeviceToHost,
+                              pl->stream));
+    GEPI_CUDA(cudaStreamSynchronize(pl->stream));
+    if (pl->h_state->kerr)
+        return set_error(GEPI_ERR_TIMEOUT, "counting kernel gave up a bounded wait (code " +
+                                               std::to_string(pl->h_state->kerr) + ")");
+    GEPI_CUDA(cudaEventElapsedTime(ms, pl->ev[2], pl->ev[3]));
+    return GEPI_OK;
+}
+
+// Counting method for a request.  AUTO is tuned once per plane set: both
+// counting kernels are timed on the leading triangle of up to 4,096 SNPs at
+// the set's full sample width (sample count is what moves the crossover: the
+// tensor-core kernel's fixed per-tile epilogue is amortised over the samples),
+// and the faster one is kept.  Plane sets of fewer than 256 SNPs use the
+// popcount kernel without timing.
+gepi_status resolve_method(gepi_planes *pl, int m, int *out) {
+    if (m == GEPI_METHOD_POPC || m == GEPI_METHOD_TENSOR) {
+        *out = m;
+        return GEPI_OK;
+    }
+    if (!pl->auto_method) {
+        if (pl->n_snps < 256) {
+            pl->auto_method = GEPI_METHOD_POPC;
+        } else {
+            GEPI_TRY(ensure_tables(pl));
+            GEPI_TRY(ensure_scan_buffers(pl, 1));
+            const int n = std::min(pl->n_snps, 4096);
+            float t_popc = 0.f, t_tc = 0.f;
+            GEPI_TRY(time_count_kernel(pl, false, n, &t_popc));
+            GEPI_TRY(time_count_kernel(pl, true, n, &t_tc));
+            pl->auto_method = t_tc < t_popc ? GEPI_METHOD_TENSOR : GEPI_METHOD_POPC;
+            pl->tune_ms[0] = t_popc;
+            pl->tune_ms[1] = t_tc;
+        }
+    }
+    *out = pl->auto_method;
+    return GEPI_OK;
 }
 
 bool cand_better(const Cand &a, const Cand &b) {
@@ -292,7 +370,8 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
     GEPI_TRY(ensure_scan_buffers(pl, k));
     std::memset(tops, 0, sizeof(gepi_result) * (size_t)k);
 
-    const int method = resolve_method(par->method);
+    int method = 0;
+    GEPI_TRY(resolve_method(pl, par->method, &method));
     const bool tc = method == GEPI_METHOD_TENSOR;
     if (tc) GEPI_TRY(ensure_tc_blocks(pl));
     const int TA = tc ? tc_tile_a_snps() : popc_tile_snps();
@@ -634,7 +713,9 @@ gepi_status gepi_pair_counts(gepi_planes *pl, int method, int a0, int na, int b0
         return set_error(GEPI_ERR_ARG, "gepi_pair_counts: unknown method");
     DeviceGuard g(pl->device);
     if (!g.ok) return set_error(GEPI_ERR_CUDA, "cudaSetDevice failed");
-    const bool tc = resolve_method(method) == GEPI_METHOD_TENSOR;
+    int resolved = 0;
+    GEPI_TRY(resolve_method(pl, method, &resolved));
+    const bool tc = resolved == GEPI_METHOD_TENSOR;
     if (tc) GEPI_TRY(ensure_tc_blocks(pl));
     std::vector<int2> tiles;
     build_tiles(a0, a0 + na, b0, b0 + nb, tc ? tc_tile_a_snps() : popc_tile_snps(),
@@ -664,6 +745,39 @@ gepi_status gepi_pair_counts(gepi_planes *pl, int method, int a0, int na, int b0
     if (herr)
         return set_error(GEPI_ERR_TIMEOUT, "counting kernel gave up a bounded wait (code " +
                                                std::to_string(herr) + ")");
+    return GEPI_OK;
+}
+
+gepi_status gepi_planes_autotune(gepi_planes *pl, int32_t *method, float *popc_ms,
+                                 float *tensor_ms) {
+    clear_error();
+    if (!pl) return set_error(GEPI_ERR_ARG, "gepi_planes_autotune: null planes");
+    DeviceGuard g(pl->device);
+    if (!g.ok) return set_error(GEPI_ERR_CUDA, "cudaSetDevice failed");
+    int m = 0;
+    GEPI_TRY(resolve_method(pl, GEPI_METHOD_AUTO, &m));
+    if (method) *method = m;
+    if (popc_ms) *popc_ms = pl->tune_ms[0];
+    if (tensor_ms) *tensor_ms = pl->tune_ms[1];
+    return GEPI_OK;
+}
+
+gepi_status gepi_tensor_peak_tflops(int device, double *tflops) {
+    clear_error();
+    if (!tflops) return set_error(GEPI_ERR_ARG, "gepi_tensor_peak_tflops: null output");
+    DeviceGuard g(device);
+    if (!g.ok) return set_error(GEPI_ERR_CUDA, "cudaSetDevice failed");
+    int sms = 0;
+    GEPI_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    int *d_err = nullptr;
+    GEPI_CUDA(cudaMalloc(&d_err, sizeof(int)));
+    cudaError_t e = cudaMemset(d_err, 0, sizeof(int));
+    if (e == cudaSuccess) e = tc_measure_peak(sms, 3, tflops, d_err, 0);
+    int herr = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(d_err);
+    if (e != cudaSuccess) return set_error(GEPI_ERR_CUDA, std::string("tensor peak: ") + cudaGetErrorString(e));
+    if (herr) return set_error(GEPI_ERR_TIMEOUT, "tensor peak kernel gave up its bounded wait");
     return GEPI_OK;
 }
 

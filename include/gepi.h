@@ -178,6 +178,23 @@ typedef struct gepi_scan_stats {
 } gepi_scan_stats;
 gepi_status gepi_last_scan_stats(const gepi_planes *pl, gepi_scan_stats *out);
 
+/* Counting-method autotuner (replaces the reference's --block-sizes /
+ * --max-grid-area tuning, gEpiCount.cpp:135-141 and misc1.cu:35-89, which
+ * size its batch grid).  GEPI_METHOD_AUTO requests on `pl` use the method this
+ * picks: the first call times both counting kernels on the leading triangle
+ * of up to 4,096 SNPs at the plane set's full sample width and keeps the
+ * faster; later calls return the cached choice.  Sets under 256 SNPs use
+ * the popcount kernel untimed (times reported as 0).  Outputs may be NULL. */
+gepi_status gepi_planes_autotune(gepi_planes *pl, int32_t *method, float *popc_ms,
+                                 float *tensor_ms);
+
+/* Dense kind::mxf4 (packed FP4) tensor-core rate of `device` in TFLOP/s (2 per
+ * multiply-accumulate), measured now: one CTA per SM issues back-to-back
+ * M=128 x N=256 x K=64 MMAs; best of 3 timed launches.  It is the roofline
+ * denominator of the tensor-core counting kernel.  No counterpart in the
+ * reference. */
+gepi_status gepi_tensor_peak_tflops(int32_t device, double *tflops);
+
 /* ---- drop-in for the reference's process_gpu_1 ----------------------------- */
 /* Same inputs as process_gpu_1 reads from its PlinkReader (BitData, ValidData,
  * numSNPs() = n_rows, elementsSNP() = n_words, classData(1|2)->mask()), same

@@ -142,14 +142,37 @@ def test_scan_is_deterministic_and_method_independent(gepi, tmp_path):
     pl.close()
 
 
+def test_autotune_choice_drives_auto(gepi, tmp_path):
+    """METHOD_AUTO uses the autotuner's pick; both methods give the same list."""
+    kw = dict(n_snps=400, n_cases=600, n_controls=700, missing=0.02, seed=91)
+    pl, rows, fs, _ = make_planes(gepi, kw, tmp_path)
+    t = pl.autotune()
+    assert t["method"] in (METHODS["popc"], METHODS["tensor"])
+    assert t["popc_ms"] > 0 and t["tensor_ms"] > 0
+    assert (t["tensor_ms"] < t["popc_ms"]) == (t["method"] == METHODS["tensor"])
+    assert pl.autotune() == t  # cached per plane set
+    a = pl.scan(300)
+    assert pl.last_stats()["method"] == t["method"]
+    b = pl.scan(300, method=METHODS["popc"] + METHODS["tensor"] - t["method"])
+    assert a.tobytes() == b.tobytes()
+    want, _, _ = H.oracle_topk(rows, 300)
+    assert_same_topk(a, want)
+    pl.close()
+    small, _, _, _ = make_planes(gepi, dict(n_snps=100, n_cases=50, n_controls=60, seed=92),
+                                 tmp_path, "s")
+    assert small.autotune() == {"method": METHODS["popc"], "popc_ms": 0.0, "tensor_ms": 0.0}
+    small.close()
+
+
+@pytest.mark.parametrize("method", sorted(METHODS))
 @pytest.mark.parametrize("cap", ["4096", "20000"])
-def test_scan_exact_under_candidate_overflow(gepi, tmp_path, cap, monkeypatch):
+def test_scan_exact_under_candidate_overflow(gepi, tmp_path, cap, monkeypatch, method):
     """A tiny candidate buffer forces overflow, select, compaction and batch
     retries; the result must stay exact."""
     kw = dict(n_snps=200, n_cases=150, n_controls=170, missing=0.03, seed=31)
     pl, rows, fs, _ = make_planes(gepi, kw, tmp_path)
     monkeypatch.setenv("GEPI_DEBUG_CAP", cap)
-    got = pl.scan(300)
+    got = pl.scan(300, method=METHODS[method])
     monkeypatch.delenv("GEPI_DEBUG_CAP")
     want, _, _ = H.oracle_topk(rows, 300)
     assert_same_topk(got, want)
@@ -194,14 +217,15 @@ def test_process_gpu_1_dropin(gepi, tmp_path):
     assert_same_topk(tops, want)
 
 
+@pytest.mark.parametrize("method", sorted(METHODS))
 @pytest.mark.parametrize("kw", [
     dict(n_snps=60, n_cases=70, n_controls=65, missing=0.02, seed=81),
     dict(n_snps=40, n_cases=300, n_controls=420, missing=0.05, n_planted=2, seed=82),
 ])
-def test_scan_fisher_matches_oracle(gepi, tmp_path, kw):
+def test_scan_fisher_matches_oracle(gepi, tmp_path, kw, method):
     pl, rows, fs, _ = make_planes(gepi, kw, tmp_path)
     k = 150
-    got = pl.scan(k, objective=gepi.FISHER)
+    got = pl.scan(k, objective=gepi.FISHER, method=METHODS[method])
     want, keys, nranked = H.oracle_topk(rows, k, objective=1)
     assert nranked >= k
     # values: every returned test re-scored by the oracle within tolerance

@@ -39,6 +39,10 @@ CONFIGS = {
                  missing=0.01, n_planted=3, seed=1002, k=1000),
     "cfg3": dict(n_snps=100000, n_cases=5000, n_controls=5000, maf_lo=0.01, maf_hi=0.5,
                  missing=0.01, n_planted=10, seed=1003, k=10000),
+    # profiling case: cfg3's sample width on 40,000 SNPs (planes 154 MB, above L2;
+    # a scan of ~0.1 s), small enough for full ncu captures
+    "prof40k": dict(n_snps=40000, n_cases=5000, n_controls=5000, maf_lo=0.01, maf_hi=0.5,
+                    missing=0.01, n_planted=4, seed=1005, k=1000),
 }
 METRIC = "pair-tests/sec at 100k SNP x 10k samples"
 UNIT = "pair-tests/s"

@@ -137,10 +137,6 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t b
         : "memory");
 }
 
-// Warp-uniform bounded wait: lane 0 polls, the verdict is broadcast.
-__device__ __forceinline__ bool mbar_wait_warp(uint64_t *b, uint32_t parity,
-                                               volatile int *abort_flag, int *err, int code);
-
 // Bounded wait; false when the CTA aborts or the clock budget runs out.
 __device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, volatile int *abort_flag,
                                           int *err, int code) {
@@ -157,11 +153,20 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, volatile
     return true;
 }
 
+// Warp-wide bounded wait: every lane polls the same barrier, so the warp
+// never diverges (a lane-0 poll plus a broadcast costs a reconvergence per
+// wait).
 __device__ __forceinline__ bool mbar_wait_warp(uint64_t *b, uint32_t parity,
                                                volatile int *abort_flag, int *err, int code) {
-    int ok = 0;
-    if ((threadIdx.x & 31) == 0) ok = mbar_wait(b, parity, abort_flag, err, code) ? 1 : 0;
-    return __shfl_sync(0xffffffffu, ok, 0) != 0;
+    return mbar_wait(b, parity, abort_flag, err, code);
+}
+
+// One arrival per warp, by a lane elected in-line (predicated, no branch).
+__device__ __forceinline__ void mbar_arrive_warp(uint64_t *b) {
+    asm volatile(
+        "{\n .reg .pred p;\n elect.sync _|p, 0xffffffff;\n"
+        " @p mbarrier.arrive.shared::cta.b64 _, [%0];\n}\n" ::"r"(su32(b))
+        : "memory");
 }
 
 __device__ __forceinline__ void tc_fence_before() {
@@ -425,20 +430,26 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const int h = warp >= 8;            // words 6h .. 6h+5 of each row
         const int u = q * 32 + lane;        // B row of this thread (q < 3)
         const bool arow = lane < 30, brow = q < 3;
+        const int arow_off = (30 * q + (arow ? lane : 29)) * (kTcChunkWords * 4);
         const uint32_t ta0 = tbase + ((uint32_t)(32 * q) << 16) + kTcACol + 24 * h;
         unsigned char *bst0 = tc_smem + (u >> 3) * kTcSbo + (6 * h) * kTcLbo + (u & 7) * 16;
         for (int idx = 0; idx < total; ++idx) {
             const uint32_t j = (uint32_t)idx % kTcPStages, s = (uint32_t)idx % kTcStages;
             if (!mbar_wait_warp(&pfull_bar[j], ((uint32_t)idx / kTcPStages) & 1, vabort, err, 5)) break;
             const unsigned char *pk = tc_smem + kTcPOff + (size_t)j * kTcPStageBytes + 24 * h;
+            // every lane loads (lanes 30, 31 re-read row 30q+29 and clear it): no divergence
             uint2 pa[3], pb[3];
+            {
+                const uint2 *r = reinterpret_cast<const uint2 *>(pk + arow_off);
 #pragma unroll
-            for (int m = 0; m < 3; ++m) pa[m] = pb[m] = make_uint2(0, 0);
-            if (arow) {
-                const uint2 *r = reinterpret_cast<const uint2 *>(pk + (30 * q + lane) * (kTcChunkWords * 4));
-#pragma unroll
-                for (int m = 0; m < 3; ++m) pa[m] = r[m];
+                for (int m = 0; m < 3; ++m) {
+                    pa[m] = r[m];
+                    pa[m].x = arow ? pa[m].x : 0u;
+                    pa[m].y = arow ? pa[m].y : 0u;
+                }
             }
+#pragma unroll
+            for (int m = 0; m < 3; ++m) pb[m] = make_uint2(0, 0);
             if (brow) {
                 const uint2 *r =
                     reinterpret_cast<const uint2 *>(pk + kTcPABytes + u * (kTcChunkWords * 4));
@@ -446,7 +457,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 for (int m = 0; m < 3; ++m) pb[m] = r[m];
             }
             __syncwarp();
-            if (lane == 0) mbar_arrive(&pempty_bar[j]);
+            mbar_arrive_warp(&pempty_bar[j]);
             if (!mbar_wait_warp(&empty_bar[s], (((uint32_t)idx / kTcStages) & 1) ^ 1, vabort, err, 1))
                 break;
             tc_fence_after();
@@ -476,7 +487,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             tc_fence_before();
             __syncwarp();
-            if (lane == 0) mbar_arrive(&full_bar[s]);
+            mbar_arrive_warp(&full_bar[s]);
         }
     } else if (warp == kTcTmaWarp) {
         // ---------------- bulk-copy issuer ----------------
@@ -579,7 +590,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 if (g8 == 2 * eh + 1) {
                     tc_fence_before();
                     __syncwarp();
-                    if (lane == 0) mbar_arrive(&dempty_bar[b]);
+                    mbar_arrive_warp(&dempty_bar[b]);
                 }
                 if (DUMP) {
                     if (lane < 30 && sA < a1) {

@@ -26,7 +26,7 @@ import numpy as np
 __all__ = [
     "GepiError", "RESULT_DTYPE", "FUNC_NAMES", "Params", "BinPlinkReader", "Planes",
     "process_gpu_1", "process_gpu_1_noalloc", "fisher_pval", "fisher_log10p", "SynthSpec", "synth_bed", "synth_write",
-    "library_path", "lib",
+    "library_path", "lib", "ScanRequest", "scan_batch", "Server",
 ]
 
 _PKG = os.path.dirname(os.path.abspath(__file__))
@@ -77,6 +77,19 @@ class _ScanStats(ctypes.Structure):
                 ("diag_snps", ctypes.c_uint64), ("tiles", ctypes.c_uint64),
                 ("candidates", ctypes.c_uint64), ("method", ctypes.c_int32),
                 ("tile_snps", ctypes.c_int32)]
+
+
+class _ScanReq(ctypes.Structure):
+    _fields_ = [("planes", ctypes.c_void_p), ("a0", ctypes.c_int32), ("na", ctypes.c_int32),
+                ("b0", ctypes.c_int32), ("nb", ctypes.c_int32), ("topmost", ctypes.c_int32),
+                ("objective", ctypes.c_int32), ("method", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+class _RequestInfo(ctypes.Structure):
+    _fields_ = [("queue_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
+                ("device_ms", ctypes.c_double), ("snp_pairs", ctypes.c_uint64),
+                ("method", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 _lib = None
@@ -130,6 +143,13 @@ def lib():
                                        ctypes.POINTER(ctypes.c_float)]
     L.gepi_tensor_peak_tflops.argtypes = [i32, ctypes.POINTER(ctypes.c_double)]
     L.gepi_process_gpu_1_noalloc.argtypes = [P, P, i32, i32, P, P, P, ctypes.POINTER(_Params)]
+    L.gepi_scan_batch.argtypes = [ctypes.POINTER(_ScanReq), i32, ctypes.POINTER(P),
+                                  ctypes.POINTER(_ScanStats)]
+    L.gepi_server_create.argtypes = [i32, sz, PP]
+    L.gepi_server_submit.argtypes = [P, ctypes.POINTER(_ScanReq), ctypes.POINTER(u64)]
+    L.gepi_server_wait.argtypes = [P, u64, P, ctypes.POINTER(_RequestInfo)]
+    L.gepi_server_destroy.argtypes = [P]
+    L.gepi_server_destroy.restype = None
     L.gepi_fisher_pval.argtypes = [i32, i32, i32, i32]
     L.gepi_fisher_pval.restype = ctypes.c_float
     L.gepi_fisher_log10p.argtypes = [i32, i32, i32, i32]
@@ -142,7 +162,8 @@ def lib():
               "gepi_planes_from_bed", "gepi_planes_from_rows", "gepi_planes_class_sizes",
               "gepi_scan", "gepi_scan_range", "gepi_pair_counts", "gepi_process_gpu_1",
               "gepi_last_scan_stats", "gepi_process_gpu_1_noalloc", "gepi_planes_autotune",
-              "gepi_tensor_peak_tflops",
+              "gepi_tensor_peak_tflops", "gepi_scan_batch", "gepi_server_create",
+              "gepi_server_submit", "gepi_server_wait",
               "gepi_synth_bed", "gepi_synth_write"):
         getattr(L, f).restype = i32
     _lib = L
@@ -394,6 +415,83 @@ def process_gpu_1_noalloc(pr: BinPlinkReader, tops: np.ndarray, par: Params) -> 
     _check(lib().gepi_process_gpu_1_noalloc(_ptr(bits), _ptr(valid), bits.shape[0],
                                             bits.shape[1], _ptr(m1), _ptr(m2), _ptr(tops),
                                             ctypes.byref(par._c())))
+
+
+# ---- many scans at once --------------------------------------------------------
+@dataclass
+class ScanRequest:
+    """One scan: SNP ranges [a0, a0+na) x [b0, b0+nb) of `planes` (na or nb
+    negative: the whole plane set), the k best by `objective`."""
+    planes: Planes
+    k: int
+    objective: int = ENTROPY
+    method: int = METHOD_AUTO
+    a0: int = 0
+    na: int = -1
+    b0: int = 0
+    nb: int = -1
+
+    def _c(self) -> _ScanReq:
+        return _ScanReq(self.planes._h, self.a0, self.na, self.b0, self.nb, self.k,
+                        self.objective, self.method, 0)
+
+
+def scan_batch(reqs, with_stats: bool = False):
+    """Runs the requests together (gepi_scan_batch); returns one RESULT_DTYPE
+    array per request (and the per-request scan stats if asked)."""
+    reqs = list(reqs)
+    n = len(reqs)
+    creqs = (_ScanReq * n)(*[r._c() for r in reqs])
+    outs = [np.zeros(r.k, dtype=RESULT_DTYPE) for r in reqs]
+    ptrs = (ctypes.c_void_p * n)(*[_ptr(o) for o in outs])
+    stats = (_ScanStats * n)()
+    _check(lib().gepi_scan_batch(creqs, n, ptrs, stats))
+    if with_stats:
+        return outs, [{f: getattr(st, f) for f, _ in _ScanStats._fields_} for st in stats]
+    return outs
+
+
+class Server:
+    """The serving loop (gepi_server_*): submit() returns a ticket at once,
+    wait(ticket) blocks for that request's results and timings."""
+
+    def __init__(self, device: int = 0, hbm_budget_bytes: int = 0):
+        h = ctypes.c_void_p()
+        _check(lib().gepi_server_create(device, hbm_budget_bytes, ctypes.byref(h)))
+        self._h = h
+        self._k = {}
+
+    def submit(self, req: ScanRequest) -> int:
+        t = ctypes.c_uint64()
+        c = req._c()
+        _check(lib().gepi_server_submit(self._h, ctypes.byref(c), ctypes.byref(t)))
+        self._k[t.value] = req.k
+        return t.value
+
+    def wait(self, ticket: int):
+        """(results, info dict) of the ticket's request."""
+        k = self._k.pop(ticket, 1)
+        tops = np.zeros(k, dtype=RESULT_DTYPE)
+        info = _RequestInfo()
+        _check(lib().gepi_server_wait(self._h, ticket, _ptr(tops), ctypes.byref(info)))
+        return tops, {f: getattr(info, f) for f, _ in _RequestInfo._fields_ if f != "reserved"}
+
+    def close(self):
+        if self._h:
+            lib().gepi_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def tensor_peak_tflops(device: int = 0) -> float:

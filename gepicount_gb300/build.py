@@ -24,7 +24,8 @@ LIB = os.path.join(OUT, "libgepi.so")
 CLI = os.path.join(OUT, "gepi")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["scan.cu", "decode.cu", "count_popc.cu", "select.cu", "noalloc.cu", "count_tc.cu"]
+CU_SOURCES = ["scan.cu", "decode.cu", "count_popc.cu", "select.cu", "noalloc.cu", "count_tc.cu",
+              "engine.cu"]
 CPP_SOURCES = ["plink.cpp", "synth.cpp", "tables.cpp"]
 CLI_SOURCES = ["cli.cpp"]
 HOST_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-Wall",

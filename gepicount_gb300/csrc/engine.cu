@@ -1,0 +1,700 @@
+// Scan engine: runs many scan requests -- whole plane sets or SNP range x
+// range blocks, on one or many plane sets (cohorts) of a device -- together,
+// and the serving loop built on it.
+//
+// Replaces the reference's one-cohort-per-process batch loop
+// (launch_process_gpu_1, src/kernels/kernel1.cu:387-483).  Each request walks
+// its tile list in adaptive batches exactly as a direct scan does (so its
+// results are bit-identical to gepi_scan_range's); an engine step launches
+// the next batch of every active request at once, each request on its own
+// stream, so the persistent counting kernels of different cohorts run side by
+// side on the SMs, then does the per-request bookkeeping: a device radix
+// select that raises a request's threshold (replayed from a CUDA graph
+// captured once per buffer orientation), overflow retries in halves, and the
+// final select and top-k read-back of finished requests.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "internal.h"
+
+namespace gepi {
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+bool cand_better(const Cand &a, const Cand &b) {
+    if (a.key != b.key) return a.key > b.key;
+    if (a.rA != b.rA) return a.rA < b.rA;
+    return a.rBfun < b.rBfun;
+}
+
+// Candidate-buffer capacity of a request, as for direct scans: 4 Mi records,
+// more for large k; GEPI_DEBUG_CAP shrinks it (>= 4k) so tests can drive the
+// overflow path.
+uint64_t cand_cap(int k) {
+    uint64_t want = std::max<uint64_t>(1u << 22, ((uint64_t)k * 8 + 1023) & ~1023ull);
+    if (const char *e = std::getenv("GEPI_DEBUG_CAP")) {
+        long long v = std::atoll(e);
+        if (v > 0) want = std::max<uint64_t>((uint64_t)v, 4ull * (uint64_t)k);
+    }
+    return want;
+}
+
+double ms_between(Clock::time_point a, Clock::time_point b) {
+    return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+}  // namespace
+
+struct ScanRequest {
+    gepi_planes *pl = nullptr;
+    int a0 = 0, na = 0, b0 = 0, nb = 0;
+    int k = 0, objective = 0, method = 0;
+};
+
+// Device resources of one request, pooled by candidate capacity.
+struct JobBuffers {
+    Cand *cand[2] = {nullptr, nullptr};
+    uint32_t cap = 0;
+    ScanState *state = nullptr;
+    ScanState *h_state = nullptr;  // pinned
+    int2 *tiles = nullptr;
+    size_t tiles_cap = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // start, done, launch start/end
+    cudaGraphExec_t sel_graph[2] = {nullptr, nullptr};  // select+compact cand[c] -> cand[c^1]
+    int sel_k = -1, sel_obj = -1;
+    float sel_margin = 0.f;
+};
+
+struct Job {
+    ScanRequest rq;
+    gepi_result *tops = nullptr;
+    std::vector<gepi_result> own_tops;  // serving: kept until gepi_server_wait
+    uint64_t ticket = 0;
+    size_t footprint = 0;
+    bool finished = false;  // serving: results ready for the waiter
+    bool tc = false;
+    int TA = 0, TB = 0;
+    size_t ntiles = 0, next = 0, batch = 1, inflight = 0;
+    JobBuffers *buf = nullptr;
+    int cur = 0;
+    uint32_t count = 0, budget = 0;
+    int retries = 0;
+    float lp_margin = 0.f;
+    bool started = false, done = false, launched = false;
+    gepi_status status = GEPI_OK;
+    std::string error;
+    gepi_scan_stats S{};
+    Clock::time_point t_submit, t_admit, t_done;
+};
+
+class Engine {
+   public:
+    explicit Engine(int device) : device_(device) {}
+    ~Engine();
+    gepi_status init();
+    gepi_status admit(Job &j);
+    gepi_status step(std::vector<Job *> &active);
+    void release(Job &j);
+    std::mutex run_mu;  // serialises gepi_scan_batch calls on the device
+
+   private:
+    gepi_status launch(Job &j);
+    gepi_status settle(Job &j);
+    gepi_status select(Job &j, int n_override, uint32_t n_compact);
+    gepi_status finish(Job &j);
+
+    int device_ = 0, num_sms_ = 0;
+    void *d_sel_ = nullptr;  // select scratch: used by one request at a time (host-serialised)
+    std::vector<std::unique_ptr<JobBuffers>> pool_;
+    std::vector<JobBuffers *> free_;
+};
+
+Engine::~Engine() {
+    DeviceGuard g(device_);
+    for (auto &b : pool_) {
+        if (b->stream) cudaStreamSynchronize(b->stream);
+        dfree(b->cand[0]);
+        dfree(b->cand[1]);
+        dfree(b->state);
+        dfree(b->tiles);
+        if (b->h_state) cudaFreeHost(b->h_state);
+        for (cudaEvent_t e : b->ev)
+            if (e) cudaEventDestroy(e);
+        for (cudaGraphExec_t x : b->sel_graph)
+            if (x) cudaGraphExecDestroy(x);
+        if (b->stream) cudaStreamDestroy(b->stream);
+    }
+    dfree(d_sel_);
+}
+
+gepi_status Engine::init() {
+    DeviceGuard g(device_);
+    if (!g.ok) return set_error(GEPI_ERR_CUDA, "cudaSetDevice failed");
+    GEPI_CUDA(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, device_));
+    GEPI_CUDA(cudaMalloc(&d_sel_, sel_state_bytes()));
+    return GEPI_OK;
+}
+
+gepi_status Engine::admit(Job &j) {
+    DeviceGuard g(device_);
+    const ScanRequest &rq = j.rq;
+    gepi_planes *pl = rq.pl;
+    GEPI_TRY(pl_ensure_tables(pl));
+    int method = 0;
+    GEPI_TRY(pl_resolve_method(pl, rq.method, &method));
+    j.tc = method == GEPI_METHOD_TENSOR;
+    if (j.tc) GEPI_TRY(pl_ensure_tc_blocks(pl));
+    GEPI_CUDA(cudaStreamSynchronize(pl->stream));  // decode, relayout, tables done
+    j.TA = j.tc ? tc_tile_a_snps() : popc_tile_snps();
+    j.TB = j.tc ? tc_tile_b_snps() : popc_tile_snps();
+    std::vector<int2> tiles;
+    pl_build_tiles(rq.a0, rq.a0 + rq.na, rq.b0, rq.b0 + rq.nb, j.TA, j.TB, true, 8, tiles);
+    j.ntiles = tiles.size();
+
+    const uint64_t cap = cand_cap(rq.k);
+    if (cap > (1ull << 31)) return set_error(GEPI_ERR_LIMIT, "topmost too large");
+    JobBuffers *b = nullptr;
+    for (size_t i = 0; i < free_.size(); ++i)
+        if (free_[i]->cap == cap) {
+            b = free_[i];
+            free_.erase(free_.begin() + i);
+            break;
+        }
+    if (!b) {
+        GEPI_TRY(pl_check_mem(2 * cap * sizeof(Cand), "candidate buffers"));
+        auto nb = std::make_unique<JobBuffers>();
+        GEPI_CUDA(cudaMalloc(&nb->cand[0], cap * sizeof(Cand)));
+        GEPI_CUDA(cudaMalloc(&nb->cand[1], cap * sizeof(Cand)));
+        GEPI_CUDA(cudaMalloc(&nb->state, sizeof(ScanState)));
+        GEPI_CUDA(cudaMallocHost(&nb->h_state, sizeof(ScanState)));
+        GEPI_CUDA(cudaStreamCreateWithFlags(&nb->stream, cudaStreamNonBlocking));
+        for (cudaEvent_t &e : nb->ev) GEPI_CUDA(cudaEventCreate(&e));
+        nb->cap = (uint32_t)cap;
+        b = nb.get();
+        pool_.push_back(std::move(nb));
+    }
+    j.buf = b;
+    if (tiles.size() > b->tiles_cap) {
+        dfree(b->tiles);
+        GEPI_CUDA(cudaMalloc(&b->tiles, std::max<size_t>(1, tiles.size()) * sizeof(int2)));
+        b->tiles_cap = tiles.size();
+    }
+    if (!tiles.empty())
+        GEPI_CUDA(cudaMemcpyAsync(b->tiles, tiles.data(), tiles.size() * sizeof(int2),
+                                  cudaMemcpyHostToDevice, b->stream));
+    ScanState init{};
+    init.tau_key = 0ull;
+    init.theta = 0.f;
+    init.lp_thr = INFINITY;
+    init.tau_f = -INFINITY;
+    init.tau_val = -INFINITY;
+    *b->h_state = init;
+    GEPI_CUDA(cudaMemcpyAsync(b->state, b->h_state, sizeof(ScanState), cudaMemcpyHostToDevice,
+                              b->stream));
+    GEPI_CUDA(cudaStreamSynchronize(b->stream));  // tiles and state in place before reuse of h_state
+
+    j.cur = 0;
+    j.S = gepi_scan_stats{};
+    j.S.method = method;
+    j.S.tile_snps = j.TA;
+    j.S.tiles = j.ntiles;
+    {
+        // pairs (s, t), t < s, s in A, t in B; and SNPs in both ranges
+        const int64_t ia0 = rq.a0, ia1 = (int64_t)rq.a0 + rq.na, ib0 = rq.b0,
+                      ib1 = (int64_t)rq.b0 + rq.nb;
+        uint64_t pairs = 0;
+        for (int64_t s = ia0; s < ia1; ++s) {
+            const int64_t hi = std::min<int64_t>(s, ib1);
+            if (hi > ib0) pairs += (uint64_t)(hi - ib0);
+        }
+        j.S.snp_pairs = pairs;
+        const int64_t lo = std::max(ia0, ib0), hi = std::min(ia1, ib1);
+        j.S.diag_snps = hi > lo ? (uint64_t)(hi - lo) : 0;
+    }
+    // as in the direct scan: a first batch of about cap/4 tests (Fisher: 64 Ki)
+    const double tests_per_tile = 20.0 * j.TA * j.TB;
+    const double pilot = rq.objective == GEPI_ENTROPY ? b->cap / 4.0 : 1.0 * (1 << 16);
+    j.batch = (size_t)std::max(1.0, std::floor(pilot / tests_per_tile));
+    j.budget = b->cap / 2;
+    j.lp_margin = 2e-6f * pl->lf_max + 1e-3f;
+    j.next = 0;
+    j.count = 0;
+    j.retries = 0;
+    j.started = j.done = j.launched = false;
+    j.t_admit = Clock::now();
+    return GEPI_OK;
+}
+
+void Engine::release(Job &j) {
+    if (j.buf) free_.push_back(j.buf);
+    j.buf = nullptr;
+}
+
+// Queues the next batch of `j` on its stream: counting launch, state read-back.
+gepi_status Engine::launch(Job &j) {
+    JobBuffers *b = j.buf;
+    gepi_planes *pl = j.rq.pl;
+    const ScanRequest &r = j.rq;
+    j.inflight = std::min(j.batch, j.ntiles - j.next);
+    ScanCtx ctx;
+    ctx.T = pl->d_T;
+    ctx.F = pl->F;
+    ctx.lf = pl->d_lf;
+    ctx.lf32 = pl->d_lf32;
+    ctx.objective = r.objective;
+    ctx.cap = b->cap;
+    ctx.st = b->state;
+    ctx.cand = b->cand[j.cur];
+    if (!j.started) {
+        GEPI_CUDA(cudaEventRecord(b->ev[0], b->stream));
+        j.started = true;
+    }
+    GEPI_CUDA(cudaEventRecord(b->ev[2], b->stream));
+    if (j.tc)
+        GEPI_CUDA(launch_tc_tiles(pl->d_tc_blocks, pl->n_snps, pl->Wp, pl->W0, b->tiles + j.next,
+                                  (int)j.inflight, r.a0, r.a0 + r.na, r.b0, r.b0 + r.nb, ctx,
+                                  nullptr, &b->state->kerr, num_sms_, b->stream));
+    else
+        GEPI_CUDA(launch_popc_tiles(pl->d_planes, pl->Wp, pl->W0, b->tiles + j.next,
+                                    (int)j.inflight, r.a0, r.a0 + r.na, r.b0, r.b0 + r.nb, ctx,
+                                    nullptr, b->stream));
+    GEPI_CUDA(cudaEventRecord(b->ev[3], b->stream));
+    GEPI_CUDA(cudaMemcpyAsync(b->h_state, b->state, sizeof(ScanState), cudaMemcpyDeviceToHost,
+                              b->stream));
+    j.launched = true;
+    return GEPI_OK;
+}
+
+// Device radix select of the k-th best key, then compaction into the other
+// buffer.  The common form (all entries) replays a captured CUDA graph.
+gepi_status Engine::select(Job &j, int n_override, uint32_t n_compact) {
+    JobBuffers *b = j.buf;
+    const int k = j.rq.k, obj = j.rq.objective;
+    Cand *in = b->cand[j.cur], *out = b->cand[j.cur ^ 1];
+    j.S.other_launches += kSelectLaunches;
+    bool done = false;
+    if (n_override < 0 && n_compact == 0xFFFFFFFFu) {
+        if (b->sel_k != k || b->sel_obj != obj || b->sel_margin != j.lp_margin) {
+            for (cudaGraphExec_t &x : b->sel_graph)
+                if (x) {
+                    cudaGraphExecDestroy(x);
+                    x = nullptr;
+                }
+            b->sel_k = k;
+            b->sel_obj = obj;
+            b->sel_margin = j.lp_margin;
+        }
+        cudaGraphExec_t &x = b->sel_graph[j.cur];
+        if (!x) {
+            cudaGraph_t graph = nullptr;
+            if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+                cudaError_t e = run_select_compact(in, out, b->state, d_sel_, b->cap, (uint32_t)k,
+                                                   -1, 0xFFFFFFFFu, obj, j.lp_margin, num_sms_,
+                                                   b->stream);
+                cudaError_t e2 = cudaStreamEndCapture(b->stream, &graph);
+                if (e == cudaSuccess && e2 == cudaSuccess && graph &&
+                    cudaGraphInstantiate(&x, graph, 0) != cudaSuccess)
+                    x = nullptr;
+                if (graph) cudaGraphDestroy(graph);
+                cudaGetLastError();  // a failed capture leaves the plain launches below
+            }
+        }
+        if (x) {
+            GEPI_CUDA(cudaGraphLaunch(x, b->stream));
+            done = true;
+        }
+    }
+    if (!done)
+        GEPI_CUDA(run_select_compact(in, out, b->state, d_sel_, b->cap, (uint32_t)k, n_override,
+                                     n_compact, obj, j.lp_margin, num_sms_, b->stream));
+    j.cur ^= 1;
+    GEPI_CUDA(cudaMemcpyAsync(b->h_state, b->state, sizeof(ScanState), cudaMemcpyDeviceToHost,
+                              b->stream));
+    GEPI_CUDA(cudaStreamSynchronize(b->stream));
+    j.count = b->h_state->count;
+    return GEPI_OK;
+}
+
+gepi_status Engine::finish(Job &j) {
+    JobBuffers *b = j.buf;
+    if (j.count > (uint32_t)j.rq.k) GEPI_TRY(select(j, -1, 0xFFFFFFFFu));
+    const uint32_t count = j.count;
+    std::vector<Cand> host(count);
+    if (count)
+        GEPI_CUDA(cudaMemcpyAsync(host.data(), b->cand[j.cur], (size_t)count * sizeof(Cand),
+                                  cudaMemcpyDeviceToHost, b->stream));
+    GEPI_CUDA(cudaEventRecord(b->ev[1], b->stream));
+    GEPI_CUDA(cudaStreamSynchronize(b->stream));
+    float ms = 0.f;
+    if (j.started) GEPI_CUDA(cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]));
+    j.S.scan_ms = ms;
+    j.S.candidates = count;
+    const int k = j.rq.k;
+    std::memset(j.tops, 0, sizeof(gepi_result) * (size_t)k);
+    const size_t keep = std::min<size_t>(host.size(), (size_t)k);
+    std::partial_sort(host.begin(), host.begin() + keep, host.end(), cand_better);
+    for (size_t i = 0; i < keep; ++i) {
+        const Cand &c = host[i];
+        gepi_result &r = j.tops[i];
+        r.sA = c.rA;
+        r.sB = c.rBfun >> 3;
+        r.fun = (char)(c.rBfun & 7);
+        for (int q = 0; q < 4; ++q) r.n[q] = c.n[q];
+        r.ent = (float)(-value_of_key(c.key));
+    }
+    j.done = true;
+    j.t_done = Clock::now();
+    return GEPI_OK;
+}
+
+// Bookkeeping of one request after its batch's state arrived (stream synced).
+gepi_status Engine::settle(Job &j) {
+    JobBuffers *b = j.buf;
+    j.launched = false;
+    const ScanState st = *b->h_state;
+    float ms = 0.f;
+    GEPI_CUDA(cudaEventElapsedTime(&ms, b->ev[2], b->ev[3]));
+    j.S.count_ms += ms;
+    j.S.max_count_ms = std::max<double>(j.S.max_count_ms, ms);
+    j.S.count_launches += 1;
+    if (st.kerr)
+        return set_error(GEPI_ERR_TIMEOUT, "counting kernel gave up a bounded wait (code " +
+                                               std::to_string(st.kerr) + ")");
+    const size_t nbt = j.inflight;
+    if (st.overflow) {
+        // Tighten with everything captured (a valid lower bound), drop this
+        // batch's partial appends, retry it in halves.  Only more than `cap`
+        // exactly tied candidates can keep overflowing a 1-tile batch.
+        if (++j.retries > 64)
+            return set_error(GEPI_ERR_LIMIT, "candidate buffer keeps overflowing (massive ties)");
+        j.S.overflows += 1;
+        GEPI_TRY(select(j, (int)b->cap, j.count));
+        j.batch = std::max<size_t>(1, nbt / 2);
+        return GEPI_OK;
+    }
+    const uint32_t appended = st.count - j.count;
+    j.count = st.count;
+    j.next += nbt;
+    j.retries = 0;
+    j.S.batches += 1;
+    if (j.next >= j.ntiles) return finish(j);
+    if (j.count > j.budget) GEPI_TRY(select(j, -1, 0xFFFFFFFFu));
+    // Next batch: as many tiles as the remaining budget allows at the append
+    // rate just observed, growing at most 8x per step.
+    const double rate = std::max(1.0, (double)appended) / (double)nbt;
+    const double room = (double)j.budget - (double)j.count;
+    double nb_next = room > 0 ? room / rate : 1.0;
+    nb_next = std::min(nb_next, 8.0 * (double)nbt);
+    j.batch = (size_t)std::max(1.0, nb_next);
+    return GEPI_OK;
+}
+
+// One engine step: the next batch of every active request is queued on the
+// request's stream (so they run concurrently), then each is settled.  A
+// request that fails gets its status; the others carry on.
+gepi_status Engine::step(std::vector<Job *> &active) {
+    DeviceGuard g(device_);
+    std::vector<Job *> run;
+    for (Job *j : active) {
+        if (j->done || j->status != GEPI_OK) continue;
+        if (j->next >= j->ntiles) {  // empty range
+            j->status = finish(*j);
+            if (j->status != GEPI_OK) {
+                j->error = gepi_last_error();
+                j->done = true;
+            }
+            continue;
+        }
+        gepi_status st = launch(*j);
+        if (st != GEPI_OK) {
+            j->status = st;
+            j->error = gepi_last_error();
+            j->done = true;
+            continue;
+        }
+        run.push_back(j);
+    }
+    for (Job *j : run) {
+        gepi_status st = GEPI_OK;
+        if (cudaStreamSynchronize(j->buf->stream) != cudaSuccess)
+            st = set_error(GEPI_ERR_CUDA, std::string("counting launch: ") +
+                                              cudaGetErrorString(cudaGetLastError()));
+        else
+            st = settle(*j);
+        if (st != GEPI_OK) {
+            j->status = st;
+            j->error = gepi_last_error();
+            j->done = true;
+        }
+    }
+    return GEPI_OK;
+}
+
+// ---- the plane-set engine used by gepi_scan_batch ---------------------------
+
+namespace {
+
+std::mutex g_engines_mu;
+std::map<int, std::unique_ptr<Engine>> g_engines;  // one per device, kept until exit
+
+gepi_status device_engine(int device, Engine **out) {
+    std::lock_guard<std::mutex> lk(g_engines_mu);
+    auto it = g_engines.find(device);
+    if (it == g_engines.end()) {
+        auto e = std::make_unique<Engine>(device);
+        GEPI_TRY(e->init());
+        it = g_engines.emplace(device, std::move(e)).first;
+    }
+    *out = it->second.get();
+    return GEPI_OK;
+}
+
+gepi_status check_request(const gepi_scan_req &r, ScanRequest *out) {
+    if (!r.planes) return set_error(GEPI_ERR_ARG, "scan request: null planes");
+    if (r.topmost <= 0) return set_error(GEPI_ERR_ARG, "scan request: topmost must be > 0");
+    if (r.objective != GEPI_ENTROPY && r.objective != GEPI_FISHER)
+        return set_error(GEPI_ERR_ARG, "scan request: unknown objective");
+    if (r.method < GEPI_METHOD_AUTO || r.method > GEPI_METHOD_TENSOR)
+        return set_error(GEPI_ERR_ARG, "scan request: unknown method");
+    const int n = r.planes->n_snps;
+    ScanRequest q;
+    q.pl = r.planes;
+    if (r.na < 0 || r.nb < 0) {
+        q.a0 = 0;
+        q.na = n;
+        q.b0 = 0;
+        q.nb = n;
+    } else {
+        if (r.a0 < 0 || r.b0 < 0 || r.a0 + r.na > n || r.b0 + r.nb > n)
+            return set_error(GEPI_ERR_ARG, "scan request: SNP range outside the planes");
+        q.a0 = r.a0;
+        q.na = r.na;
+        q.b0 = r.b0;
+        q.nb = r.nb;
+    }
+    q.k = r.topmost;
+    q.objective = r.objective;
+    q.method = r.method;
+    *out = q;
+    return GEPI_OK;
+}
+
+// Device memory a request holds while admitted: two candidate buffers.
+size_t request_footprint(int k) { return 2 * cand_cap(k) * sizeof(Cand) + sizeof(ScanState); }
+
+}  // namespace
+
+}  // namespace gepi
+
+using namespace gepi;
+
+extern "C" {
+
+gepi_status gepi_scan_batch(const gepi_scan_req *reqs, int32_t n, gepi_result *const *tops,
+                            gepi_scan_stats *stats) {
+    clear_error();
+    if (!reqs || !tops || n <= 0) return set_error(GEPI_ERR_ARG, "gepi_scan_batch: bad argument");
+    std::vector<Job> jobs((size_t)n);
+    for (int i = 0; i < n; ++i) {
+        GEPI_TRY(check_request(reqs[i], &jobs[i].rq));
+        if (!tops[i]) return set_error(GEPI_ERR_ARG, "gepi_scan_batch: null result array");
+        if (reqs[i].planes->device != reqs[0].planes->device)
+            return set_error(GEPI_ERR_ARG, "gepi_scan_batch: requests on different devices");
+        jobs[i].tops = tops[i];
+    }
+    Engine *eng = nullptr;
+    GEPI_TRY(device_engine(reqs[0].planes->device, &eng));
+    std::lock_guard<std::mutex> run_lock(eng->run_mu);
+    std::vector<Job *> active;
+    gepi_status st = GEPI_OK;
+    for (Job &j : jobs) {
+        st = eng->admit(j);
+        active.push_back(&j);
+        if (st != GEPI_OK) break;
+    }
+    while (st == GEPI_OK) {
+        bool any = false;
+        for (Job *j : active) any |= !j->done;
+        if (!any) break;
+        st = eng->step(active);
+        for (Job *j : active)
+            if (j->status != GEPI_OK) {
+                st = set_error(j->status, j->error);
+                break;
+            }
+    }
+    for (int i = 0; i < n; ++i) {
+        if (stats) stats[i] = jobs[i].S;
+        eng->release(jobs[i]);
+    }
+    return st;
+}
+
+}  // extern "C"
+
+// The serving loop's state (C ABI handle).
+struct gepi_server {
+    int device = 0;
+    size_t budget = 0, used = 0;
+    std::unique_ptr<gepi::Engine> engine;
+    std::thread thread;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<gepi::Job *> pending;
+    std::map<uint64_t, std::unique_ptr<gepi::Job>> jobs;
+    uint64_t next_ticket = 1;
+    bool stop = false;
+
+    void run();
+};
+
+void gepi_server::run() {
+    cudaSetDevice(device);
+    std::vector<Job *> active, admitting;
+    for (;;) {
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            for (;;) {
+                // admission: FIFO while the footprint fits; the head always
+                // gets in when nothing runs, so no request starves
+                while (!pending.empty()) {
+                    Job *j = pending.front();
+                    if (!active.empty() && used + j->footprint > budget) break;
+                    pending.pop_front();
+                    used += j->footprint;
+                    admitting.push_back(j);
+                }
+                if (!active.empty() || !admitting.empty()) break;
+                if (stop) return;
+                cv_work.wait(lk);
+            }
+        }
+        for (Job *j : admitting) {
+            j->status = engine->admit(*j);
+            if (j->status != GEPI_OK) {
+                j->error = gepi_last_error();
+                j->done = true;
+            }
+            active.push_back(j);
+        }
+        admitting.clear();
+        engine->step(active);
+        std::lock_guard<std::mutex> lk(mu);
+        bool any = false;
+        for (Job *j : active)
+            if (j->done) {
+                if (j->t_done.time_since_epoch().count() == 0) j->t_done = Clock::now();
+                engine->release(*j);
+                used -= j->footprint;
+                j->finished = true;
+                any = true;
+            }
+        active.erase(std::remove_if(active.begin(), active.end(), [](Job *j) { return j->done; }),
+                     active.end());
+        if (any) cv_done.notify_all();
+    }
+}
+
+extern "C" {
+
+gepi_status gepi_server_create(int32_t device, size_t hbm_budget_bytes, gepi_server **out) {
+    clear_error();
+    if (!out) return set_error(GEPI_ERR_ARG, "gepi_server_create: null output");
+    *out = nullptr;
+    auto srv = std::make_unique<gepi_server>();
+    srv->device = device;
+    srv->budget = hbm_budget_bytes ? hbm_budget_bytes : (16ull << 30);
+    srv->engine = std::make_unique<Engine>(device);
+    GEPI_TRY(srv->engine->init());
+    gepi_server *p = srv.get();
+    p->thread = std::thread([p] { p->run(); });
+    *out = srv.release();
+    return GEPI_OK;
+}
+
+gepi_status gepi_server_submit(gepi_server *srv, const gepi_scan_req *req, uint64_t *ticket) {
+    clear_error();
+    if (!srv || !req || !ticket) return set_error(GEPI_ERR_ARG, "gepi_server_submit: bad argument");
+    ScanRequest rq;
+    GEPI_TRY(check_request(*req, &rq));
+    if (rq.pl->device != srv->device)
+        return set_error(GEPI_ERR_ARG, "gepi_server_submit: plane set on another device");
+    auto j = std::make_unique<Job>();
+    j->rq = rq;
+    j->own_tops.assign((size_t)rq.k, gepi_result{});
+    j->tops = j->own_tops.data();
+    j->footprint = request_footprint(rq.k);
+    j->t_submit = Clock::now();
+    {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        j->ticket = srv->next_ticket++;
+        *ticket = j->ticket;
+        srv->pending.push_back(j.get());
+        srv->jobs[j->ticket] = std::move(j);
+    }
+    srv->cv_work.notify_one();
+    return GEPI_OK;
+}
+
+gepi_status gepi_server_wait(gepi_server *srv, uint64_t ticket, gepi_result *tops,
+                             gepi_request_info *info) {
+    clear_error();
+    if (!srv || !tops) return set_error(GEPI_ERR_ARG, "gepi_server_wait: bad argument");
+    std::unique_ptr<Job> j;
+    {
+        std::unique_lock<std::mutex> lk(srv->mu);
+        auto it = srv->jobs.find(ticket);
+        if (it == srv->jobs.end()) return set_error(GEPI_ERR_ARG, "gepi_server_wait: unknown ticket");
+        Job *p = it->second.get();
+        srv->cv_done.wait(lk, [p] { return p->finished; });
+        j = std::move(it->second);
+        srv->jobs.erase(it);
+    }
+    if (info) {
+        std::memset(info, 0, sizeof *info);
+        info->queue_ms = ms_between(j->t_submit, j->t_admit);
+        info->latency_ms = ms_between(j->t_submit, j->t_done);
+        info->device_ms = j->S.scan_ms;
+        info->snp_pairs = j->S.snp_pairs;
+        info->method = j->S.method;
+    }
+    if (j->status != GEPI_OK) return set_error(j->status, j->error);
+    std::memcpy(tops, j->tops, sizeof(gepi_result) * (size_t)j->rq.k);
+    return GEPI_OK;
+}
+
+void gepi_server_destroy(gepi_server *srv) {
+    if (!srv) return;
+    {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        srv->stop = true;
+        for (Job *j : srv->pending) {
+            j->status = GEPI_ERR_ARG;
+            j->error = "server destroyed before the request was admitted";
+            j->finished = true;
+        }
+        srv->pending.clear();
+    }
+    srv->cv_work.notify_all();
+    if (srv->thread.joinable()) srv->thread.join();
+    srv->cv_done.notify_all();
+    delete srv;
+}
+
+}  // extern "C"

@@ -18,35 +18,10 @@
 #include <string>
 #include <vector>
 
-#include "common.h"
-#include "device.cuh"
+#include "internal.h"
 #include "tables.h"
 
 namespace gepi {
-
-cudaError_t launch_decode_bed(const uint8_t *bed_payload, size_t bps, int n_snps,
-                              const int32_t *perm, int Wp, uint32_t *planes, cudaStream_t stream);
-cudaError_t launch_decode_rows(const uint64_t *bits, const uint64_t *valid, int nw, int n_snps,
-                               const int32_t *perm, int Wp, uint32_t *planes,
-                               cudaStream_t stream, int num_sms);
-cudaError_t launch_popc_tiles(const uint32_t *planes, int Wp, int W0, const int2 *tiles,
-                              int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
-                              uint32_t *dump, cudaStream_t stream);
-cudaError_t launch_tc_tiles(const uint32_t *blk, int n_snps, int Wp, int W0, const int2 *tiles,
-                            int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
-                            uint32_t *dump, int *err, int num_sms, cudaStream_t stream);
-cudaError_t launch_tc_relayout(const uint32_t *planes, int Wp, int W0, int n_snps, uint32_t *blk,
-                               int num_sms, cudaStream_t stream);
-size_t tc_block_words(int n_snps, int Wp, int W0);
-cudaError_t tc_measure_peak(int num_sms, int reps, double *tflops, int *err, cudaStream_t stream);
-int tc_tile_a_snps();
-int tc_tile_b_snps();
-cudaError_t run_select_compact(Cand *in, Cand *out, ScanState *st, void *sel, uint32_t cap,
-                               uint32_t k, int n_override, uint32_t n_compact, int objective,
-                               float lp_margin, int num_sms, cudaStream_t stream);
-size_t sel_state_bytes();
-int popc_tile_snps();
-constexpr int kSelectLaunches = 20;  // init + 8 x (histogram, pick) + apply + compact + count
 
 static thread_local std::string g_last_error;
 
@@ -60,49 +35,7 @@ void clear_error() { g_last_error.clear(); }
 
 using namespace gepi;
 
-struct gepi_planes {
-    int device = 0, num_sms = 0;
-    int auto_method = 0;  // AUTO's choice for this plane set (0 = not tuned yet)
-    float tune_ms[2] = {0.f, 0.f};  // autotuner timings: popcount, tensor core
-    int n_snps = 0, S0 = 0, S1 = 0, W0 = 0, W1 = 0, Wp = 0;
-    uint32_t *d_planes = nullptr;
-    uint32_t *d_tc_blocks = nullptr;  // block-major copy for the tensor-core kernel (lazy)
-    cudaStream_t stream = nullptr;
-    uint64_t *d_T = nullptr;
-    int F = 0;
-    double *d_lf = nullptr;
-    float *d_lf32 = nullptr;
-    float lf_max = 0.f;
-    Cand *d_cand[2] = {nullptr, nullptr};
-    uint32_t cap = 0;
-    ScanState *d_state = nullptr;
-    ScanState *h_state = nullptr;
-    void *d_sel = nullptr;
-    int2 *d_tiles = nullptr;
-    size_t tiles_cap = 0;
-    std::vector<cudaEvent_t> ev;  // timing events, reused across scans
-    gepi_scan_stats stats{};
-};
-
 namespace {
-
-struct DeviceGuard {
-    int prev = -1;
-    bool ok = false;
-    explicit DeviceGuard(int dev) {
-        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-        ok = cudaSetDevice(dev) == cudaSuccess;
-    }
-    ~DeviceGuard() {
-        if (prev >= 0) cudaSetDevice(prev);
-    }
-};
-
-template <class T>
-void dfree(T *&p) {
-    if (p) cudaFree(p);
-    p = nullptr;
-}
 
 gepi_status check_mem(size_t bytes, const char *what) {
     size_t fr = 0, tot = 0;
@@ -540,6 +473,19 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
 }
 
 }  // namespace
+
+namespace gepi {
+
+gepi_status pl_check_mem(size_t bytes, const char *what) { return check_mem(bytes, what); }
+gepi_status pl_ensure_tables(gepi_planes *pl) { return ensure_tables(pl); }
+gepi_status pl_ensure_tc_blocks(gepi_planes *pl) { return ensure_tc_blocks(pl); }
+gepi_status pl_resolve_method(gepi_planes *pl, int m, int *out) { return resolve_method(pl, m, out); }
+void pl_build_tiles(int a0, int a1, int b0, int b1, int TA, int TB, bool triangle, int band,
+                    std::vector<int2> &out) {
+    build_tiles(a0, a1, b0, b1, TA, TB, triangle, band, out);
+}
+
+}  // namespace gepi
 
 extern "C" {
 

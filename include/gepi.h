@@ -195,6 +195,62 @@ gepi_status gepi_planes_autotune(gepi_planes *pl, int32_t *method, float *popc_m
  * reference. */
 gepi_status gepi_tensor_peak_tflops(int32_t device, double *tflops);
 
+/* ---- many scans at once: cohort batches and the serving loop ---------------- */
+/* One scan request: SNP ranges [a0, a0+na) x [b0, b0+nb) of `planes` (na < 0 or
+ * nb < 0: the whole plane set), the `topmost` best results by `objective`
+ * (GEPI_ENTROPY / GEPI_FISHER), counting `method` (GEPI_METHOD_*).  Results are
+ * those gepi_scan_range gives for the same arguments, bit for bit. */
+typedef struct gepi_scan_req {
+    gepi_planes *planes;
+    int32_t a0, na, b0, nb;
+    int32_t topmost;
+    int32_t objective;
+    int32_t method;
+    int32_t reserved;
+} gepi_scan_req;
+
+/* Runs `n` requests together on the device of their plane sets (all on one
+ * device; plane sets may differ, so a call scans many cohorts): every request
+ * walks its tile list in its own adaptive batches on its own stream, and each
+ * engine step launches the next batch of every unfinished request at once.
+ * Replaces a loop of one reference process per cohort (the batch loop of
+ * launch_process_gpu_1, src/kernels/kernel1.cu:387-483, run per cohort).
+ * tops[i] receives reqs[i].topmost results; stats (may be NULL) receives one
+ * gepi_scan_stats per request.  The first failing request's status is
+ * returned.  Calls on one device are serialised internally; a plane set must
+ * not be used by another call while it runs.  No counterpart in the reference. */
+gepi_status gepi_scan_batch(const gepi_scan_req *reqs, int32_t n, gepi_result *const *tops,
+                            gepi_scan_stats *stats);
+
+/* Serving loop: a thread that admits submitted requests first-in first-out
+ * while their device footprint (2 candidate buffers each: 256 MiB at topmost
+ * <= 512 Ki) fits `hbm_budget_bytes` (0: 16 GiB; the oldest request is always
+ * admitted when nothing runs), and runs all admitted requests together as
+ * gepi_scan_batch does, admitting new ones between engine steps.  Plane sets
+ * submitted to a server must not be used by other calls until their requests
+ * are waited for.  No counterpart in the reference (it runs one scan per
+ * process). */
+typedef struct gepi_server gepi_server;
+typedef struct gepi_request_info {
+    double queue_ms;    /* submit -> admission                          */
+    double latency_ms;  /* submit -> results ready                      */
+    double device_ms;   /* device time of the request's scan            */
+    uint64_t snp_pairs; /* SNP pairs the request tested                 */
+    int32_t method;     /* counting method used                          */
+    int32_t reserved;
+} gepi_request_info;
+gepi_status gepi_server_create(int32_t device, size_t hbm_budget_bytes, gepi_server **out);
+/* Queues a request; returns at once with its ticket. */
+gepi_status gepi_server_submit(gepi_server *srv, const gepi_scan_req *req, uint64_t *ticket);
+/* Blocks until the ticket's request is done; copies its topmost results to
+ * tops and its timings to info (may be NULL); returns the request's status.
+ * Each ticket is waited for once. */
+gepi_status gepi_server_wait(gepi_server *srv, uint64_t ticket, gepi_result *tops,
+                             gepi_request_info *info);
+/* Finishes admitted requests, fails queued ones, stops the thread.  No wait
+ * may be in progress. */
+void gepi_server_destroy(gepi_server *srv);
+
 /* ---- drop-in for the reference's process_gpu_1 ----------------------------- */
 /* Same inputs as process_gpu_1 reads from its PlinkReader (BitData, ValidData,
  * numSNPs() = n_rows, elementsSNP() = n_words, classData(1|2)->mask()), same

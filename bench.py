@@ -44,6 +44,12 @@ CONFIGS = {
     "prof40k": dict(n_snps=40000, n_cases=5000, n_controls=5000, maf_lo=0.01, maf_hi=0.5,
                     missing=0.01, n_planted=4, seed=1005, k=1000),
 }
+# Many-request workloads (run by --config cohorts64 / serving).
+COHORTS64 = dict(n_cohorts=64, snps=(500, 50000), samples=(200, 20000), case_frac=(0.3, 0.7),
+                 missing=0.01, k=1000, seed=1004)
+SERVING = dict(n_matrices=8, snps=(5000, 100000), samples=(1000, 10000), missing=0.01,
+               ranges=(1000, 50000), ks=(100, 1000, 10000), whole_frac=0.2, seed=1006,
+               loads=(0.2, 0.5, 0.8, 1.0))
 METRIC = "pair-tests/sec at 100k SNP x 10k samples"
 UNIT = "pair-tests/s"
 
@@ -360,13 +366,214 @@ def run_ours(args, cfg):
     return 0
 
 
+def _log_uniform(rng, lo, hi):
+    import math
+
+    return int(round(math.exp(rng.uniform(math.log(lo), math.log(hi)))))
+
+
+def _make_cohort(g, rng, snps, samples, case_frac, missing, seed, device):
+    n = _log_uniform(rng, *snps)
+    s = max(2, _log_uniform(rng, *samples))
+    cases = min(s - 1, max(1, int(round(s * rng.uniform(*case_frac)))))
+    spec = g.SynthSpec(n_snps=n, n_cases=cases, n_controls=s - cases, maf_lo=0.01, maf_hi=0.5,
+                       missing=missing, n_planted=0, seed=seed)
+    bed, ph, _ = g.synth_bed(spec)
+    return g.Planes.from_bed(bed, n, ph, device=device), n, s
+
+
+def run_cohorts(args):
+    """64 independent uneven cohorts, each scanned all-pairs top-1,000: one
+    gepi_scan_batch call per step against the same scans one after another."""
+    import numpy as np
+    import torch
+
+    import gepicount_gb300 as g
+
+    c = COHORTS64
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    rng = np.random.default_rng(c["seed"] + 7919 * rank)
+    cohorts = [_make_cohort(g, rng, c["snps"], c["samples"], c["case_frac"], c["missing"],
+                            c["seed"] * 100 + i + 7919 * rank, local)
+               for i in range(c["n_cohorts"])]
+    reqs = [g.ScanRequest(pl, c["k"]) for pl, _, _ in cohorts]
+    tunes = [pl.autotune() for pl, _, _ in cohorts]
+    for _ in range(args.warmup):
+        g.scan_batch(reqs)
+    torch.cuda.synchronize()
+    times, stats = [], None
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            outs, stats = g.scan_batch(reqs, with_stats=True)
+            times.append(time.perf_counter() - t0)
+    pairs = sum(s_["snp_pairs"] for s_ in stats)
+    # the same scans one at a time (direct gepi_scan per cohort)
+    seq = []
+    for _ in range(max(1, min(args.steps, 2))):
+        t0 = time.perf_counter()
+        for pl, _, _ in cohorts:
+            pl.scan(c["k"])
+        seq.append(time.perf_counter() - t0)
+    same = all(o.tobytes() == pl.scan(c["k"]).tobytes() for o, (pl, _, _) in zip(outs, cohorts))
+    t_b, t_s = statistics.median(times), statistics.median(seq)
+    nsamp = [s for _, _, s in cohorts]
+    nsnp = [n for _, n, _ in cohorts]
+    line = {
+        "metric": "pair-tests/sec, 64 uneven cohorts batched (one gepi_scan_batch per step)",
+        "value": world * pairs / t_b, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_b, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "mixed (autotuned per cohort)",
+        "data": "synthetic (seeded generator, HWE)",
+        "config": {"workload": (f"{c['n_cohorts']} cohorts, SNPs log-U{c['snps']}, samples "
+                                f"log-U{c['samples']}, case fraction U{c['case_frac']}, "
+                                f"{c['missing']:.0%} missing, top-{c['k']:,} each"),
+                   "snps_total": sum(nsnp), "snps_max": max(nsnp), "samples_max": max(nsamp),
+                   "pair_tests_per_step": pairs,
+                   "methods": {"popc": sum(t["method"] == 1 for t in tunes),
+                               "tensor": sum(t["method"] == 2 for t in tunes)}},
+        "clocks": clk.summary(),
+        "sequential": {"value": world * pairs / t_s, "ms_per_step": 1e3 * t_s,
+                       "what": "the same 64 scans as direct gepi_scan calls in turn"},
+        "vs_sequential": t_s / t_b,
+        "same_results_as_sequential": same,
+        "gpu_launches": sum(s_["count_launches"] + s_["other_launches"] for s_ in stats),
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    for pl, _, _ in cohorts:
+        pl.close()
+    return 0
+
+
+def run_serving(args):
+    """Poisson stream of scan requests against 8 resident genotype matrices,
+    through the serving loop: per-request latency alone, then p50/p99 latency
+    and pair-tests/s at offered loads relative to the loop's peak rate."""
+    import numpy as np
+    import torch
+
+    import gepicount_gb300 as g
+
+    c = SERVING
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    rng = np.random.default_rng(c["seed"] + 7919 * rank)
+    mats = [_make_cohort(g, rng, c["snps"], c["samples"], (0.5, 0.5), c["missing"],
+                         c["seed"] * 100 + i + 7919 * rank, local)
+            for i in range(c["n_matrices"])]
+    for pl, _, _ in mats:
+        pl.autotune()
+
+    def make_requests(n):
+        out = []
+        for _ in range(n):
+            pl, N, _ = mats[int(rng.integers(len(mats)))]
+            k = int(c["ks"][int(rng.integers(len(c["ks"])))])
+            if rng.random() < c["whole_frac"]:
+                out.append(g.ScanRequest(pl, k))
+            else:
+                la = min(N, _log_uniform(rng, *c["ranges"]))
+                lb = min(N, _log_uniform(rng, *c["ranges"]))
+                a0 = int(rng.integers(0, N - la + 1))
+                b0 = int(rng.integers(0, N - lb + 1))
+                out.append(g.ScanRequest(pl, k, a0=a0, na=la, b0=b0, nb=lb))
+        return out
+
+    nreq = max(20, args.requests)
+    reqs = make_requests(nreq)
+
+    def pct(v, q):
+        v = sorted(v)
+        return v[min(len(v) - 1, max(0, int(round(q * (len(v) - 1)))))]
+
+    with g.Server(local) as srv:
+        for r in reqs[: min(len(reqs), 3 + args.warmup)]:  # warm-up
+            srv.wait(srv.submit(r))
+        # alone: one request in the loop at a time
+        alone, pairs = [], []
+        for r in reqs:
+            _, info = srv.wait(srv.submit(r))
+            alone.append(info["latency_ms"])
+            pairs.append(info["snp_pairs"])
+        # peak rate: the whole list submitted at once
+        t0 = time.perf_counter()
+        tickets = [srv.submit(r) for r in reqs]
+        for t in tickets:
+            srv.wait(t)
+        burst_s = time.perf_counter() - t0
+        peak_rps = nreq / burst_s
+        levels = []
+        with ClockSampler(local) as clk:
+            for load in c["loads"]:
+                rate = load * peak_rps
+                gaps = rng.exponential(1.0 / rate, size=nreq)
+                infos = [None] * nreq
+                tick = [None] * nreq
+                ready = threading.Semaphore(0)
+
+                def waiter():
+                    for i in range(nreq):
+                        ready.acquire()
+                        infos[i] = srv.wait(tick[i])[1]
+
+                th = threading.Thread(target=waiter)
+                th.start()
+                t0 = time.perf_counter()
+                due = t0
+                for i, r in enumerate(reqs):
+                    due += gaps[i]
+                    d = due - time.perf_counter()
+                    if d > 0:
+                        time.sleep(d)
+                    tick[i] = srv.submit(r)
+                    ready.release()
+                th.join()
+                span = time.perf_counter() - t0
+                lat = [x["latency_ms"] for x in infos]
+                slow = [x["latency_ms"] / max(a, 1e-3) for x, a in zip(infos, alone)]
+                levels.append({
+                    "offered_load": load, "offered_rps": rate, "p50_ms": pct(lat, 0.5),
+                    "p99_ms": pct(lat, 0.99), "pair_tests_per_s": sum(pairs) / span,
+                    "p99_over_alone_p99": pct(lat, 0.99) / pct(alone, 0.99),
+                    "slowdown_p50": pct(slow, 0.5), "slowdown_p99": pct(slow, 0.99),
+                    "queue_p99_ms": pct([x["queue_ms"] for x in infos], 0.99)})
+    at80 = min(levels, key=lambda L: abs(L["offered_load"] - 0.8))
+    line = {
+        "metric": "p50/p99 request latency, served mixed stream at 80% of peak offered load",
+        "value": at80["p99_ms"], "unit": "ms (p99)", "n_gpus": world, "steps": nreq,
+        "warmup": args.warmup, "ms_per_step": at80["p50_ms"], "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "mixed (autotuned per matrix)",
+        "data": "synthetic (seeded generator, HWE)",
+        "config": {"workload": (f"{c['n_matrices']} resident matrices (SNPs log-U{c['snps']}, "
+                                f"samples log-U{c['samples']}); {nreq} requests, "
+                                f"{c['whole_frac']:.0%} whole-genome, others range x range with "
+                                f"lengths log-U{c['ranges']}; top-k in {c['ks']}; Poisson "
+                                "arrivals"),
+                   "matrices": [[n, s] for _, n, s in mats]},
+        "clocks": clk.summary(),
+        "alone": {"p50_ms": pct(alone, 0.5), "p99_ms": pct(alone, 0.99)},
+        "peak": {"requests_per_s": peak_rps, "pair_tests_per_s": sum(pairs) / burst_s},
+        "levels": levels,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    for pl, _, _ in mats:
+        pl.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--config", choices=sorted(CONFIGS), default="cfg3")
+    ap.add_argument("--config", choices=sorted(CONFIGS) + ["cohorts64", "serving"],
+                    default="cfg3")
+    ap.add_argument("--requests", type=int, default=200,
+                    help="requests per offered-load level (--config serving)")
     ap.add_argument("--method", choices=["auto", "popc", "tensor"], default="auto")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-seconds", type=float, default=10.0)
@@ -375,6 +582,12 @@ def main():
                     help="timed scans of the plain popcount kernel for vs_plain (0 = skip)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    if args.config in ("cohorts64", "serving"):
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference scans one "
+                              "cohort per process and has no request loop"}), flush=True)
+            return 0
+        return run_cohorts(args) if args.config == "cohorts64" else run_serving(args)
     cfg = CONFIGS[args.config]
     if args.impl == "reference":
         return run_reference(args, cfg)

@@ -4,14 +4,15 @@
 //
 // Replaces the reference's one-cohort-per-process batch loop
 // (launch_process_gpu_1, src/kernels/kernel1.cu:387-483).  Each request walks
-// its tile list in adaptive batches exactly as a direct scan does (so its
-// results are bit-identical to gepi_scan_range's); an engine step launches
-// the next batch of every active request at once, each request on its own
-// stream, so the persistent counting kernels of different cohorts run side by
-// side on the SMs, then does the per-request bookkeeping: a device radix
-// select that raises a request's threshold (replayed from a CUDA graph
-// captured once per buffer orientation), overflow retries in halves, and the
-// final select and top-k read-back of finished requests.
+// its tile list in adaptive batches as a direct scan does, with the same
+// exact thresholds, so its results are bit-identical to gepi_scan_range's.
+// Requests progress independently: the engine polls each request's
+// completion event, settles a finished batch (threshold raise by a device
+// radix select replayed from a CUDA graph, overflow retry in halves, final
+// select and top-k read-back) and launches its next batch at once, so the
+// counting kernels of different requests share the SMs.  Batches can be
+// capped to a device-time quantum, and requests with little work left run on
+// a high-priority stream, so short requests are not held behind long ones.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -58,6 +59,10 @@ double ms_between(Clock::time_point a, Clock::time_point b) {
     return std::chrono::duration<double, std::milli>(b - a).count();
 }
 
+// Requests whose remaining device work is estimated below this run on the
+// high-priority stream.
+constexpr double kShortMs = 50.0;
+
 }  // namespace
 
 struct ScanRequest {
@@ -74,8 +79,9 @@ struct JobBuffers {
     ScanState *h_state = nullptr;  // pinned
     int2 *tiles = nullptr;
     size_t tiles_cap = 0;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // start, done, launch start/end
+    cudaStream_t stream[2] = {nullptr, nullptr};  // normal, high priority
+    // scan start, scan done, batch launch start / end, batch state read back
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     cudaGraphExec_t sel_graph[2] = {nullptr, nullptr};  // select+compact cand[c] -> cand[c^1]
     int sel_k = -1, sel_obj = -1;
     float sel_margin = 0.f;
@@ -91,7 +97,9 @@ struct Job {
     bool tc = false;
     int TA = 0, TB = 0;
     size_t ntiles = 0, next = 0, batch = 1, inflight = 0;
+    double ms_per_tile = 0.0;  // from the last batch (0: not measured yet)
     JobBuffers *buf = nullptr;
+    cudaStream_t s = nullptr;  // stream of the job's work in flight
     int cur = 0;
     uint32_t count = 0, budget = 0;
     int retries = 0;
@@ -105,11 +113,14 @@ struct Job {
 
 class Engine {
    public:
-    explicit Engine(int device) : device_(device) {}
+    // quantum_ms > 0 caps each batch at about that much device time.
+    Engine(int device, double quantum_ms) : device_(device), quantum_ms_(quantum_ms) {}
     ~Engine();
     gepi_status init();
     gepi_status admit(Job &j);
-    gepi_status step(std::vector<Job *> &active);
+    // Launches the next batch of every idle request and settles those whose
+    // batch has completed; returns how many were settled or finished.
+    int poll(std::vector<Job *> &active);
     void release(Job &j);
     std::mutex run_mu;  // serialises gepi_scan_batch calls on the device
 
@@ -118,9 +129,12 @@ class Engine {
     gepi_status settle(Job &j);
     gepi_status select(Job &j, int n_override, uint32_t n_compact);
     gepi_status finish(Job &j);
+    void fail(Job &j, gepi_status st);
 
     int device_ = 0, num_sms_ = 0;
-    void *d_sel_ = nullptr;  // select scratch: used by one request at a time (host-serialised)
+    double quantum_ms_ = 0.0;
+    int prio_lo_ = 0, prio_hi_ = 0;
+    void *d_sel_ = nullptr;  // select scratch: one select in flight at a time (host-serialised)
     std::vector<std::unique_ptr<JobBuffers>> pool_;
     std::vector<JobBuffers *> free_;
 };
@@ -128,7 +142,8 @@ class Engine {
 Engine::~Engine() {
     DeviceGuard g(device_);
     for (auto &b : pool_) {
-        if (b->stream) cudaStreamSynchronize(b->stream);
+        for (cudaStream_t s : b->stream)
+            if (s) cudaStreamSynchronize(s);
         dfree(b->cand[0]);
         dfree(b->cand[1]);
         dfree(b->state);
@@ -138,7 +153,8 @@ Engine::~Engine() {
             if (e) cudaEventDestroy(e);
         for (cudaGraphExec_t x : b->sel_graph)
             if (x) cudaGraphExecDestroy(x);
-        if (b->stream) cudaStreamDestroy(b->stream);
+        for (cudaStream_t s : b->stream)
+            if (s) cudaStreamDestroy(s);
     }
     dfree(d_sel_);
 }
@@ -147,6 +163,7 @@ gepi_status Engine::init() {
     DeviceGuard g(device_);
     if (!g.ok) return set_error(GEPI_ERR_CUDA, "cudaSetDevice failed");
     GEPI_CUDA(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, device_));
+    GEPI_CUDA(cudaDeviceGetStreamPriorityRange(&prio_lo_, &prio_hi_));
     GEPI_CUDA(cudaMalloc(&d_sel_, sel_state_bytes()));
     return GEPI_OK;
 }
@@ -179,17 +196,20 @@ gepi_status Engine::admit(Job &j) {
     if (!b) {
         GEPI_TRY(pl_check_mem(2 * cap * sizeof(Cand), "candidate buffers"));
         auto nb = std::make_unique<JobBuffers>();
-        GEPI_CUDA(cudaMalloc(&nb->cand[0], cap * sizeof(Cand)));
-        GEPI_CUDA(cudaMalloc(&nb->cand[1], cap * sizeof(Cand)));
-        GEPI_CUDA(cudaMalloc(&nb->state, sizeof(ScanState)));
-        GEPI_CUDA(cudaMallocHost(&nb->h_state, sizeof(ScanState)));
-        GEPI_CUDA(cudaStreamCreateWithFlags(&nb->stream, cudaStreamNonBlocking));
-        for (cudaEvent_t &e : nb->ev) GEPI_CUDA(cudaEventCreate(&e));
         nb->cap = (uint32_t)cap;
+        // owned by the pool from here on, so the destructor frees a partial set
         b = nb.get();
         pool_.push_back(std::move(nb));
+        GEPI_CUDA(cudaMalloc(&b->cand[0], cap * sizeof(Cand)));
+        GEPI_CUDA(cudaMalloc(&b->cand[1], cap * sizeof(Cand)));
+        GEPI_CUDA(cudaMalloc(&b->state, sizeof(ScanState)));
+        GEPI_CUDA(cudaMallocHost(&b->h_state, sizeof(ScanState)));
+        GEPI_CUDA(cudaStreamCreateWithPriority(&b->stream[0], cudaStreamNonBlocking, prio_lo_));
+        GEPI_CUDA(cudaStreamCreateWithPriority(&b->stream[1], cudaStreamNonBlocking, prio_hi_));
+        for (cudaEvent_t &e : b->ev) GEPI_CUDA(cudaEventCreate(&e));
     }
     j.buf = b;
+    j.s = b->stream[0];
     if (tiles.size() > b->tiles_cap) {
         dfree(b->tiles);
         GEPI_CUDA(cudaMalloc(&b->tiles, std::max<size_t>(1, tiles.size()) * sizeof(int2)));
@@ -197,7 +217,7 @@ gepi_status Engine::admit(Job &j) {
     }
     if (!tiles.empty())
         GEPI_CUDA(cudaMemcpyAsync(b->tiles, tiles.data(), tiles.size() * sizeof(int2),
-                                  cudaMemcpyHostToDevice, b->stream));
+                                  cudaMemcpyHostToDevice, j.s));
     ScanState init{};
     init.tau_key = 0ull;
     init.theta = 0.f;
@@ -205,9 +225,8 @@ gepi_status Engine::admit(Job &j) {
     init.tau_f = -INFINITY;
     init.tau_val = -INFINITY;
     *b->h_state = init;
-    GEPI_CUDA(cudaMemcpyAsync(b->state, b->h_state, sizeof(ScanState), cudaMemcpyHostToDevice,
-                              b->stream));
-    GEPI_CUDA(cudaStreamSynchronize(b->stream));  // tiles and state in place before reuse of h_state
+    GEPI_CUDA(cudaMemcpyAsync(b->state, b->h_state, sizeof(ScanState), cudaMemcpyHostToDevice, j.s));
+    GEPI_CUDA(cudaStreamSynchronize(j.s));  // tiles and state in place before h_state is reused
 
     j.cur = 0;
     j.S = gepi_scan_stats{};
@@ -236,22 +255,40 @@ gepi_status Engine::admit(Job &j) {
     j.next = 0;
     j.count = 0;
     j.retries = 0;
+    j.ms_per_tile = 0.0;
     j.started = j.done = j.launched = false;
     j.t_admit = Clock::now();
     return GEPI_OK;
 }
 
 void Engine::release(Job &j) {
-    if (j.buf) free_.push_back(j.buf);
+    if (!j.buf) return;
+    DeviceGuard g(device_);
+    for (cudaStream_t s : j.buf->stream) cudaStreamSynchronize(s);  // nothing in flight on reuse
+    free_.push_back(j.buf);
     j.buf = nullptr;
 }
 
-// Queues the next batch of `j` on its stream: counting launch, state read-back.
+void Engine::fail(Job &j, gepi_status st) {
+    j.status = st;
+    j.error = gepi_last_error();
+    j.done = true;
+    j.launched = false;
+    j.t_done = Clock::now();
+}
+
+// Queues the next batch of `j`: counting launch, then the state read-back
+// and its completion event.  A request with little work left goes on the
+// high-priority stream; everything earlier of the request has completed, so
+// changing streams between batches keeps its order.
 gepi_status Engine::launch(Job &j) {
     JobBuffers *b = j.buf;
     gepi_planes *pl = j.rq.pl;
     const ScanRequest &r = j.rq;
     j.inflight = std::min(j.batch, j.ntiles - j.next);
+    const bool short_job =
+        j.ms_per_tile <= 0.0 || (double)(j.ntiles - j.next) * j.ms_per_tile < kShortMs;
+    j.s = b->stream[short_job ? 1 : 0];
     ScanCtx ctx;
     ctx.T = pl->d_T;
     ctx.F = pl->F;
@@ -262,21 +299,21 @@ gepi_status Engine::launch(Job &j) {
     ctx.st = b->state;
     ctx.cand = b->cand[j.cur];
     if (!j.started) {
-        GEPI_CUDA(cudaEventRecord(b->ev[0], b->stream));
+        GEPI_CUDA(cudaEventRecord(b->ev[0], j.s));
         j.started = true;
     }
-    GEPI_CUDA(cudaEventRecord(b->ev[2], b->stream));
+    GEPI_CUDA(cudaEventRecord(b->ev[2], j.s));
     if (j.tc)
         GEPI_CUDA(launch_tc_tiles(pl->d_tc_blocks, pl->n_snps, pl->Wp, pl->W0, b->tiles + j.next,
                                   (int)j.inflight, r.a0, r.a0 + r.na, r.b0, r.b0 + r.nb, ctx,
-                                  nullptr, &b->state->kerr, num_sms_, b->stream));
+                                  nullptr, &b->state->kerr, num_sms_, j.s));
     else
         GEPI_CUDA(launch_popc_tiles(pl->d_planes, pl->Wp, pl->W0, b->tiles + j.next,
                                     (int)j.inflight, r.a0, r.a0 + r.na, r.b0, r.b0 + r.nb, ctx,
-                                    nullptr, b->stream));
-    GEPI_CUDA(cudaEventRecord(b->ev[3], b->stream));
-    GEPI_CUDA(cudaMemcpyAsync(b->h_state, b->state, sizeof(ScanState), cudaMemcpyDeviceToHost,
-                              b->stream));
+                                    nullptr, j.s));
+    GEPI_CUDA(cudaEventRecord(b->ev[3], j.s));
+    GEPI_CUDA(cudaMemcpyAsync(b->h_state, b->state, sizeof(ScanState), cudaMemcpyDeviceToHost, j.s));
+    GEPI_CUDA(cudaEventRecord(b->ev[4], j.s));
     j.launched = true;
     return GEPI_OK;
 }
@@ -303,11 +340,10 @@ gepi_status Engine::select(Job &j, int n_override, uint32_t n_compact) {
         cudaGraphExec_t &x = b->sel_graph[j.cur];
         if (!x) {
             cudaGraph_t graph = nullptr;
-            if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+            if (cudaStreamBeginCapture(j.s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
                 cudaError_t e = run_select_compact(in, out, b->state, d_sel_, b->cap, (uint32_t)k,
-                                                   -1, 0xFFFFFFFFu, obj, j.lp_margin, num_sms_,
-                                                   b->stream);
-                cudaError_t e2 = cudaStreamEndCapture(b->stream, &graph);
+                                                   -1, 0xFFFFFFFFu, obj, j.lp_margin, num_sms_, j.s);
+                cudaError_t e2 = cudaStreamEndCapture(j.s, &graph);
                 if (e == cudaSuccess && e2 == cudaSuccess && graph &&
                     cudaGraphInstantiate(&x, graph, 0) != cudaSuccess)
                     x = nullptr;
@@ -316,17 +352,16 @@ gepi_status Engine::select(Job &j, int n_override, uint32_t n_compact) {
             }
         }
         if (x) {
-            GEPI_CUDA(cudaGraphLaunch(x, b->stream));
+            GEPI_CUDA(cudaGraphLaunch(x, j.s));
             done = true;
         }
     }
     if (!done)
         GEPI_CUDA(run_select_compact(in, out, b->state, d_sel_, b->cap, (uint32_t)k, n_override,
-                                     n_compact, obj, j.lp_margin, num_sms_, b->stream));
+                                     n_compact, obj, j.lp_margin, num_sms_, j.s));
     j.cur ^= 1;
-    GEPI_CUDA(cudaMemcpyAsync(b->h_state, b->state, sizeof(ScanState), cudaMemcpyDeviceToHost,
-                              b->stream));
-    GEPI_CUDA(cudaStreamSynchronize(b->stream));
+    GEPI_CUDA(cudaMemcpyAsync(b->h_state, b->state, sizeof(ScanState), cudaMemcpyDeviceToHost, j.s));
+    GEPI_CUDA(cudaStreamSynchronize(j.s));
     j.count = b->h_state->count;
     return GEPI_OK;
 }
@@ -338,9 +373,9 @@ gepi_status Engine::finish(Job &j) {
     std::vector<Cand> host(count);
     if (count)
         GEPI_CUDA(cudaMemcpyAsync(host.data(), b->cand[j.cur], (size_t)count * sizeof(Cand),
-                                  cudaMemcpyDeviceToHost, b->stream));
-    GEPI_CUDA(cudaEventRecord(b->ev[1], b->stream));
-    GEPI_CUDA(cudaStreamSynchronize(b->stream));
+                                  cudaMemcpyDeviceToHost, j.s));
+    GEPI_CUDA(cudaEventRecord(b->ev[1], j.s));
+    GEPI_CUDA(cudaStreamSynchronize(j.s));
     float ms = 0.f;
     if (j.started) GEPI_CUDA(cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]));
     j.S.scan_ms = ms;
@@ -363,7 +398,7 @@ gepi_status Engine::finish(Job &j) {
     return GEPI_OK;
 }
 
-// Bookkeeping of one request after its batch's state arrived (stream synced).
+// Bookkeeping of one request after its batch's state arrived.
 gepi_status Engine::settle(Job &j) {
     JobBuffers *b = j.buf;
     j.launched = false;
@@ -377,6 +412,7 @@ gepi_status Engine::settle(Job &j) {
         return set_error(GEPI_ERR_TIMEOUT, "counting kernel gave up a bounded wait (code " +
                                                std::to_string(st.kerr) + ")");
     const size_t nbt = j.inflight;
+    if (nbt > 0 && ms > 0.f) j.ms_per_tile = (double)ms / (double)nbt;
     if (st.overflow) {
         // Tighten with everything captured (a valid lower bound), drop this
         // batch's partial appends, retry it in halves.  Only more than `cap`
@@ -396,57 +432,59 @@ gepi_status Engine::settle(Job &j) {
     if (j.next >= j.ntiles) return finish(j);
     if (j.count > j.budget) GEPI_TRY(select(j, -1, 0xFFFFFFFFu));
     // Next batch: as many tiles as the remaining budget allows at the append
-    // rate just observed, growing at most 8x per step.
+    // rate just observed, growing at most 8x per step, and within the device
+    // time quantum at the rate just measured (an over-estimate when other
+    // requests shared the SMs).
     const double rate = std::max(1.0, (double)appended) / (double)nbt;
     const double room = (double)j.budget - (double)j.count;
     double nb_next = room > 0 ? room / rate : 1.0;
     nb_next = std::min(nb_next, 8.0 * (double)nbt);
+    if (quantum_ms_ > 0.0 && j.ms_per_tile > 0.0)
+        nb_next = std::min(nb_next, quantum_ms_ / j.ms_per_tile);
     j.batch = (size_t)std::max(1.0, nb_next);
     return GEPI_OK;
 }
 
-// One engine step: the next batch of every active request is queued on the
-// request's stream (so they run concurrently), then each is settled.  A
-// request that fails gets its status; the others carry on.
-gepi_status Engine::step(std::vector<Job *> &active) {
+int Engine::poll(std::vector<Job *> &active) {
     DeviceGuard g(device_);
-    std::vector<Job *> run;
+    int progressed = 0;
     for (Job *j : active) {
-        if (j->done || j->status != GEPI_OK) continue;
+        if (j->done || j->launched) continue;
         if (j->next >= j->ntiles) {  // empty range
-            j->status = finish(*j);
-            if (j->status != GEPI_OK) {
-                j->error = gepi_last_error();
-                j->done = true;
-            }
+            gepi_status st = finish(*j);
+            if (st != GEPI_OK) fail(*j, st);
+            ++progressed;
             continue;
         }
         gepi_status st = launch(*j);
         if (st != GEPI_OK) {
-            j->status = st;
-            j->error = gepi_last_error();
-            j->done = true;
-            continue;
+            fail(*j, st);
+            ++progressed;
         }
-        run.push_back(j);
     }
-    for (Job *j : run) {
+    for (Job *j : active) {
+        if (!j->launched) continue;
+        const cudaError_t q = cudaEventQuery(j->buf->ev[4]);
+        if (q == cudaErrorNotReady) continue;
         gepi_status st = GEPI_OK;
-        if (cudaStreamSynchronize(j->buf->stream) != cudaSuccess)
-            st = set_error(GEPI_ERR_CUDA, std::string("counting launch: ") +
-                                              cudaGetErrorString(cudaGetLastError()));
-        else
+        if (q != cudaSuccess) {
+            cudaGetLastError();
+            st = set_error(GEPI_ERR_CUDA, std::string("counting launch: ") + cudaGetErrorString(q));
+        } else {
             st = settle(*j);
-        if (st != GEPI_OK) {
-            j->status = st;
-            j->error = gepi_last_error();
-            j->done = true;
+        }
+        if (st != GEPI_OK) fail(*j, st);
+        ++progressed;
+        // a request whose batch just settled launches its next one at once
+        if (!j->done && !j->launched && j->next < j->ntiles) {
+            st = launch(*j);
+            if (st != GEPI_OK) fail(*j, st);
         }
     }
-    return GEPI_OK;
+    return progressed;
 }
 
-// ---- the plane-set engine used by gepi_scan_batch ---------------------------
+// ---- the device engines used by gepi_scan_batch -----------------------------
 
 namespace {
 
@@ -457,7 +495,7 @@ gepi_status device_engine(int device, Engine **out) {
     std::lock_guard<std::mutex> lk(g_engines_mu);
     auto it = g_engines.find(device);
     if (it == g_engines.end()) {
-        auto e = std::make_unique<Engine>(device);
+        auto e = std::make_unique<Engine>(device, 0.0);
         GEPI_TRY(e->init());
         it = g_engines.emplace(device, std::move(e)).first;
     }
@@ -481,7 +519,7 @@ gepi_status check_request(const gepi_scan_req &r, ScanRequest *out) {
         q.b0 = 0;
         q.nb = n;
     } else {
-        if (r.a0 < 0 || r.b0 < 0 || r.a0 + r.na > n || r.b0 + r.nb > n)
+        if (r.a0 < 0 || r.b0 < 0 || (int64_t)r.a0 + r.na > n || (int64_t)r.b0 + r.nb > n)
             return set_error(GEPI_ERR_ARG, "scan request: SNP range outside the planes");
         q.a0 = r.a0;
         q.na = r.na;
@@ -497,6 +535,8 @@ gepi_status check_request(const gepi_scan_req &r, ScanRequest *out) {
 
 // Device memory a request holds while admitted: two candidate buffers.
 size_t request_footprint(int k) { return 2 * cand_cap(k) * sizeof(Cand) + sizeof(ScanState); }
+
+void idle_wait() { std::this_thread::sleep_for(std::chrono::microseconds(20)); }
 
 }  // namespace
 
@@ -532,7 +572,7 @@ gepi_status gepi_scan_batch(const gepi_scan_req *reqs, int32_t n, gepi_result *c
         bool any = false;
         for (Job *j : active) any |= !j->done;
         if (!any) break;
-        st = eng->step(active);
+        if (eng->poll(active) == 0) idle_wait();
         for (Job *j : active)
             if (j->status != GEPI_OK) {
                 st = set_error(j->status, j->error);
@@ -567,6 +607,7 @@ struct gepi_server {
 void gepi_server::run() {
     cudaSetDevice(device);
     std::vector<Job *> active, admitting;
+    int idle = 0;
     for (;;) {
         {
             std::unique_lock<std::mutex> lk(mu);
@@ -584,30 +625,39 @@ void gepi_server::run() {
                 if (stop) return;
                 cv_work.wait(lk);
             }
+            // nothing settled last round: sleep briefly, waking on a submit
+            if (idle > 0 && admitting.empty())
+                cv_work.wait_for(lk, std::chrono::microseconds(20));
         }
         for (Job *j : admitting) {
-            j->status = engine->admit(*j);
-            if (j->status != GEPI_OK) {
+            gepi_status st = engine->admit(*j);
+            if (st != GEPI_OK) {
+                j->status = st;
                 j->error = gepi_last_error();
                 j->done = true;
+                j->t_done = Clock::now();
             }
             active.push_back(j);
         }
         admitting.clear();
-        engine->step(active);
-        std::lock_guard<std::mutex> lk(mu);
+        idle = engine->poll(active) == 0 ? 1 : 0;
         bool any = false;
         for (Job *j : active)
             if (j->done) {
-                if (j->t_done.time_since_epoch().count() == 0) j->t_done = Clock::now();
                 engine->release(*j);
+                any = true;
+            }
+        if (!any) continue;
+        std::lock_guard<std::mutex> lk(mu);
+        for (Job *j : active)
+            if (j->done) {
                 used -= j->footprint;
                 j->finished = true;
-                any = true;
             }
         active.erase(std::remove_if(active.begin(), active.end(), [](Job *j) { return j->done; }),
                      active.end());
-        if (any) cv_done.notify_all();
+        idle = 0;
+        cv_done.notify_all();
     }
 }
 
@@ -620,7 +670,7 @@ gepi_status gepi_server_create(int32_t device, size_t hbm_budget_bytes, gepi_ser
     auto srv = std::make_unique<gepi_server>();
     srv->device = device;
     srv->budget = hbm_budget_bytes ? hbm_budget_bytes : (16ull << 30);
-    srv->engine = std::make_unique<Engine>(device);
+    srv->engine = std::make_unique<Engine>(device, 20.0);
     GEPI_TRY(srv->engine->init());
     gepi_server *p = srv.get();
     p->thread = std::thread([p] { p->run(); });
@@ -668,7 +718,8 @@ gepi_status gepi_server_wait(gepi_server *srv, uint64_t ticket, gepi_result *top
     }
     if (info) {
         std::memset(info, 0, sizeof *info);
-        info->queue_ms = ms_between(j->t_submit, j->t_admit);
+        const bool admitted = j->t_admit.time_since_epoch().count() != 0;
+        info->queue_ms = admitted ? ms_between(j->t_submit, j->t_admit) : 0.0;
         info->latency_ms = ms_between(j->t_submit, j->t_done);
         info->device_ms = j->S.scan_ms;
         info->snp_pairs = j->S.snp_pairs;
@@ -687,6 +738,7 @@ void gepi_server_destroy(gepi_server *srv) {
         for (Job *j : srv->pending) {
             j->status = GEPI_ERR_ARG;
             j->error = "server destroyed before the request was admitted";
+            j->t_done = Clock::now();
             j->finished = true;
         }
         srv->pending.clear();

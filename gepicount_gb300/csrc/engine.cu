@@ -6,16 +6,19 @@
 // (launch_process_gpu_1, src/kernels/kernel1.cu:387-483).  Each request walks
 // its tile list in adaptive batches as a direct scan does, with the same
 // exact thresholds, so its results are bit-identical to gepi_scan_range's.
-// Requests progress independently: the engine polls each request's
-// completion event, settles a finished batch (threshold raise by a device
-// radix select replayed from a CUDA graph, overflow retry in halves, final
-// select and top-k read-back) and launches its next batch at once, so the
-// counting kernels of different requests share the SMs.  Batches can be
-// capped to a device-time quantum, and requests with little work left run on
-// a high-priority stream, so short requests are not held behind long ones.
+// Requests progress independently and the host never waits on one request's
+// device work while others could be launched: every device operation of a
+// request (a counting batch, a threshold-raising radix select replayed from a
+// CUDA graph, an overflow retry's compaction) ends in a completion event that
+// the engine polls; when it fires, the request's next operation is issued at
+// once.  Batches can be capped to a device-time quantum, and requests with
+// little work left run on a high-priority stream, so short requests are not
+// held behind long ones.  Tile lists depend only on the SNP ranges and tile
+// shape and are cached on the device across requests.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
@@ -62,6 +65,8 @@ double ms_between(Clock::time_point a, Clock::time_point b) {
 // Requests whose remaining device work is estimated below this run on the
 // high-priority stream.
 constexpr double kShortMs = 50.0;
+// Device bytes of cached tile lists kept when no request uses them.
+constexpr size_t kTileCacheBytes = 1ull << 30;
 
 }  // namespace
 
@@ -71,21 +76,32 @@ struct ScanRequest {
     int k = 0, objective = 0, method = 0;
 };
 
+// Device tile list of one (SNP ranges, tile shape), shared by requests.
+struct TileList {
+    int2 *d = nullptr;
+    size_t n = 0;
+    int refs = 0;
+    uint64_t stamp = 0;  // last use, for eviction
+};
+using TileKey = std::array<int, 6>;
+
 // Device resources of one request, pooled by candidate capacity.
 struct JobBuffers {
     Cand *cand[2] = {nullptr, nullptr};
     uint32_t cap = 0;
     ScanState *state = nullptr;
     ScanState *h_state = nullptr;  // pinned
-    int2 *tiles = nullptr;
-    size_t tiles_cap = 0;
+    void *sel = nullptr;           // radix-select scratch
     cudaStream_t stream[2] = {nullptr, nullptr};  // normal, high priority
-    // scan start, scan done, batch launch start / end, batch state read back
+    // scan start, scan done, batch launch start / end, operation complete
     cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     cudaGraphExec_t sel_graph[2] = {nullptr, nullptr};  // select+compact cand[c] -> cand[c^1]
     int sel_k = -1, sel_obj = -1;
     float sel_margin = 0.f;
 };
+
+// The device operation a request has in flight.
+enum class Op { None, Batch, SelRetry, SelBudget, SelFinal };
 
 struct Job {
     ScanRequest rq;
@@ -96,15 +112,18 @@ struct Job {
     bool finished = false;  // serving: results ready for the waiter
     bool tc = false;
     int TA = 0, TB = 0;
-    size_t ntiles = 0, next = 0, batch = 1, inflight = 0;
+    TileList *tl = nullptr;
+    size_t ntiles = 0, next = 0, batch = 1, inflight = 0, last_nbt = 0;
+    uint32_t last_appended = 0;
     double ms_per_tile = 0.0;  // from the last batch (0: not measured yet)
     JobBuffers *buf = nullptr;
-    cudaStream_t s = nullptr;  // stream of the job's work in flight
+    cudaStream_t s = nullptr;  // stream of the request's last operation
+    Op op = Op::None;
     int cur = 0;
     uint32_t count = 0, budget = 0;
     int retries = 0;
     float lp_margin = 0.f;
-    bool started = false, done = false, launched = false;
+    bool started = false, done = false, final_selected = false;
     gepi_status status = GEPI_OK;
     std::string error;
     gepi_scan_stats S{};
@@ -117,26 +136,37 @@ class Engine {
     Engine(int device, double quantum_ms) : device_(device), quantum_ms_(quantum_ms) {}
     ~Engine();
     gepi_status init();
+    // Method choice, plane-set tables and the device tile list: may run on
+    // any thread (serialised internally).
+    gepi_status prepare(Job &j);
+    // Candidate buffers and the initial scan state: the polling thread.
     gepi_status admit(Job &j);
-    // Launches the next batch of every idle request and settles those whose
-    // batch has completed; returns how many were settled or finished.
+    // Issues the next operation of every idle request and completes those
+    // whose operation has finished; returns how many completed or finished.
     int poll(std::vector<Job *> &active);
+    // Returns a request's buffers (after its streams drain) and tile list.
     void release(Job &j);
     std::mutex run_mu;  // serialises gepi_scan_batch calls on the device
 
    private:
+    gepi_status advance(Job &j);
+    gepi_status complete(Job &j);
     gepi_status launch(Job &j);
-    gepi_status settle(Job &j);
-    gepi_status select(Job &j, int n_override, uint32_t n_compact);
+    gepi_status select_async(Job &j, int n_override, uint32_t n_compact, Op op);
     gepi_status finish(Job &j);
+    void size_next_batch(Job &j);
     void fail(Job &j, gepi_status st);
 
     int device_ = 0, num_sms_ = 0;
     double quantum_ms_ = 0.0;
     int prio_lo_ = 0, prio_hi_ = 0;
-    void *d_sel_ = nullptr;  // select scratch: one select in flight at a time (host-serialised)
     std::vector<std::unique_ptr<JobBuffers>> pool_;
     std::vector<JobBuffers *> free_;
+    std::mutex prep_mu_, cache_mu_;
+    cudaStream_t upload_ = nullptr;
+    std::map<TileKey, TileList> tiles_;
+    size_t tile_bytes_ = 0;
+    uint64_t stamp_ = 0;
 };
 
 Engine::~Engine() {
@@ -147,7 +177,7 @@ Engine::~Engine() {
         dfree(b->cand[0]);
         dfree(b->cand[1]);
         dfree(b->state);
-        dfree(b->tiles);
+        dfree(b->sel);
         if (b->h_state) cudaFreeHost(b->h_state);
         for (cudaEvent_t e : b->ev)
             if (e) cudaEventDestroy(e);
@@ -156,7 +186,12 @@ Engine::~Engine() {
         for (cudaStream_t s : b->stream)
             if (s) cudaStreamDestroy(s);
     }
-    dfree(d_sel_);
+    for (auto &kv : tiles_)
+        if (kv.second.d) cudaFreeAsync(kv.second.d, upload_);
+    if (upload_) {
+        cudaStreamSynchronize(upload_);
+        cudaStreamDestroy(upload_);
+    }
 }
 
 gepi_status Engine::init() {
@@ -164,11 +199,12 @@ gepi_status Engine::init() {
     if (!g.ok) return set_error(GEPI_ERR_CUDA, "cudaSetDevice failed");
     GEPI_CUDA(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, device_));
     GEPI_CUDA(cudaDeviceGetStreamPriorityRange(&prio_lo_, &prio_hi_));
-    GEPI_CUDA(cudaMalloc(&d_sel_, sel_state_bytes()));
+    GEPI_CUDA(cudaStreamCreateWithFlags(&upload_, cudaStreamNonBlocking));
     return GEPI_OK;
 }
 
-gepi_status Engine::admit(Job &j) {
+gepi_status Engine::prepare(Job &j) {
+    std::lock_guard<std::mutex> lk(prep_mu_);
     DeviceGuard g(device_);
     const ScanRequest &rq = j.rq;
     gepi_planes *pl = rq.pl;
@@ -180,11 +216,74 @@ gepi_status Engine::admit(Job &j) {
     GEPI_CUDA(cudaStreamSynchronize(pl->stream));  // decode, relayout, tables done
     j.TA = j.tc ? tc_tile_a_snps() : popc_tile_snps();
     j.TB = j.tc ? tc_tile_b_snps() : popc_tile_snps();
-    std::vector<int2> tiles;
-    pl_build_tiles(rq.a0, rq.a0 + rq.na, rq.b0, rq.b0 + rq.nb, j.TA, j.TB, true, 8, tiles);
-    j.ntiles = tiles.size();
 
-    const uint64_t cap = cand_cap(rq.k);
+    const TileKey key{rq.a0, rq.a0 + rq.na, rq.b0, rq.b0 + rq.nb, j.TA, j.TB};
+    {
+        std::lock_guard<std::mutex> ck(cache_mu_);
+        auto it = tiles_.find(key);
+        if (it != tiles_.end()) {
+            it->second.refs += 1;
+            it->second.stamp = ++stamp_;
+            j.tl = &it->second;
+        }
+    }
+    if (!j.tl) {
+        // only this thread inserts (prep_mu_ held), so the key is still absent
+        std::vector<int2> tiles;
+        pl_build_tiles(key[0], key[1], key[2], key[3], j.TA, j.TB, true, 8, tiles);
+        TileList t;
+        t.n = tiles.size();
+        if (t.n) {
+            const size_t bytes = t.n * sizeof(int2);
+            GEPI_TRY(pl_check_mem(bytes, "tile list"));
+            GEPI_CUDA(cudaMallocAsync((void **)&t.d, bytes, upload_));
+            GEPI_CUDA(cudaMemcpyAsync(t.d, tiles.data(), bytes, cudaMemcpyHostToDevice, upload_));
+            GEPI_CUDA(cudaStreamSynchronize(upload_));
+        }
+        std::lock_guard<std::mutex> ck(cache_mu_);
+        t.refs = 1;
+        t.stamp = ++stamp_;
+        TileList &e = tiles_[key];
+        e = t;
+        j.tl = &e;
+        tile_bytes_ += t.n * sizeof(int2);
+        // evict unused lists, least recently used first, above the cache size
+        while (tile_bytes_ > kTileCacheBytes) {
+            auto victim = tiles_.end();
+            for (auto it = tiles_.begin(); it != tiles_.end(); ++it)
+                if (it->second.refs == 0 &&
+                    (victim == tiles_.end() || it->second.stamp < victim->second.stamp))
+                    victim = it;
+            if (victim == tiles_.end()) break;
+            tile_bytes_ -= victim->second.n * sizeof(int2);
+            if (victim->second.d) cudaFreeAsync(victim->second.d, upload_);
+            tiles_.erase(victim);
+        }
+    }
+    j.ntiles = j.tl->n;
+    j.S = gepi_scan_stats{};
+    j.S.method = method;
+    j.S.tile_snps = j.TA;
+    j.S.tiles = j.ntiles;
+    {
+        // pairs (s, t), t < s, s in A, t in B; and SNPs in both ranges
+        const int64_t ia0 = rq.a0, ia1 = (int64_t)rq.a0 + rq.na, ib0 = rq.b0,
+                      ib1 = (int64_t)rq.b0 + rq.nb;
+        uint64_t pairs = 0;
+        for (int64_t s = ia0; s < ia1; ++s) {
+            const int64_t hi = std::min<int64_t>(s, ib1);
+            if (hi > ib0) pairs += (uint64_t)(hi - ib0);
+        }
+        j.S.snp_pairs = pairs;
+        const int64_t lo = std::max(ia0, ib0), hi = std::min(ia1, ib1);
+        j.S.diag_snps = hi > lo ? (uint64_t)(hi - lo) : 0;
+    }
+    return GEPI_OK;
+}
+
+gepi_status Engine::admit(Job &j) {
+    DeviceGuard g(device_);
+    const uint64_t cap = cand_cap(j.rq.k);
     if (cap > (1ull << 31)) return set_error(GEPI_ERR_LIMIT, "topmost too large");
     JobBuffers *b = nullptr;
     for (size_t i = 0; i < free_.size(); ++i)
@@ -203,84 +302,68 @@ gepi_status Engine::admit(Job &j) {
         GEPI_CUDA(cudaMalloc(&b->cand[0], cap * sizeof(Cand)));
         GEPI_CUDA(cudaMalloc(&b->cand[1], cap * sizeof(Cand)));
         GEPI_CUDA(cudaMalloc(&b->state, sizeof(ScanState)));
+        GEPI_CUDA(cudaMalloc(&b->sel, sel_state_bytes()));
         GEPI_CUDA(cudaMallocHost(&b->h_state, sizeof(ScanState)));
         GEPI_CUDA(cudaStreamCreateWithPriority(&b->stream[0], cudaStreamNonBlocking, prio_lo_));
         GEPI_CUDA(cudaStreamCreateWithPriority(&b->stream[1], cudaStreamNonBlocking, prio_hi_));
         for (cudaEvent_t &e : b->ev) GEPI_CUDA(cudaEventCreate(&e));
     }
     j.buf = b;
-    j.s = b->stream[0];
-    if (tiles.size() > b->tiles_cap) {
-        dfree(b->tiles);
-        GEPI_CUDA(cudaMalloc(&b->tiles, std::max<size_t>(1, tiles.size()) * sizeof(int2)));
-        b->tiles_cap = tiles.size();
-    }
-    if (!tiles.empty())
-        GEPI_CUDA(cudaMemcpyAsync(b->tiles, tiles.data(), tiles.size() * sizeof(int2),
-                                  cudaMemcpyHostToDevice, j.s));
+    // the first batch goes on the high-priority stream (no rate measured yet),
+    // so the state upload is ordered before it on that stream
+    j.s = b->stream[1];
     ScanState init{};
     init.tau_key = 0ull;
     init.theta = 0.f;
     init.lp_thr = INFINITY;
     init.tau_f = -INFINITY;
     init.tau_val = -INFINITY;
-    *b->h_state = init;
+    *b->h_state = init;  // the previous user's copies have drained (release)
     GEPI_CUDA(cudaMemcpyAsync(b->state, b->h_state, sizeof(ScanState), cudaMemcpyHostToDevice, j.s));
-    GEPI_CUDA(cudaStreamSynchronize(j.s));  // tiles and state in place before h_state is reused
 
-    j.cur = 0;
-    j.S = gepi_scan_stats{};
-    j.S.method = method;
-    j.S.tile_snps = j.TA;
-    j.S.tiles = j.ntiles;
-    {
-        // pairs (s, t), t < s, s in A, t in B; and SNPs in both ranges
-        const int64_t ia0 = rq.a0, ia1 = (int64_t)rq.a0 + rq.na, ib0 = rq.b0,
-                      ib1 = (int64_t)rq.b0 + rq.nb;
-        uint64_t pairs = 0;
-        for (int64_t s = ia0; s < ia1; ++s) {
-            const int64_t hi = std::min<int64_t>(s, ib1);
-            if (hi > ib0) pairs += (uint64_t)(hi - ib0);
-        }
-        j.S.snp_pairs = pairs;
-        const int64_t lo = std::max(ia0, ib0), hi = std::min(ia1, ib1);
-        j.S.diag_snps = hi > lo ? (uint64_t)(hi - lo) : 0;
-    }
     // as in the direct scan: a first batch of about cap/4 tests (Fisher: 64 Ki)
     const double tests_per_tile = 20.0 * j.TA * j.TB;
-    const double pilot = rq.objective == GEPI_ENTROPY ? b->cap / 4.0 : 1.0 * (1 << 16);
+    const double pilot = j.rq.objective == GEPI_ENTROPY ? b->cap / 4.0 : 1.0 * (1 << 16);
     j.batch = (size_t)std::max(1.0, std::floor(pilot / tests_per_tile));
     j.budget = b->cap / 2;
-    j.lp_margin = 2e-6f * pl->lf_max + 1e-3f;
+    j.lp_margin = 2e-6f * j.rq.pl->lf_max + 1e-3f;
+    j.cur = 0;
     j.next = 0;
     j.count = 0;
     j.retries = 0;
     j.ms_per_tile = 0.0;
-    j.started = j.done = j.launched = false;
+    j.op = Op::None;
+    j.started = j.done = j.final_selected = false;
     j.t_admit = Clock::now();
     return GEPI_OK;
 }
 
 void Engine::release(Job &j) {
-    if (!j.buf) return;
     DeviceGuard g(device_);
-    for (cudaStream_t s : j.buf->stream) cudaStreamSynchronize(s);  // nothing in flight on reuse
-    free_.push_back(j.buf);
-    j.buf = nullptr;
+    if (j.buf) {
+        for (cudaStream_t s : j.buf->stream) cudaStreamSynchronize(s);  // nothing in flight on reuse
+        free_.push_back(j.buf);
+        j.buf = nullptr;
+    }
+    if (j.tl) {
+        std::lock_guard<std::mutex> ck(cache_mu_);
+        j.tl->refs -= 1;
+        j.tl = nullptr;
+    }
 }
 
 void Engine::fail(Job &j, gepi_status st) {
     j.status = st;
     j.error = gepi_last_error();
     j.done = true;
-    j.launched = false;
+    j.op = Op::None;
     j.t_done = Clock::now();
 }
 
-// Queues the next batch of `j`: counting launch, then the state read-back
-// and its completion event.  A request with little work left goes on the
-// high-priority stream; everything earlier of the request has completed, so
-// changing streams between batches keeps its order.
+// Queues the next batch of `j`: counting launch, state read-back, completion
+// event.  A request with little work left goes on the high-priority stream;
+// every earlier operation of the request has completed, so changing streams
+// between operations keeps its order.
 gepi_status Engine::launch(Job &j) {
     JobBuffers *b = j.buf;
     gepi_planes *pl = j.rq.pl;
@@ -304,23 +387,24 @@ gepi_status Engine::launch(Job &j) {
     }
     GEPI_CUDA(cudaEventRecord(b->ev[2], j.s));
     if (j.tc)
-        GEPI_CUDA(launch_tc_tiles(pl->d_tc_blocks, pl->n_snps, pl->Wp, pl->W0, b->tiles + j.next,
+        GEPI_CUDA(launch_tc_tiles(pl->d_tc_blocks, pl->n_snps, pl->Wp, pl->W0, j.tl->d + j.next,
                                   (int)j.inflight, r.a0, r.a0 + r.na, r.b0, r.b0 + r.nb, ctx,
                                   nullptr, &b->state->kerr, num_sms_, j.s));
     else
-        GEPI_CUDA(launch_popc_tiles(pl->d_planes, pl->Wp, pl->W0, b->tiles + j.next,
+        GEPI_CUDA(launch_popc_tiles(pl->d_planes, pl->Wp, pl->W0, j.tl->d + j.next,
                                     (int)j.inflight, r.a0, r.a0 + r.na, r.b0, r.b0 + r.nb, ctx,
                                     nullptr, j.s));
     GEPI_CUDA(cudaEventRecord(b->ev[3], j.s));
     GEPI_CUDA(cudaMemcpyAsync(b->h_state, b->state, sizeof(ScanState), cudaMemcpyDeviceToHost, j.s));
     GEPI_CUDA(cudaEventRecord(b->ev[4], j.s));
-    j.launched = true;
+    j.op = Op::Batch;
     return GEPI_OK;
 }
 
 // Device radix select of the k-th best key, then compaction into the other
-// buffer.  The common form (all entries) replays a captured CUDA graph.
-gepi_status Engine::select(Job &j, int n_override, uint32_t n_compact) {
+// buffer, state read-back and completion event.  The common form (all
+// entries) replays a CUDA graph captured once per buffer orientation.
+gepi_status Engine::select_async(Job &j, int n_override, uint32_t n_compact, Op op) {
     JobBuffers *b = j.buf;
     const int k = j.rq.k, obj = j.rq.objective;
     Cand *in = b->cand[j.cur], *out = b->cand[j.cur ^ 1];
@@ -341,7 +425,7 @@ gepi_status Engine::select(Job &j, int n_override, uint32_t n_compact) {
         if (!x) {
             cudaGraph_t graph = nullptr;
             if (cudaStreamBeginCapture(j.s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-                cudaError_t e = run_select_compact(in, out, b->state, d_sel_, b->cap, (uint32_t)k,
+                cudaError_t e = run_select_compact(in, out, b->state, b->sel, b->cap, (uint32_t)k,
                                                    -1, 0xFFFFFFFFu, obj, j.lp_margin, num_sms_, j.s);
                 cudaError_t e2 = cudaStreamEndCapture(j.s, &graph);
                 if (e == cudaSuccess && e2 == cudaSuccess && graph &&
@@ -357,25 +441,25 @@ gepi_status Engine::select(Job &j, int n_override, uint32_t n_compact) {
         }
     }
     if (!done)
-        GEPI_CUDA(run_select_compact(in, out, b->state, d_sel_, b->cap, (uint32_t)k, n_override,
+        GEPI_CUDA(run_select_compact(in, out, b->state, b->sel, b->cap, (uint32_t)k, n_override,
                                      n_compact, obj, j.lp_margin, num_sms_, j.s));
     j.cur ^= 1;
     GEPI_CUDA(cudaMemcpyAsync(b->h_state, b->state, sizeof(ScanState), cudaMemcpyDeviceToHost, j.s));
-    GEPI_CUDA(cudaStreamSynchronize(j.s));
-    j.count = b->h_state->count;
+    GEPI_CUDA(cudaEventRecord(b->ev[4], j.s));
+    j.op = op;
     return GEPI_OK;
 }
 
+// Reads the surviving candidates back and writes the ranked top-k.
 gepi_status Engine::finish(Job &j) {
     JobBuffers *b = j.buf;
-    if (j.count > (uint32_t)j.rq.k) GEPI_TRY(select(j, -1, 0xFFFFFFFFu));
     const uint32_t count = j.count;
     std::vector<Cand> host(count);
-    if (count)
+    GEPI_CUDA(cudaEventRecord(b->ev[1], j.s));
+    if (count)  // pageable destination: returns when the copy is done
         GEPI_CUDA(cudaMemcpyAsync(host.data(), b->cand[j.cur], (size_t)count * sizeof(Cand),
                                   cudaMemcpyDeviceToHost, j.s));
-    GEPI_CUDA(cudaEventRecord(b->ev[1], j.s));
-    GEPI_CUDA(cudaStreamSynchronize(j.s));
+    GEPI_CUDA(cudaEventSynchronize(b->ev[1]));
     float ms = 0.f;
     if (j.started) GEPI_CUDA(cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]));
     j.S.scan_ms = ms;
@@ -398,88 +482,109 @@ gepi_status Engine::finish(Job &j) {
     return GEPI_OK;
 }
 
-// Bookkeeping of one request after its batch's state arrived.
-gepi_status Engine::settle(Job &j) {
-    JobBuffers *b = j.buf;
-    j.launched = false;
-    const ScanState st = *b->h_state;
-    float ms = 0.f;
-    GEPI_CUDA(cudaEventElapsedTime(&ms, b->ev[2], b->ev[3]));
-    j.S.count_ms += ms;
-    j.S.max_count_ms = std::max<double>(j.S.max_count_ms, ms);
-    j.S.count_launches += 1;
-    if (st.kerr)
-        return set_error(GEPI_ERR_TIMEOUT, "counting kernel gave up a bounded wait (code " +
-                                               std::to_string(st.kerr) + ")");
-    const size_t nbt = j.inflight;
-    if (nbt > 0 && ms > 0.f) j.ms_per_tile = (double)ms / (double)nbt;
-    if (st.overflow) {
-        // Tighten with everything captured (a valid lower bound), drop this
-        // batch's partial appends, retry it in halves.  Only more than `cap`
-        // exactly tied candidates can keep overflowing a 1-tile batch.
-        if (++j.retries > 64)
-            return set_error(GEPI_ERR_LIMIT, "candidate buffer keeps overflowing (massive ties)");
-        j.S.overflows += 1;
-        GEPI_TRY(select(j, (int)b->cap, j.count));
-        j.batch = std::max<size_t>(1, nbt / 2);
-        return GEPI_OK;
-    }
-    const uint32_t appended = st.count - j.count;
-    j.count = st.count;
-    j.next += nbt;
-    j.retries = 0;
-    j.S.batches += 1;
-    if (j.next >= j.ntiles) return finish(j);
-    if (j.count > j.budget) GEPI_TRY(select(j, -1, 0xFFFFFFFFu));
-    // Next batch: as many tiles as the remaining budget allows at the append
-    // rate just observed, growing at most 8x per step, and within the device
-    // time quantum at the rate just measured (an over-estimate when other
-    // requests shared the SMs).
-    const double rate = std::max(1.0, (double)appended) / (double)nbt;
+// Next batch: as many tiles as the remaining budget allows at the append
+// rate just observed, growing at most 8x per step, and within the device-time
+// quantum at the rate just measured (an over-estimate when other requests
+// shared the SMs).
+void Engine::size_next_batch(Job &j) {
+    const double nbt = (double)std::max<size_t>(1, j.last_nbt);
+    const double rate = std::max(1.0, (double)j.last_appended) / nbt;
     const double room = (double)j.budget - (double)j.count;
     double nb_next = room > 0 ? room / rate : 1.0;
-    nb_next = std::min(nb_next, 8.0 * (double)nbt);
+    nb_next = std::min(nb_next, 8.0 * nbt);
     if (quantum_ms_ > 0.0 && j.ms_per_tile > 0.0)
         nb_next = std::min(nb_next, quantum_ms_ / j.ms_per_tile);
     j.batch = (size_t)std::max(1.0, nb_next);
-    return GEPI_OK;
+}
+
+// Issues the request's next operation (no operation in flight).
+gepi_status Engine::advance(Job &j) {
+    if (j.next >= j.ntiles) {
+        if (j.count > (uint32_t)j.rq.k && !j.final_selected)
+            return select_async(j, -1, 0xFFFFFFFFu, Op::SelFinal);
+        return finish(j);
+    }
+    return launch(j);
+}
+
+// Consumes the result of the operation that just completed, then advances.
+gepi_status Engine::complete(Job &j) {
+    JobBuffers *b = j.buf;
+    const Op op = j.op;
+    j.op = Op::None;
+    const ScanState st = *b->h_state;
+    switch (op) {
+    case Op::Batch: {
+        float ms = 0.f;
+        GEPI_CUDA(cudaEventElapsedTime(&ms, b->ev[2], b->ev[3]));
+        j.S.count_ms += ms;
+        j.S.max_count_ms = std::max<double>(j.S.max_count_ms, ms);
+        j.S.count_launches += 1;
+        if (st.kerr)
+            return set_error(GEPI_ERR_TIMEOUT, "counting kernel gave up a bounded wait (code " +
+                                                   std::to_string(st.kerr) + ")");
+        const size_t nbt = j.inflight;
+        if (nbt > 0 && ms > 0.f) j.ms_per_tile = (double)ms / (double)nbt;
+        j.last_nbt = nbt;
+        if (st.overflow) {
+            // Tighten with everything captured (a valid lower bound), drop
+            // this batch's partial appends, retry it in halves.  Only more
+            // than `cap` exactly tied candidates keep overflowing 1 tile.
+            if (++j.retries > 64)
+                return set_error(GEPI_ERR_LIMIT, "candidate buffer keeps overflowing (massive ties)");
+            j.S.overflows += 1;
+            return select_async(j, (int)b->cap, j.count, Op::SelRetry);
+        }
+        j.last_appended = st.count - j.count;
+        j.count = st.count;
+        j.next += nbt;
+        j.retries = 0;
+        j.S.batches += 1;
+        if (j.next < j.ntiles && j.count > j.budget)
+            return select_async(j, -1, 0xFFFFFFFFu, Op::SelBudget);
+        if (j.next < j.ntiles) size_next_batch(j);
+        return advance(j);
+    }
+    case Op::SelRetry:
+        j.count = st.count;
+        j.batch = std::max<size_t>(1, j.last_nbt / 2);
+        return advance(j);
+    case Op::SelBudget:
+        j.count = st.count;
+        size_next_batch(j);
+        return advance(j);
+    case Op::SelFinal:
+        j.count = st.count;
+        j.final_selected = true;
+        return advance(j);
+    case Op::None:
+        break;
+    }
+    return advance(j);
 }
 
 int Engine::poll(std::vector<Job *> &active) {
     DeviceGuard g(device_);
     int progressed = 0;
     for (Job *j : active) {
-        if (j->done || j->launched) continue;
-        if (j->next >= j->ntiles) {  // empty range
-            gepi_status st = finish(*j);
-            if (st != GEPI_OK) fail(*j, st);
-            ++progressed;
-            continue;
-        }
-        gepi_status st = launch(*j);
-        if (st != GEPI_OK) {
-            fail(*j, st);
-            ++progressed;
-        }
+        if (j->done || j->op != Op::None) continue;
+        gepi_status st = advance(*j);  // newly admitted, or an empty range
+        if (st != GEPI_OK) fail(*j, st);
+        if (j->done) ++progressed;
     }
     for (Job *j : active) {
-        if (!j->launched) continue;
+        if (j->done || j->op == Op::None) continue;
         const cudaError_t q = cudaEventQuery(j->buf->ev[4]);
         if (q == cudaErrorNotReady) continue;
         gepi_status st = GEPI_OK;
         if (q != cudaSuccess) {
             cudaGetLastError();
-            st = set_error(GEPI_ERR_CUDA, std::string("counting launch: ") + cudaGetErrorString(q));
+            st = set_error(GEPI_ERR_CUDA, std::string("scan operation: ") + cudaGetErrorString(q));
         } else {
-            st = settle(*j);
+            st = complete(*j);
         }
         if (st != GEPI_OK) fail(*j, st);
         ++progressed;
-        // a request whose batch just settled launches its next one at once
-        if (!j->done && !j->launched && j->next < j->ntiles) {
-            st = launch(*j);
-            if (st != GEPI_OK) fail(*j, st);
-        }
     }
     return progressed;
 }
@@ -538,6 +643,14 @@ size_t request_footprint(int k) { return 2 * cand_cap(k) * sizeof(Cand) + sizeof
 
 void idle_wait() { std::this_thread::sleep_for(std::chrono::microseconds(20)); }
 
+double env_quantum_ms(double dflt) {
+    if (const char *e = std::getenv("GEPI_QUANTUM_MS")) {
+        const double v = std::atof(e);
+        if (v >= 0.0) return v;
+    }
+    return dflt;
+}
+
 }  // namespace
 
 }  // namespace gepi
@@ -564,7 +677,8 @@ gepi_status gepi_scan_batch(const gepi_scan_req *reqs, int32_t n, gepi_result *c
     std::vector<Job *> active;
     gepi_status st = GEPI_OK;
     for (Job &j : jobs) {
-        st = eng->admit(j);
+        st = eng->prepare(j);
+        if (st == GEPI_OK) st = eng->admit(j);
         active.push_back(&j);
         if (st != GEPI_OK) break;
     }
@@ -607,7 +721,7 @@ struct gepi_server {
 void gepi_server::run() {
     cudaSetDevice(device);
     std::vector<Job *> active, admitting;
-    int idle = 0;
+    bool idle = false;
     for (;;) {
         {
             std::unique_lock<std::mutex> lk(mu);
@@ -625,9 +739,8 @@ void gepi_server::run() {
                 if (stop) return;
                 cv_work.wait(lk);
             }
-            // nothing settled last round: sleep briefly, waking on a submit
-            if (idle > 0 && admitting.empty())
-                cv_work.wait_for(lk, std::chrono::microseconds(20));
+            // nothing completed last time round: sleep briefly, waking on a submit
+            if (idle && admitting.empty()) cv_work.wait_for(lk, std::chrono::microseconds(20));
         }
         for (Job *j : admitting) {
             gepi_status st = engine->admit(*j);
@@ -640,7 +753,7 @@ void gepi_server::run() {
             active.push_back(j);
         }
         admitting.clear();
-        idle = engine->poll(active) == 0 ? 1 : 0;
+        idle = engine->poll(active) == 0;
         bool any = false;
         for (Job *j : active)
             if (j->done) {
@@ -656,7 +769,7 @@ void gepi_server::run() {
             }
         active.erase(std::remove_if(active.begin(), active.end(), [](Job *j) { return j->done; }),
                      active.end());
-        idle = 0;
+        idle = false;
         cv_done.notify_all();
     }
 }
@@ -670,7 +783,7 @@ gepi_status gepi_server_create(int32_t device, size_t hbm_budget_bytes, gepi_ser
     auto srv = std::make_unique<gepi_server>();
     srv->device = device;
     srv->budget = hbm_budget_bytes ? hbm_budget_bytes : (16ull << 30);
-    srv->engine = std::make_unique<Engine>(device, 20.0);
+    srv->engine = std::make_unique<Engine>(device, env_quantum_ms(10.0));
     GEPI_TRY(srv->engine->init());
     gepi_server *p = srv.get();
     p->thread = std::thread([p] { p->run(); });
@@ -687,10 +800,16 @@ gepi_status gepi_server_submit(gepi_server *srv, const gepi_scan_req *req, uint6
         return set_error(GEPI_ERR_ARG, "gepi_server_submit: plane set on another device");
     auto j = std::make_unique<Job>();
     j->rq = rq;
+    j->t_submit = Clock::now();
     j->own_tops.assign((size_t)rq.k, gepi_result{});
     j->tops = j->own_tops.data();
     j->footprint = request_footprint(rq.k);
-    j->t_submit = Clock::now();
+    // method, tables and tile list on the caller's thread, off the loop
+    gepi_status st = srv->engine->prepare(*j);
+    if (st != GEPI_OK) {
+        srv->engine->release(*j);
+        return st;
+    }
     {
         std::lock_guard<std::mutex> lk(srv->mu);
         j->ticket = srv->next_ticket++;
@@ -732,19 +851,24 @@ gepi_status gepi_server_wait(gepi_server *srv, uint64_t ticket, gepi_result *top
 
 void gepi_server_destroy(gepi_server *srv) {
     if (!srv) return;
+    std::deque<Job *> dropped;
     {
         std::lock_guard<std::mutex> lk(srv->mu);
         srv->stop = true;
-        for (Job *j : srv->pending) {
+        dropped.swap(srv->pending);
+    }
+    srv->cv_work.notify_all();
+    if (srv->thread.joinable()) srv->thread.join();
+    {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        for (Job *j : dropped) {
+            srv->engine->release(*j);
             j->status = GEPI_ERR_ARG;
             j->error = "server destroyed before the request was admitted";
             j->t_done = Clock::now();
             j->finished = true;
         }
-        srv->pending.clear();
     }
-    srv->cv_work.notify_all();
-    if (srv->thread.joinable()) srv->thread.join();
     srv->cv_done.notify_all();
     delete srv;
 }

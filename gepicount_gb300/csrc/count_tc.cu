@@ -112,13 +112,17 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *b) {
                  : "memory");
 }
 
+// A waiting thread may sleep in try_wait until the phase completes, for at
+// most kTcSuspendNs; spinning warps would take issue slots from the producers.
+constexpr uint32_t kTcSuspendNs = 20000;
+
 __device__ __forceinline__ bool mbar_try(uint64_t *b, uint32_t parity) {
     uint32_t done;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
         " selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done)
-        : "r"(su32(b)), "r"(parity)
+        : "r"(su32(b)), "r"(parity), "r"(kTcSuspendNs)
         : "memory");
     return done != 0;
 }
@@ -458,16 +462,20 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
             __syncwarp();
             mbar_arrive_warp(&pempty_bar[j]);
+            // expand into registers before waiting for the stage: the wait is
+            // on the MMAs two chunks back, and only the stores follow it
+            uint32_t r[24], o[24];
+#pragma unroll
+            for (int m = 0; m < 3; ++m) {
+                expand_word(pa[m].x, r + 8 * m);
+                expand_word(pa[m].y, r + 8 * m + 4);
+                expand_word(pb[m].x, o + 8 * m);
+                expand_word(pb[m].y, o + 8 * m + 4);
+            }
             if (!mbar_wait_warp(&empty_bar[s], (((uint32_t)idx / kTcStages) & 1) ^ 1, vabort, err, 1))
                 break;
             tc_fence_after();
             {
-                uint32_t r[24];
-#pragma unroll
-                for (int m = 0; m < 3; ++m) {
-                    expand_word(pa[m].x, r + 8 * m);
-                    expand_word(pa[m].y, r + 8 * m + 4);
-                }
                 const uint32_t ta = ta0 + s * kTcAStageCols;
                 tmem_st16(ta, r);
                 tmem_st8(ta + 16, r + 16);
@@ -475,13 +483,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             if (brow) {
                 unsigned char *bst = bst0 + (size_t)s * kTcBStageBytes;
 #pragma unroll
-                for (int m = 0; m < 3; ++m) {
-                    uint32_t o[8];
-                    expand_word(pb[m].x, o);
-                    expand_word(pb[m].y, o + 4);
-                    *reinterpret_cast<uint4 *>(bst + (2 * m) * kTcLbo) = make_uint4(o[0], o[1], o[2], o[3]);
-                    *reinterpret_cast<uint4 *>(bst + (2 * m + 1) * kTcLbo) = make_uint4(o[4], o[5], o[6], o[7]);
-                }
+                for (int m = 0; m < 6; ++m)
+                    *reinterpret_cast<uint4 *>(bst + m * kTcLbo) =
+                        make_uint4(o[4 * m], o[4 * m + 1], o[4 * m + 2], o[4 * m + 3]);
             }
             asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");

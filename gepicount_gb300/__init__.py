@@ -86,6 +86,15 @@ class _ScanReq(ctypes.Structure):
                 ("reserved", ctypes.c_int32)]
 
 
+class _Progress(ctypes.Structure):
+    _fields_ = [("elapsed_s", ctypes.c_double), ("tiles_done", ctypes.c_uint64),
+                ("tiles_total", ctypes.c_uint64), ("snps_done", ctypes.c_int32),
+                ("ntops", ctypes.c_int32), ("tops", ctypes.c_void_p)]
+
+
+_PROGRESS_FN = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.POINTER(_Progress))
+
+
 class _RequestInfo(ctypes.Structure):
     _fields_ = [("queue_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
                 ("device_ms", ctypes.c_double), ("snp_pairs", ctypes.c_uint64),
@@ -137,6 +146,8 @@ def lib():
     L.gepi_scan.argtypes = [P, ctypes.POINTER(_Params), P, i32]
     L.gepi_scan_range.argtypes = [P, ctypes.POINTER(_Params), i32, i32, i32, i32, P, i32]
     L.gepi_pair_counts.argtypes = [P, i32, i32, i32, i32, i32, P]
+    L.gepi_scan_progress.argtypes = [P, ctypes.POINTER(_Params), i32, i32, i32, i32, P, i32,
+                                     _PROGRESS_FN, P, i32, i32]
     L.gepi_process_gpu_1.argtypes = [P, P, i32, i32, P, P, P, ctypes.POINTER(_Params)]
     L.gepi_last_scan_stats.argtypes = [P, ctypes.POINTER(_ScanStats)]
     L.gepi_planes_autotune.argtypes = [P, ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_float),
@@ -162,7 +173,7 @@ def lib():
               "gepi_planes_from_bed", "gepi_planes_from_rows", "gepi_planes_class_sizes",
               "gepi_scan", "gepi_scan_range", "gepi_pair_counts", "gepi_process_gpu_1",
               "gepi_last_scan_stats", "gepi_process_gpu_1_noalloc", "gepi_planes_autotune",
-              "gepi_tensor_peak_tflops", "gepi_scan_batch", "gepi_server_create",
+              "gepi_tensor_peak_tflops", "gepi_scan_batch", "gepi_scan_progress", "gepi_server_create",
               "gepi_server_submit", "gepi_server_wait",
               "gepi_synth_bed", "gepi_synth_write"):
         getattr(L, f).restype = i32
@@ -349,6 +360,37 @@ class Planes:
         tops = np.zeros(k, dtype=RESULT_DTYPE)
         _check(lib().gepi_scan_range(self._h, ctypes.byref(par._c()), a0, na, b0, nb,
                                      _ptr(tops), k))
+        return tops
+
+    def scan_progress(self, k: int, callback, points: int = 0, with_tops: bool = False,
+                      objective: int = ENTROPY, method: int = METHOD_AUTO, a0: int = 0,
+                      na: int | None = None, b0: int = 0, nb: int | None = None) -> np.ndarray:
+        """scan_range with progress: callback(dict) at tile-band ends (see
+        gepi_scan_progress); with_tops adds the exact ranked top-k so far."""
+        n = self.n_snps
+        na = n - a0 if na is None else na
+        nb = n - b0 if nb is None else nb
+        par = Params(topmost=k, ffun=objective, method=method, gpuNum=self.device)
+        tops = np.zeros(k, dtype=RESULT_DTYPE)
+        errors = []
+
+        def tramp(_user, pp):
+            try:
+                p = pp.contents
+                snap = None
+                if p.tops and p.ntops > 0:
+                    buf = (ctypes.c_char * (p.ntops * RESULT_DTYPE.itemsize)).from_address(p.tops)
+                    snap = np.frombuffer(bytes(buf), dtype=RESULT_DTYPE).copy()
+                callback({"elapsed_s": p.elapsed_s, "tiles_done": p.tiles_done,
+                          "tiles_total": p.tiles_total, "snps_done": p.snps_done, "tops": snap})
+            except Exception as e:  # re-raised after the scan
+                errors.append(e)
+
+        fn = _PROGRESS_FN(tramp)
+        _check(lib().gepi_scan_progress(self._h, ctypes.byref(par._c()), a0, na, b0, nb,
+                                        _ptr(tops), k, fn, None, points, 1 if with_tops else 0))
+        if errors:
+            raise errors[0]
         return tops
 
     def pair_counts(self, a0: int, na: int, b0: int, nb: int,

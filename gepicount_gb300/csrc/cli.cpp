@@ -154,22 +154,64 @@ void check_quality(gepi_plink *p, const std::vector<uint64_t> &valid, float maxM
                  maxMissSNPs);
 }
 
-void print_interactions(gepi_plink *p, const std::vector<gepi_result> &tops) {
+void print_interaction(gepi_plink *p, int num, const gepi_result &ir) {
+    const char *ia = "", *ib = "";
+    char aa = '?', ab = '?';
+    int ca = 0, pa = 0, cb = 0, pb = 0;
+    gepi_plink_row_info(p, ir.sA, &ia, &aa, &ca, &pa);
+    gepi_plink_row_info(p, ir.sB, &ib, &ab, &cb, &pb);
+    const int w = ir.n[0], x = ir.n[1], y = ir.n[2], z = ir.n[3];
+    float pv = gepi_fisher_pval(w, y - w, x, z - x);
+    int f = (ir.fun >= 0 && ir.fun < 5) ? ir.fun : 5;
+    std::fprintf(stderr, "%d:\t%d[%s %c %d:%d]\t%s\t%d[%s %c %d:%d]\t%g\t%g\t(%d,%d,%d,%d)\n", num,
+                 ir.sA, ia, aa, ca, pa, kFuncName[f], ir.sB, ib, ab, cb, pb, ir.ent, pv, w, y - w, x,
+                 z - x);
+}
+
+// printInteractions (print_misc.h:57-66): ranks within `context` of every
+// multiple of `stride`.
+void print_interactions(gepi_plink *p, const gepi_result *tops, int n, int stride = 1,
+                        int context = 0) {
     std::fprintf(stderr,
                  "\nRank:\tidxA[id allele chr:pos]\tFunc\tidxB[id allele chr:pos]\tObj\tFPv\t(c00,c01,c10,c11)\n");
-    for (size_t j = 0; j < tops.size(); ++j) {
-        const gepi_result &ir = tops[j];
-        const char *ia = "", *ib = "";
-        char aa = '?', ab = '?';
-        int ca = 0, pa = 0, cb = 0, pb = 0;
-        gepi_plink_row_info(p, ir.sA, &ia, &aa, &ca, &pa);
-        gepi_plink_row_info(p, ir.sB, &ib, &ab, &cb, &pb);
-        const int w = ir.n[0], x = ir.n[1], y = ir.n[2], z = ir.n[3];
-        float pv = gepi_fisher_pval(w, y - w, x, z - x);
-        int f = (ir.fun >= 0 && ir.fun < 5) ? ir.fun : 5;
-        std::fprintf(stderr, "%d:\t%d[%s %c %d:%d]\t%s\t%d[%s %c %d:%d]\t%g\t%g\t(%d,%d,%d,%d)\n",
-                     (int)j, ir.sA, ia, aa, ca, pa, kFuncName[f], ir.sB, ib, ab, cb, pb, ir.ent, pv,
-                     w, y - w, x, z - x);
+    if (stride - 2 * context < 1) context = stride / 2;
+    for (int j = 0; j < n; j += stride)
+        for (int k = j - context < 0 ? 0 : j - context; k < (j + context + 1 > n ? n : j + context + 1); ++k)
+            print_interaction(p, k, tops[k]);
+}
+
+constexpr int kPrintStride = 100000, kPrintContext = 5;  // print_misc.h:30-31
+
+// Progress lines at tile-band ends, as the reference prints them at the
+// diagonal points of its batch grid (kernel1.cu:417-439, "K1") or every 1,024
+// rows of the gold loop (proc_gold_1.h:140-163, "G1"); with -D the ranked
+// results so far follow.
+struct CliProgress {
+    gepi_plink *p = nullptr;
+    int rows = 0;  // allele rows (the reference's numSNPs())
+    bool gold = false, intermediate = false;
+};
+
+void cli_progress(void *user, const gepi_progress *pr) {
+    const CliProgress *c = static_cast<const CliProgress *>(user);
+    if (pr->snps_done <= 0) return;
+    const char *tag = c->gold ? "G1" : "K1";
+    const int done_rows = 2 * pr->snps_done;
+    float nt = (float)c->rows / (float)done_rows;  // fraction so far is 1/nt
+    nt = nt * nt;
+    const float tot = (float)pr->elapsed_s;
+    float rem = (nt - 1.0f) * tot;
+    const float pct = 100.0f / nt;
+    const char *uu = "sec";
+    if (rem > 3600.0f) {
+        rem /= 3600.0f;
+        uu = "hr";
+    }
+    std::fprintf(stderr, "%s: Total time %gsec (%g%%) Remaining: %g%s\n", tag, tot, pct, rem, uu);
+    if (c->intermediate && pr->tops && pr->ntops > 0) {
+        if (c->gold) std::fprintf(stderr, "G1: Sorting... Limit: %g\n", pr->tops[pr->ntops - 1].ent);
+        std::fprintf(stderr, "%s: Last processed: %d,%d\n", tag, done_rows - 1, done_rows - 1);
+        print_interactions(c->p, pr->tops, pr->ntops, kPrintStride, kPrintContext);
     }
 }
 
@@ -219,8 +261,18 @@ int main(int argc, char **argv) {
         gp.topmost = par.topmost;
         gp.objective = par.ffun;
         gp.method = par.method;
-        gp.verbose = par.verbose || par.intermediate;
-        st = gepi_scan(pl, &gp, tops.data(), par.topmost);
+        gp.verbose = par.verbose;
+        if (!par.gold)
+            std::fprintf(stderr, "K1: Objective function is %s\n",
+                         par.ffun == GEPI_FISHER ? "FISHER PV" : "ENTROPY");
+        CliProgress cp;
+        cp.p = p;
+        cp.rows = nR;
+        cp.gold = par.gold;
+        cp.intermediate = par.intermediate;
+        // every band end for the progress lines; with -D at most 32 snapshots
+        st = gepi_scan_progress(pl, &gp, 0, nR / 2, 0, nR / 2, tops.data(), par.topmost, cli_progress,
+                                &cp, par.intermediate ? 32 : 0, par.intermediate ? 1 : 0);
         gepi_planes_destroy(pl);
     }
     double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -229,8 +281,9 @@ int main(int argc, char **argv) {
         gepi_plink_close(p);
         return 1;
     }
-    std::fprintf(stderr, "process_gpu_1: %g \n", secs);
-    print_interactions(p, tops);
+    if (par.gold) std::fprintf(stderr, "G1: Sorting... Limit: %g\n", tops[par.topmost - 1].ent);
+    std::fprintf(stderr, par.gold ? "process_gold_1: %g \n" : "process_gpu_1: %g \n", secs);
+    print_interactions(p, tops.data(), (int)tops.size());
     gepi_plink_close(p);
     std::printf("Cleaned\n");
     return 0;

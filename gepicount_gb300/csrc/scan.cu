@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -287,8 +288,71 @@ bool cand_better(const Cand &a, const Cand &b) {
     return a.rBfun < b.rBfun;
 }
 
+// Top-k of `count` candidates (ranked by the deterministic tie-break) into
+// tops[0, k), zero-filling the rest.
+void rank_candidates(std::vector<Cand> &host, gepi_result *tops, int k) {
+    std::memset(tops, 0, sizeof(gepi_result) * (size_t)k);
+    const size_t keep = std::min<size_t>(host.size(), (size_t)k);
+    std::partial_sort(host.begin(), host.begin() + keep, host.end(), cand_better);
+    for (size_t i = 0; i < keep; ++i) {
+        const Cand &c = host[i];
+        gepi_result &r = tops[i];
+        r.sA = c.rA;
+        r.sB = c.rBfun >> 3;
+        r.fun = (char)(c.rBfun & 7);
+        for (int j = 0; j < 4; ++j) r.n[j] = c.n[j];
+        r.ent = (float)(-value_of_key(c.key));
+    }
+}
+
+// Progress reporting at tile-band ends (gepi_scan_progress).
+constexpr int kTileBand = 8;  // A-tile rows per band of the tile list (build_tiles)
+
+struct Progress {
+    gepi_progress_fn fn = nullptr;
+    void *user = nullptr;
+    int points = 0;
+    bool with_tops = false;
+    const std::vector<int2> *tiles = nullptr;
+    size_t next_end = 0;  // tile index (a band end) at which the next callback fires
+    int next_point = 1;
+    std::chrono::steady_clock::time_point t0;
+
+    bool band_end(size_t t) const {
+        const auto &T = *tiles;
+        return t == 0 || t >= T.size() || T[t].x / kTileBand != T[t - 1].x / kTileBand;
+    }
+    // first band end at or after tile index `thr`
+    size_t end_at_or_after(size_t thr) const {
+        const size_t n = tiles->size();
+        if (thr >= n) return n;
+        if (thr == 0) thr = 1;
+        while (thr < n && !band_end(thr)) ++thr;
+        return thr;
+    }
+    size_t threshold(int point) const {
+        return (size_t)std::ceil((double)point * (double)tiles->size() / (double)points);
+    }
+    void start(const std::vector<int2> &T) {
+        tiles = &T;
+        t0 = std::chrono::steady_clock::now();
+        next_point = 1;
+        next_end = points > 0 ? end_at_or_after(threshold(1)) : end_at_or_after(1);
+    }
+    // after a callback at tile index t: the next firing point
+    void advance(size_t t) {
+        const size_t n = tiles->size();
+        if (points > 0) {
+            while (next_point <= points && end_at_or_after(threshold(next_point)) <= t) ++next_point;
+            next_end = next_point <= points ? end_at_or_after(threshold(next_point)) : n + 1;
+        } else {
+            next_end = t < n ? end_at_or_after(t + 1) : n + 1;
+        }
+    }
+};
+
 gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, int b0, int nb,
-                      gepi_result *tops, int k) {
+                      gepi_result *tops, int k, Progress *prog = nullptr) {
     clear_error();
     if (!pl || !par || !tops || k <= 0) return set_error(GEPI_ERR_ARG, "gepi_scan: bad argument");
     if (par->objective != GEPI_ENTROPY && par->objective != GEPI_FISHER)
@@ -331,6 +395,8 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
         S.diag_snps = hi > lo ? (uint64_t)(hi - lo) : 0;
     }
     GEPI_CUDA(cudaEventRecord(pl->ev[0], pl->stream));
+    if (prog && prog->fn) prog->start(tiles);
+    else prog = nullptr;
 
     ScanState init{};
     init.tau_key = 0ull;
@@ -362,7 +428,9 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
     uint32_t count = 0;
     int retries = 0;
     while (t < ntiles) {
-        const size_t nbt = std::min(batch, ntiles - t);
+        size_t nbt = std::min(batch, ntiles - t);
+        // a snapshot needs exactly the tiles before its band end
+        if (prog && prog->with_tops && t < prog->next_end) nbt = std::min(nbt, prog->next_end - t);
         ctx.cand = pl->d_cand[cur];
         GEPI_CUDA(cudaEventRecord(pl->ev[2], pl->stream));
         if (tc)
@@ -423,6 +491,29 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
             GEPI_CUDA(cudaStreamSynchronize(pl->stream));
             count = pl->h_state->count;
         }
+        if (prog && t >= prog->next_end) {
+            gepi_progress pr{};
+            pr.elapsed_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - prog->t0).count();
+            pr.tiles_done = t;
+            pr.tiles_total = ntiles;
+            // bands before the one in progress are complete
+            const int bands_done = t < ntiles ? tiles[t].x / kTileBand : (na + TA - 1) / TA;
+            pr.snps_done = a0 + std::min(na, bands_done * kTileBand * TA);
+            std::vector<gepi_result> snap;
+            if (prog->with_tops) {
+                std::vector<Cand> host(count);
+                if (count)
+                    GEPI_CUDA(cudaMemcpyAsync(host.data(), pl->d_cand[cur], (size_t)count * sizeof(Cand),
+                                              cudaMemcpyDeviceToHost, pl->stream));
+                GEPI_CUDA(cudaStreamSynchronize(pl->stream));
+                snap.resize((size_t)k);
+                rank_candidates(host, snap.data(), k);
+                pr.tops = snap.data();
+                pr.ntops = k;
+            }
+            prog->fn(prog->user, &pr);
+            prog->advance(t);
+        }
         // Next batch: as many tiles as the remaining budget allows at the
         // append rate just observed (an over-estimate once tau has risen),
         // growing at most 8x per step.
@@ -458,16 +549,17 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
         S.scan_ms = ms;
         S.candidates = count;
     }
-    const size_t keep = std::min<size_t>(host.size(), (size_t)k);
-    std::partial_sort(host.begin(), host.begin() + keep, host.end(), cand_better);
-    for (size_t i = 0; i < keep; ++i) {
-        const Cand &c = host[i];
-        gepi_result &r = tops[i];
-        r.sA = c.rA;
-        r.sB = c.rBfun >> 3;
-        r.fun = (char)(c.rBfun & 7);
-        for (int j = 0; j < 4; ++j) r.n[j] = c.n[j];
-        r.ent = (float)(-value_of_key(c.key));
+    rank_candidates(host, tops, k);
+    if (prog && prog->next_end <= ntiles) {  // the last band end: the scan is complete
+        gepi_progress pr{};
+        pr.elapsed_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - prog->t0).count();
+        pr.tiles_done = pr.tiles_total = ntiles;
+        pr.snps_done = a0 + na;
+        if (prog->with_tops) {
+            pr.tops = tops;
+            pr.ntops = k;
+        }
+        prog->fn(prog->user, &pr);
     }
     return GEPI_OK;
 }
@@ -647,6 +739,17 @@ gepi_status gepi_scan(gepi_planes *pl, const gepi_params *par, gepi_result *tops
 gepi_status gepi_scan_range(gepi_planes *pl, const gepi_params *par, int a0, int na, int b0,
                             int nb, gepi_result *tops, int k) {
     return scan_impl(pl, par, a0, na, b0, nb, tops, k);
+}
+
+gepi_status gepi_scan_progress(gepi_planes *pl, const gepi_params *par, int a0, int na, int b0,
+                               int nb, gepi_result *tops, int k, gepi_progress_fn fn, void *user,
+                               int32_t points, int32_t with_tops) {
+    Progress prog;
+    prog.fn = fn;
+    prog.user = user;
+    prog.points = points;
+    prog.with_tops = with_tops != 0;
+    return scan_impl(pl, par, a0, na, b0, nb, tops, k, &prog);
 }
 
 gepi_status gepi_pair_counts(gepi_planes *pl, int method, int a0, int na, int b0, int nb,

@@ -151,6 +151,33 @@ gepi_status gepi_scan(gepi_planes *pl, const gepi_params *par, gepi_result *tops
 gepi_status gepi_scan_range(gepi_planes *pl, const gepi_params *par, int a0, int na,
                             int b0, int nb, gepi_result *tops, int k);
 
+/* Progress of a scan, reported at tile-band ends.  Tiles are walked in bands of
+ * 8 A-tile rows (320 SNPs for the tensor-core kernel, 256 for the popcount
+ * kernel); when a callback fires, every band before the current one is done,
+ * so for a whole-genome scan all pairs (s, t), t <= s < snps_done, are tested.
+ * Replaces the reference's progress block at diagonal points
+ * (src/kernels/kernel1.cu:417-439; gold path src/proc_gold_1.h:140-163). */
+typedef struct gepi_progress {
+    double elapsed_s;          /* wall time since the scan started                       */
+    uint64_t tiles_done;       /* tiles of the scan's list processed                      */
+    uint64_t tiles_total;
+    int32_t snps_done;         /* A-range SNPs [a0, snps_done) complete                   */
+    int32_t ntops;             /* entries in tops: the scan's k when asked for, else 0     */
+    const gepi_result *tops;   /* ranked top-k of every test done so far, or NULL;
+                                  valid during the callback only                          */
+} gepi_progress;
+typedef void (*gepi_progress_fn)(void *user, const gepi_progress *p);
+
+/* gepi_scan_range with a progress callback.  points > 0: at most that many
+ * callbacks, at the first band end past each 1/points of the tile list;
+ * points <= 0: at every band end.  with_tops != 0: each callback also gets the
+ * exact ranked top-k of the tests done so far (the batches are cut at the
+ * callback's band end for it, and every snapshot reads the candidate buffer
+ * back).  Results are identical to gepi_scan_range's. */
+gepi_status gepi_scan_progress(gepi_planes *pl, const gepi_params *par, int a0, int na, int b0,
+                               int nb, gepi_result *tops, int k, gepi_progress_fn fn, void *user,
+                               int32_t points, int32_t with_tops);
+
 /* Per-SNP-pair Gram counts, for verification: for every s in [a0,a0+na),
  * t in [b0,b0+nb) writes 18 uint32 at out[((s-a0)*nb + (t-b0))*18]:
  * class c (0,1) x planes (p,q) in {A-carrier row, a-carrier row, valid}^2,

@@ -17,6 +17,7 @@ import argparse
 import hashlib
 import json
 import os
+import re
 import subprocess
 import sys
 import tempfile
@@ -51,10 +52,20 @@ def sha(path: str) -> str:
     return hashlib.sha256(open(path, "rb").read()).hexdigest()
 
 
+_QC = re.compile(r"^(Checking data in |Sample \d+:\t|SNP \d+:\t|\d+ Samples checked|"
+                 r"\d+ SNPs checked|-?\d+ -?\d+ \S+$)")
+
+
 def run_gold(gold: str, base: str, k: int):
+    """Ranked rows, stdout, the QC report lines (PlinkReader.h:237-335) and the final
+    "G1: Sorting... Limit:" line.  One OpenMP thread: the QC report's periodic lines come
+    from thread 0's chunk only, so a single chunk makes the report complete and ordered."""
     r = subprocess.run([gold, "-g", "-i", base, "-N", str(k)], capture_output=True, text=True,
-                       check=True)
-    return parse_ranked(r.stderr), r.stdout
+                       check=True, env=dict(os.environ, OMP_NUM_THREADS="1"))
+    lines = r.stderr.splitlines()
+    qc = [ln for ln in lines if _QC.match(ln)]
+    limit = [ln for ln in lines if ln.startswith("G1: Sorting... Limit:")]
+    return parse_ranked(r.stderr), r.stdout, qc, limit[-1:]
 
 
 def main():
@@ -73,19 +84,19 @@ def main():
             spec = g.SynthSpec(**kw)
             base = os.path.join(td, name)
             g.synth_write(spec, base)
-            rows, stdout = run_gold(gold, base, k)
+            rows, stdout, qc, limit = run_gold(gold, base, k)
             doc = dict(case=name, kind="synthetic", spec=kw, k=k,
                        sha256={e: sha(base + "." + e) for e in ("bed", "bim", "fam")},
-                       stdout=stdout.splitlines(), rows=rows)
+                       stdout=stdout.splitlines(), rows=rows, qc=qc, g1_limit=limit)
             with open(os.path.join(HERE, f"gold_{name}.json"), "w") as f:
                 json.dump(doc, f, indent=0)
             print(name, len(rows))
     for name, (rel, k) in REF_CASES.items():
         base = os.path.join(args.ref, rel)
-        rows, stdout = run_gold(gold, base, k)
+        rows, stdout, qc, limit = run_gold(gold, base, k)
         doc = dict(case=name, kind="reference-data", path=rel, k=k,
                    sha256={e: sha(base + "." + e) for e in ("bed", "bim", "fam")},
-                   stdout=stdout.splitlines(), rows=rows)
+                   stdout=stdout.splitlines(), rows=rows, qc=qc, g1_limit=limit)
         with open(os.path.join(HERE, f"gold_{name}.json"), "w") as f:
             json.dump(doc, f, indent=0)
         print(name, len(rows))

@@ -91,7 +91,9 @@ constexpr uint32_t kTcIdesc = (1u << 7) | (1u << 10)           // A, B = E2M1
                               | ((uint32_t)(128 >> 4) << 24);  // M
 constexpr size_t kTcPOff = kTcStages * (size_t)kTcBStageBytes;               // packed ring
 constexpr size_t kTcXOff = kTcPOff + kTcPStages * (size_t)kTcPStageBytes;    // exchange rows
-constexpr size_t kTcSmem = kTcXOff + (size_t)kTcEpiWarps * 32 * kTcXStride * 4;
+constexpr int kTcQueueCap = 3 * 32;                // pairs a warp can queue per 8 B SNPs
+constexpr size_t kTcQOff = kTcXOff + (size_t)kTcEpiWarps * 32 * kTcXStride * 4;  // pair queues
+constexpr size_t kTcSmem = kTcQOff + (size_t)kTcEpiWarps * kTcQueueCap * 4;
 static_assert(kTcSfCol + 32 <= kTcCols, "tensor memory budget");
 constexpr long long kTcWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
 static_assert(kTcPStageBytes % 128 == 0 && kTcPABytes % 128 == 0 && kTcPOff % 128 == 0,
@@ -271,49 +273,83 @@ __device__ __forceinline__ void mbar_drain(uint64_t *b, uint32_t parity) {
 // score_tests; the tests that pass are refined one by one out of line, which
 // keeps the epilogue's code small (its warps share the instruction cache with
 // the producers).
-template <int OBJ>
-__device__ __forceinline__ uint32_t tc_stage1(const ScanCtx &ctx, const float *G0, const float *G1,
-                                              bool diag, float theta, float lp_thr) {
-    const float y = G0[8], z = G1[8];
-    const float m = y + z, yz = y * z;
-    uint32_t mask = 0;
+// Row-pair bound of an SNP pair for the entropy objective: bit 2i+j set when
+// row pair (2s+i, 2t+j) may hold a test that passes stage 1.  Every function
+// tested for a row pair is a function of the cell (bit of row 2s+i, bit of row
+// 2t+j), so its phi^2 is at most the class x cell table's chi^2 / m =
+// sum_k D_k^2 / (c_k y z m), D_k = a_k z - b_k y over the four cells (data
+// processing for the chi^2 divergence); below theta none of the row pair's
+// five tests passes.  D_k carries the product rounding margin, the sum a 2^-18
+// margin for the approximate reciprocals.  On the diagonal row 2t+j must be
+// <= row 2s+i, which drops (i, j) = (0, 1), bit 1.
+__device__ __forceinline__ uint32_t tc_rowpairs(const float *G0, const float *G1, bool diag,
+                                                float theta) {
+    const float y = G0[8], z = G1[8], yzm = y * z * (y + z);
+    uint32_t ok = 0;
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
-            if (diag && j > i) continue;  // row 2t+j must be <= row 2s+i
-            float on0[5], on1[5];
-            {
-                const float n11 = G0[i * 3 + j], r = G0[i * 3 + 2], c = G0[6 + j];
-                const float n10 = r - n11, n01 = c - n11;
-                on0[0] = n11; on0[1] = n01; on0[2] = n10; on0[3] = y - r - c + n11; on0[4] = n10 + n01;
-            }
-            {
-                const float n11 = G1[i * 3 + j], r = G1[i * 3 + 2], c = G1[6 + j];
-                const float n10 = r - n11, n01 = c - n11;
-                on1[0] = n11; on1[1] = n01; on1[2] = n10; on1[3] = z - r - c + n11; on1[4] = n10 + n01;
-            }
+            const float a11 = G0[i * 3 + j], ar = G0[i * 3 + 2], ac = G0[6 + j];
+            const float b11 = G1[i * 3 + j], br = G1[i * 3 + 2], bc = G1[6 + j];
+            const float a[4] = {a11, ar - a11, ac - a11, y - ar - ac + a11};
+            const float b[4] = {b11, br - b11, bc - b11, z - br - bc + b11};
+            float S = 0.f;
 #pragma unroll
-            for (int f = 0; f < 5; ++f) {
-                const float w = on0[f], x = on1[f];
-                bool pass;
-                if (OBJ == 0) {
-                    const float xx = w + x;
-                    const float Q = xx * (m - xx) * yz;
-                    const float wz = w * z, xy = x * y;
-                    const float D = fabsf(wz - xy) + (wz + xy) * 2.384185791015625e-07f;  // 2^-22
-                    pass = D * D >= theta * Q;
-                } else {
-                    const int iw = (int)w, ix = (int)x, iy = (int)y, iz = (int)z;
-                    const float *L = ctx.lf32;
-                    const float lp = __ldg(L + (iw + ix)) + __ldg(L + (iy + iz - iw - ix)) +
-                                     __ldg(L + iy) + __ldg(L + iz) - __ldg(L + (iy + iz)) -
-                                     __ldg(L + iw) - __ldg(L + (iy - iw)) - __ldg(L + ix) -
-                                     __ldg(L + (iz - ix));
-                    pass = lp <= lp_thr;
-                }
-                mask |= (uint32_t)pass << (5 * (2 * i + j) + f);
+            for (int k = 0; k < 4; ++k) {
+                const float az = a[k] * z, by = b[k] * y;
+                const float D = fabsf(az - by) + (az + by) * 2.384185791015625e-07f;  // 2^-22
+                S = fmaf(D * D, __fdividef(1.f, fmaxf(a[k] + b[k], 1.f)), S);
             }
+            ok |= (uint32_t)(S * 1.0000038146972656f >= theta * yzm) << (2 * i + j);  // 1 + 2^-18
+        }
+    }
+    return ok & (diag ? 0xDu : 0xFu);
+}
+
+// Stage-1 bounds of the five tests of every row pair in `rp` (bit 2i+j) as a
+// bit mask, bit 5 * (2i + j) + f.  Same bounds as score_tests; the tests that
+// pass are refined one by one out of line.
+template <int OBJ>
+__device__ __forceinline__ uint32_t tc_stage1(const ScanCtx &ctx, const float *G0, const float *G1,
+                                              uint32_t rp, float theta, float lp_thr) {
+    const float y = G0[8], z = G1[8];
+    const float m = y + z, yz = y * z;
+    uint32_t mask = 0;
+    for (int r = 0; r < 4; ++r) {
+        if (!((rp >> r) & 1u)) continue;
+        const int i = r >> 1, j = r & 1;
+        float on0[5], on1[5];
+        {
+            const float n11 = G0[i * 3 + j], rr = G0[i * 3 + 2], c = G0[6 + j];
+            const float n10 = rr - n11, n01 = c - n11;
+            on0[0] = n11; on0[1] = n01; on0[2] = n10; on0[3] = y - rr - c + n11; on0[4] = n10 + n01;
+        }
+        {
+            const float n11 = G1[i * 3 + j], rr = G1[i * 3 + 2], c = G1[6 + j];
+            const float n10 = rr - n11, n01 = c - n11;
+            on1[0] = n11; on1[1] = n01; on1[2] = n10; on1[3] = z - rr - c + n11; on1[4] = n10 + n01;
+        }
+#pragma unroll
+        for (int f = 0; f < 5; ++f) {
+            const float w = on0[f], x = on1[f];
+            bool pass;
+            if (OBJ == 0) {
+                const float xx = w + x;
+                const float Q = xx * (m - xx) * yz;
+                const float wz = w * z, xy = x * y;
+                const float D = fabsf(wz - xy) + (wz + xy) * 2.384185791015625e-07f;  // 2^-22
+                pass = D * D >= theta * Q;
+            } else {
+                const int iw = (int)w, ix = (int)x, iy = (int)y, iz = (int)z;
+                const float *L = ctx.lf32;
+                const float lp = __ldg(L + (iw + ix)) + __ldg(L + (iy + iz - iw - ix)) +
+                                 __ldg(L + iy) + __ldg(L + iz) - __ldg(L + (iy + iz)) -
+                                 __ldg(L + iw) - __ldg(L + (iy - iw)) - __ldg(L + ix) -
+                                 __ldg(L + (iz - ix));
+                pass = lp <= lp_thr;
+            }
+            mask |= (uint32_t)pass << (5 * r + f);
         }
     }
     return mask;
@@ -572,6 +608,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const int eh = warp >= 12;  // which half of the B SNPs
         const int ew = q + 4 * eh;  // 0..7
         float *xb = reinterpret_cast<float *>(tc_smem + kTcXOff) + (size_t)ew * 32 * kTcXStride;
+        uint32_t *qu = reinterpret_cast<uint32_t *>(tc_smem + kTcQOff) + (size_t)ew * kTcQueueCap;
         const int i = lane / 3, p = lane % 3;
         const float theta = DUMP ? 0.f : ctx.st->theta;
         const float lp_thr = DUMP ? 0.f : ctx.st->lp_thr;
@@ -619,32 +656,57 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     row[24 + k] = __uint_as_float(v1[k]);
                 }
                 __syncwarp();
-                if (lane < 30 && sA < a1) {
-                    for (int jl = p; jl < 8; jl += 3) {
-                        const int sBt = sB0 + 8 * g8 + jl;
-                        if (sBt >= b1 || sBt > sA) continue;
-                        float G[18];
+                // Phase 1: every lane bounds its SNP pairs (i, jl), jl = p + 3r, and
+                // queues those with a row pair that may pass.  Phase 2: the warp
+                // runs stage 1 and the refinement over the queue, densely.
+                int qn = 0;
 #pragma unroll
-                        for (int pp = 0; pp < 3; ++pp)
+                for (int r = 0; r < 3; ++r) {
+                    const int jl = p + 3 * r;
+                    const int sBt = sB0 + 8 * g8 + jl;
+                    uint32_t rp = 0;
+                    if (lane < 30 && sA < a1 && jl < 8 && sBt < b1 && sBt <= sA) {
+                        if (OBJ == 0) {
+                            float G[18];
 #pragma unroll
-                            for (int qq = 0; qq < 3; ++qq) {
-                                G[pp * 3 + qq] = xb[(3 * i + pp) * kTcXStride + 3 * jl + qq];
-                                G[9 + pp * 3 + qq] = xb[(3 * i + pp) * kTcXStride + 24 + 3 * jl + qq];
-                            }
-                        uint32_t mask = tc_stage1<OBJ>(ctx, G, G + 9, sA == sBt, theta, lp_thr);
-                        const int y = (int)G[8], z = (int)G[17];
-                        while (mask) {
-                            const int bit = __ffs(mask) - 1;
-                            mask &= mask - 1;
-                            const int rp = bit / 5, f = bit - 5 * rp, ri = rp >> 1, rj = rp & 1;
-                            const float *g0 = xb + (3 * i) * kTcXStride + 3 * jl;
-                            const int w = fun_count((int)g0[ri * kTcXStride + rj], (int)g0[ri * kTcXStride + 2],
-                                                    (int)g0[2 * kTcXStride + rj], y, f);
-                            const int x = fun_count((int)g0[ri * kTcXStride + 24 + rj],
-                                                    (int)g0[ri * kTcXStride + 24 + 2],
-                                                    (int)g0[2 * kTcXStride + 24 + rj], z, f);
-                            tc_refine<OBJ>(ctx, 2 * sA + ri, 2 * sBt + rj, f, w, x, y, z);
+                            for (int pp = 0; pp < 3; ++pp)
+#pragma unroll
+                                for (int qq = 0; qq < 3; ++qq) {
+                                    G[pp * 3 + qq] = xb[(3 * i + pp) * kTcXStride + 3 * jl + qq];
+                                    G[9 + pp * 3 + qq] = xb[(3 * i + pp) * kTcXStride + 24 + 3 * jl + qq];
+                                }
+                            rp = tc_rowpairs(G, G + 9, sA == sBt, theta);
+                        } else {
+                            rp = sA == sBt ? 0xDu : 0xFu;
                         }
+                    }
+                    const uint32_t bal = __ballot_sync(0xffffffffu, rp != 0);
+                    if (rp) qu[qn + __popc(bal & ((1u << lane) - 1u))] = ((uint32_t)lane << 8) | ((uint32_t)jl << 4) | rp;
+                    qn += __popc(bal);
+                }
+                __syncwarp();
+                for (int e = lane; e < qn; e += 32) {
+                    const uint32_t ent = qu[e];
+                    const int il = (int)(ent >> 8) / 3, jl = (int)(ent >> 4) & 15;
+                    const int sAe = a0 + tl.x * kTcASnps + 10 * q + il, sBt = sB0 + 8 * g8 + jl;
+                    float G[18];
+#pragma unroll
+                    for (int pp = 0; pp < 3; ++pp)
+#pragma unroll
+                        for (int qq = 0; qq < 3; ++qq) {
+                            G[pp * 3 + qq] = xb[(3 * il + pp) * kTcXStride + 3 * jl + qq];
+                            G[9 + pp * 3 + qq] = xb[(3 * il + pp) * kTcXStride + 24 + 3 * jl + qq];
+                        }
+                    uint32_t mask = tc_stage1<OBJ>(ctx, G, G + 9, ent & 15u, theta, lp_thr);
+                    const int y = (int)G[8], z = (int)G[17];
+                    while (mask) {
+                        const int bit = __ffs(mask) - 1;
+                        mask &= mask - 1;
+                        const int rp = bit / 5, f = bit - 5 * rp, ri = rp >> 1, rj = rp & 1;
+                        const int w = fun_count((int)G[ri * 3 + rj], (int)G[ri * 3 + 2], (int)G[6 + rj], y, f);
+                        const int x = fun_count((int)G[9 + ri * 3 + rj], (int)G[9 + ri * 3 + 2],
+                                                (int)G[15 + rj], z, f);
+                        tc_refine<OBJ>(ctx, 2 * sAe + ri, 2 * sBt + rj, f, w, x, y, z);
                     }
                 }
                 __syncwarp();

@@ -321,11 +321,10 @@ gepi_status Engine::admit(Job &j) {
     *b->h_state = init;  // the previous user's copies have drained (release)
     GEPI_CUDA(cudaMemcpyAsync(b->state, b->h_state, sizeof(ScanState), cudaMemcpyHostToDevice, j.s));
 
-    // as in the direct scan: a first batch of about cap/4 tests (Fisher: 64 Ki)
+    // as in the direct scan: the same select budget and first batch
     const double tests_per_tile = 20.0 * j.TA * j.TB;
-    const double pilot = j.rq.objective == GEPI_ENTROPY ? b->cap / 4.0 : 1.0 * (1 << 16);
-    j.batch = (size_t)std::max(1.0, std::floor(pilot / tests_per_tile));
-    j.budget = b->cap / 2;
+    j.budget = select_budget(b->cap, j.rq.k);
+    j.batch = (size_t)std::max(1.0, std::floor(pilot_tests(j.rq.objective, j.budget) / tests_per_tile));
     j.lp_margin = 2e-6f * j.rq.pl->lf_max + 1e-3f;
     j.cur = 0;
     j.next = 0;

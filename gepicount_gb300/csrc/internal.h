@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -36,6 +37,19 @@ cudaError_t run_select_compact(Cand *in, Cand *out, ScanState *st, void *sel, ui
 size_t sel_state_bytes();
 int popc_tile_snps();
 constexpr int kSelectLaunches = 20;  // init + 8 x (histogram, pick) + apply + compact + count
+
+// Candidates a scan lets accumulate before a device select raises its
+// threshold: 64 k (at least 64 Ki), at most half the buffer.  Raising the
+// threshold early keeps the bound passes -- and the exact scoring they cost --
+// for the few tests near the final top-k; the results do not depend on it.
+inline uint32_t select_budget(uint32_t cap, int k) {
+    const uint64_t want = std::max<uint64_t>(65536u, 64ull * (uint64_t)k);
+    return (uint32_t)std::min<uint64_t>(cap / 2, want);
+}
+// Tests in a scan's first batch: half the select budget (Fisher: 64 Ki).
+inline double pilot_tests(int objective, uint32_t budget) {
+    return objective == GEPI_ENTROPY ? budget / 2.0 : 1.0 * (1 << 16);
+}
 
 struct DeviceGuard {
     int prev = -1;

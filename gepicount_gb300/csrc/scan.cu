@@ -421,9 +421,9 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
 
     const size_t ntiles = tiles.size();
     const double tests_per_tile = 20.0 * TA * TB;
-    const uint32_t budget = pl->cap / 2;
-    const double pilot_tests = par->objective == GEPI_ENTROPY ? pl->cap / 4.0 : 1.0 * (1 << 16);
-    size_t batch = (size_t)std::max(1.0, std::floor(pilot_tests / tests_per_tile));
+    const uint32_t budget = select_budget(pl->cap, k);
+    size_t batch =
+        (size_t)std::max(1.0, std::floor(pilot_tests(par->objective, budget) / tests_per_tile));
     size_t t = 0;
     uint32_t count = 0;
     int retries = 0;

@@ -39,11 +39,11 @@ int popc_tile_snps();
 constexpr int kSelectLaunches = 20;  // init + 8 x (histogram, pick) + apply + compact + count
 
 // Candidates a scan lets accumulate before a device select raises its
-// threshold: 64 k (at least 64 Ki), at most half the buffer.  Raising the
+// threshold: 16 k (at least 64 Ki), at most half the buffer.  Raising the
 // threshold early keeps the bound passes -- and the exact scoring they cost --
 // for the few tests near the final top-k; the results do not depend on it.
 inline uint32_t select_budget(uint32_t cap, int k) {
-    const uint64_t want = std::max<uint64_t>(65536u, 64ull * (uint64_t)k);
+    const uint64_t want = std::max<uint64_t>(65536u, 16ull * (uint64_t)k);
     return (uint32_t)std::min<uint64_t>(cap / 2, want);
 }
 // Tests in a scan's first batch: half the select budget (Fisher: 64 Ki).

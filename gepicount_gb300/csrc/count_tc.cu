@@ -563,10 +563,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     } else if (warp == kTcMmaWarp) {
         // ---------------- MMA issuer ----------------
         if (lane == 0) {
-            uint64_t bdesc[kTcStages];
-#pragma unroll
-            for (int st = 0; st < kTcStages; ++st)
-                bdesc[st] = tc_bdesc(su32(tc_smem + (size_t)st * kTcBStageBytes));
+            // stage s's descriptor: the start-address field (address >> 4) moves by
+            // s * kTcBStageBytes >> 4 (no per-stage array: a runtime-indexed one
+            // would live in local memory, one load per chunk on the issue path)
+            const uint64_t bdesc0 = tc_bdesc(su32(tc_smem));
             const uint32_t sf = tbase + kTcSfCol;
             uint32_t gc = 0, lt = 0;
             bool ok = true;
@@ -581,7 +581,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     const uint32_t d = dbuf + (c < cm.n0 ? 0u : (uint32_t)kTcN);
                     const uint32_t acc0 = (c == 0 || c == cm.n0) ? 0u : 1u;
                     const uint32_t a = tbase + kTcACol + s * kTcAStageCols;
-                    const uint64_t bd = bdesc[s];
+                    const uint64_t bd = bdesc0 + (uint64_t)((s * (uint32_t)kTcBStageBytes) >> 4);
                     if (!mbar_wait(&full_bar[s], (gc / kTcStages) & 1, vabort, err, 3)) {
                         ok = false;
                         break;

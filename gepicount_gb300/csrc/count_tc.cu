@@ -41,9 +41,11 @@
 //              alternate between chunks
 //   epilogue   warps 4-7 and 12-15 (two per lane quarter, each half of the B
 //              SNPs): drain an accumulator buffer per tile (tcgen05.ld),
-//              exchange the three A planes of a SNP through shared memory and
-//              score every SNP pair (stage-1 bit mask, survivors refined
-//              out of line)
+//              exchange the three A planes of a SNP through shared memory,
+//              bound every SNP pair per row pair (one chi^2 bound covers a
+//              row pair's five tests) and queue the few that may pass; the
+//              warp then runs the per-test bounds and the out-of-line
+//              refinement over its queue densely
 //   MMA        warp 16, one thread: up to 6 x tcgen05.mma per chunk, commits
 //   TMA        warp 17, one thread: two bulk copies per chunk
 // mbarriers: pfull[j] (copy transaction bytes) / pempty[j] (8 producer warps)

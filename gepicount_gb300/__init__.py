@@ -26,7 +26,7 @@ import numpy as np
 __all__ = [
     "GepiError", "RESULT_DTYPE", "FUNC_NAMES", "Params", "BinPlinkReader", "Planes",
     "process_gpu_1", "process_gpu_1_noalloc", "fisher_pval", "fisher_log10p", "SynthSpec", "synth_bed", "synth_write",
-    "library_path", "lib", "ScanRequest", "scan_batch", "Server",
+    "library_path", "lib", "ScanRequest", "scan_batch", "Server", "shard_range", "merge_results",
 ]
 
 _PKG = os.path.dirname(os.path.abspath(__file__))
@@ -154,6 +154,9 @@ def lib():
                                        ctypes.POINTER(ctypes.c_float)]
     L.gepi_tensor_peak_tflops.argtypes = [i32, ctypes.POINTER(ctypes.c_double)]
     L.gepi_process_gpu_1_noalloc.argtypes = [P, P, i32, i32, P, P, P, ctypes.POINTER(_Params)]
+    L.gepi_shard_range.argtypes = [i32, i32, i32] + [ctypes.POINTER(ctypes.c_int32)] * 4
+    L.gepi_merge_results.argtypes = [i32, i32, ctypes.POINTER(P), ctypes.POINTER(ctypes.c_int32),
+                                     i32, P, i32]
     L.gepi_scan_batch.argtypes = [ctypes.POINTER(_ScanReq), i32, ctypes.POINTER(P),
                                   ctypes.POINTER(_ScanStats)]
     L.gepi_server_create.argtypes = [i32, sz, PP]
@@ -173,7 +176,7 @@ def lib():
               "gepi_planes_from_bed", "gepi_planes_from_rows", "gepi_planes_class_sizes",
               "gepi_scan", "gepi_scan_range", "gepi_pair_counts", "gepi_process_gpu_1",
               "gepi_last_scan_stats", "gepi_process_gpu_1_noalloc", "gepi_planes_autotune",
-              "gepi_tensor_peak_tflops", "gepi_scan_batch", "gepi_scan_progress", "gepi_server_create",
+              "gepi_tensor_peak_tflops", "gepi_scan_batch", "gepi_scan_progress", "gepi_shard_range", "gepi_merge_results", "gepi_server_create",
               "gepi_server_submit", "gepi_server_wait",
               "gepi_synth_bed", "gepi_synth_write"):
         getattr(L, f).restype = i32
@@ -457,6 +460,28 @@ def process_gpu_1_noalloc(pr: BinPlinkReader, tops: np.ndarray, par: Params) -> 
     _check(lib().gepi_process_gpu_1_noalloc(_ptr(bits), _ptr(valid), bits.shape[0],
                                             bits.shape[1], _ptr(m1), _ptr(m2), _ptr(tops),
                                             ctypes.byref(par._c())))
+
+
+# ---- sharded scans ----------------------------------------------------------------
+def shard_range(n_snps: int, n_shards: int, shard: int):
+    """(a0, na, b0, nb) of shard `shard` of the whole-genome triangle: a
+    scan_range over it covers a disjoint, about equal share of the pairs."""
+    v = [ctypes.c_int32() for _ in range(4)]
+    _check(lib().gepi_shard_range(n_snps, n_shards, shard, *[ctypes.byref(x) for x in v]))
+    return tuple(x.value for x in v)
+
+
+def merge_results(lists, k: int, n_samples: int, objective: int = ENTROPY) -> np.ndarray:
+    """k-way merge of ranked RESULT_DTYPE lists from disjoint scans of one
+    cohort (gepi_merge_results): the k best, ranked as one scan ranks them.
+    Host only: no device is needed."""
+    lists = [np.ascontiguousarray(x, dtype=RESULT_DTYPE) for x in lists]
+    n = len(lists)
+    ptrs = (ctypes.c_void_p * max(1, n))(*[_ptr(x) if x.size else None for x in lists])
+    lens = (ctypes.c_int32 * max(1, n))(*[x.size for x in lists])
+    out = np.zeros(k, dtype=RESULT_DTYPE)
+    _check(lib().gepi_merge_results(n_samples, objective, ptrs, lens, n, _ptr(out), k))
+    return out
 
 
 # ---- many scans at once --------------------------------------------------------

@@ -16,6 +16,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -739,6 +741,81 @@ gepi_status gepi_scan(gepi_planes *pl, const gepi_params *par, gepi_result *tops
 gepi_status gepi_scan_range(gepi_planes *pl, const gepi_params *par, int a0, int na, int b0,
                             int nb, gepi_result *tops, int k) {
     return scan_impl(pl, par, a0, na, b0, nb, tops, k);
+}
+
+gepi_status gepi_shard_range(int32_t n_snps, int32_t n_shards, int32_t shard, int32_t *a0,
+                             int32_t *na, int32_t *b0, int32_t *nb) {
+    clear_error();
+    if (n_snps < 0 || n_shards <= 0 || shard < 0 || shard >= n_shards || !a0 || !na || !b0 || !nb)
+        return set_error(GEPI_ERR_ARG, "gepi_shard_range: bad argument");
+    // rows [r_s, r_{s+1}) with r_s = n sqrt(s / S): pairs per shard ~ r_{s+1}^2 - r_s^2, even
+    auto bound = [&](int s_) {
+        if (s_ >= n_shards) return n_snps;
+        return (int32_t)std::llround((double)n_snps * std::sqrt((double)s_ / (double)n_shards));
+    };
+    const int32_t r0 = bound(shard), r1 = std::max(r0, bound(shard + 1));
+    *a0 = r0;
+    *na = r1 - r0;
+    *b0 = 0;
+    *nb = r1;
+    return GEPI_OK;
+}
+
+gepi_status gepi_merge_results(int32_t n_samples, int32_t objective,
+                               const gepi_result *const *lists, const int32_t *lens,
+                               int32_t n_lists, gepi_result *out, int32_t k) {
+    clear_error();
+    if (n_samples <= 0 || !lists || !lens || n_lists < 0 || !out || k <= 0)
+        return set_error(GEPI_ERR_ARG, "gepi_merge_results: bad argument");
+    if (objective != GEPI_ENTROPY && objective != GEPI_FISHER)
+        return set_error(GEPI_ERR_ARG, "gepi_merge_results: unknown objective");
+    // the scan's fixed-point table for this sample count, built once
+    static std::mutex mu;
+    static std::map<int32_t, std::pair<int, std::vector<uint64_t>>> tables;
+    const std::pair<int, std::vector<uint64_t>> *tab = nullptr;
+    if (objective == GEPI_ENTROPY) {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = tables.find(n_samples);
+        if (it == tables.end()) {
+            std::pair<int, std::vector<uint64_t>> t;
+            t.first = tfix_bits(n_samples);
+            build_tfix(n_samples, t.first, t.second);
+            it = tables.emplace(n_samples, std::move(t)).first;
+        }
+        tab = &it->second;
+    }
+    std::vector<Cand> all;
+    for (int32_t l = 0; l < n_lists; ++l) {
+        if (lens[l] < 0 || (lens[l] > 0 && !lists[l]))
+            return set_error(GEPI_ERR_ARG, "gepi_merge_results: bad list");
+        for (int32_t i = 0; i < lens[l]; ++i) {
+            const gepi_result &r = lists[l][i];
+            const int w = r.n[0], x = r.n[1], y = r.n[2], z = r.n[3];
+            // zero-filled slots and tests without association are not ranked
+            if ((long long)w * z == (long long)x * y) continue;
+            if (w < 0 || x < 0 || w > y || x > z || (int64_t)y + z > n_samples)
+                return set_error(GEPI_ERR_ARG, "gepi_merge_results: counts inconsistent with n_samples");
+            double value;
+            if (objective == GEPI_ENTROPY) {
+                // the exact key of the scan: the same integer sum, scaling and division
+                const std::vector<uint64_t> &T = tab->second;
+                const int m = y + z, xx = w + x;
+                const uint64_t num = T[m] + T[w] + T[y - w] + T[x] + T[z - x] - T[xx] - T[m - xx] -
+                                     T[y] - T[z];
+                value = std::scalbn((double)(long long)num, -tab->first) / (double)m;
+            } else {
+                value = -fisher_lnp_host(w, y - w, x, z - x) * 0.43429448190325182765;
+            }
+            Cand c;
+            c.key = key_of(value);
+            c.rA = r.sA;
+            c.rBfun = r.sB * 8 + (int)r.fun;
+            for (int q = 0; q < 4; ++q) c.n[q] = r.n[q];
+            all.push_back(c);
+        }
+    }
+    rank_candidates(all, out, k);
+    return GEPI_OK;
 }
 
 gepi_status gepi_scan_progress(gepi_planes *pl, const gepi_params *par, int a0, int na, int b0,

@@ -178,6 +178,26 @@ gepi_status gepi_scan_progress(gepi_planes *pl, const gepi_params *par, int a0, 
                                int nb, gepi_result *tops, int k, gepi_progress_fn fn, void *user,
                                int32_t points, int32_t with_tops);
 
+/* ---- sharding a scan across GPUs or processes --------------------------------- */
+/* Shard `shard` of `n_shards` of the whole-genome triangle of `n_snps` SNPs, as
+ * the gepi_scan_range arguments: A rows [r_s, r_{s+1}) against B rows
+ * [0, r_{s+1}), r_s = round(n_snps * sqrt(s / n_shards)), so the shards are
+ * disjoint, cover every pair once and hold about equal numbers of pairs.  Tile
+ * ranges are independent, so a sharded scan needs no exchange but the merge
+ * below.  No counterpart in the reference. */
+gepi_status gepi_shard_range(int32_t n_snps, int32_t n_shards, int32_t shard, int32_t *a0,
+                             int32_t *na, int32_t *b0, int32_t *nb);
+
+/* k-way merge of ranked result lists from disjoint scans of one cohort of
+ * `n_samples` samples (e.g. the shards above), on the host: each result is
+ * re-keyed from its counts exactly as the scan keys it and the k best are
+ * written ranked as one scan ranks them, zero-filling the rest.  For entropy
+ * the merged list equals the whole-triangle scan bit for bit; for Fisher it
+ * agrees within the objective's 1e-9 relative tolerance. */
+gepi_status gepi_merge_results(int32_t n_samples, int32_t objective,
+                               const gepi_result *const *lists, const int32_t *lens,
+                               int32_t n_lists, gepi_result *out, int32_t k);
+
 /* Per-SNP-pair Gram counts, for verification: for every s in [a0,a0+na),
  * t in [b0,b0+nb) writes 18 uint32 at out[((s-a0)*nb + (t-b0))*18]:
  * class c (0,1) x planes (p,q) in {A-carrier row, a-carrier row, valid}^2,

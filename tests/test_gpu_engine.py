@@ -169,3 +169,28 @@ def test_batch_of_many_cohorts(gepi):
         assert g.tobytes() == _direct(r).tobytes()
     for p in pls:
         p.close()
+
+
+@pytest.mark.parametrize("shards", [2, 3, 5])
+@pytest.mark.parametrize("objective", [0, 1], ids=["entropy", "fisher"])
+def test_sharded_scan_merges_to_whole_scan(gepi, tmp_path, shards, objective):
+    """Shard scans on the device (gepi_shard_range + scan_range), merged on the
+    host, equal the whole-triangle scan."""
+    pl, rows, fs, _ = make_planes(gepi, COHORTS[2], tmp_path)
+    k = 300
+    parts = []
+    for s in range(shards):
+        a0, na, b0, nb = gepi.shard_range(pl.n_snps, shards, s)
+        parts.append(pl.scan_range(a0, na, b0, nb, k, objective=objective))
+    n0, n1 = pl.class_sizes()
+    merged = gepi.merge_results(parts, k, n0 + n1, objective)
+    whole = pl.scan(k, objective=objective)
+    if objective == 0:
+        assert merged.tobytes() == whole.tobytes()
+    else:
+        items = lambda t: [(int(r["sA"]), int(r["sB"]), int(r["fun"])) for r in t]
+        gk = [-float(r["ent"]) for r in merged]
+        wk = [-float(r["ent"]) for r in whole]
+        probs = H.compare_ranked(items(merged), gk, items(whole), wk, k, rtol=1e-6)
+        assert not probs, probs[:5]
+    pl.close()

@@ -11,49 +11,52 @@
 // bits t, t+4, ..., t+28 into nibbles 0..7.  The sample order inside K is the
 // same for both operands, so the dot product is popcount(a & b).
 //
-// Tile: 40 A SNPs x 32 B SNPs.  MMA M = 128 TMEM lanes: lane quarter q holds A
+// Tile: 40 A SNPs x 64 B SNPs.  MMA M = 128 TMEM lanes: lane quarter q holds A
 // SNPs 10q..10q+9, lane 3i+p of the quarter = plane p of SNP i (lanes 30, 31
-// zero).  MMA N = 96: B row 3j+q = plane q of B SNP j.  K = 64 samples per
+// zero).  MMA N = 192: B row 3j+q = plane q of B SNP j.  K = 64 samples per
 // tcgen05.mma (kind::mxf4, scale_vec::2X); a pipeline chunk is up to 384
-// samples of one class (6 MMAs, one barrier wait and one commit).
+// samples of one class (6 MMAs, one barrier wait and one commit).  The
+// expansion of the packed bits bounds this design, so the tile is as wide in B
+// as tensor memory allows: each expanded A chunk serves 64 B SNPs.
 //
 // Operand layout in HBM (built once per plane set by tc_relayout_kernel): the
 // plane words cut into 12-word (384-sample) blocks, block-major --
 // blk[(b * rows_pad + row) * 12 + w] -- with class 0 in blocks [0, n0) and
 // class 1 in [n0, n0 + n1), a short last block of a class zero-filled and
 // rows_pad - 3 * n_snps zero rows at the end.  A chunk of a tile is then two
-// contiguous runs (120 A rows x 48 B, 96 B rows x 48 B) that the bulk-copy
+// contiguous runs (120 A rows x 48 B, 192 B rows x 48 B) that the bulk-copy
 // engine (cp.async.bulk) lands in a shared-memory ring; producer warps expand
 // them, A into tensor memory (tcgen05.st), B into shared memory; one thread
 // issues the MMAs.  No thread waits on global memory.
 //
-// Tensor memory (512 columns, one CTA per SM): two accumulator buffers of 192
-// columns (class 0 at +0, class 1 at +96), two A stages of 48 columns (384
-// E2M1 per lane) and 32 columns of scale factors (all 0x7F).  Shared memory:
-// two B stages of 96 rows x 192 bytes in the SWIZZLE_NONE K-major
-// core-matrix layout (8 rows x 16 B cores, k-group stride 128 B, row-group
-// stride 1536 B), the packed ring and the epilogue exchange rows.
+// Tensor memory (512 columns, one CTA per SM): one accumulator of 384 columns
+// (class 0 at +0, class 1 at +192), two A stages of 48 columns (384 E2M1 per
+// lane) and 32 columns of scale factors (all 0x7F).  The next tile's MMAs wait
+// for the epilogue to have loaded the accumulator (each epilogue warp releases
+// it after loading its second group of 8 B SNPs).  Shared memory: two B stages
+// of 192 rows x 192 bytes in the SWIZZLE_NONE K-major core-matrix layout (8
+// rows x 16 B cores, k-group stride 128 B, row-group stride 1536 B), the packed
+// ring (3 slots), the epilogue exchange rows and pair queues.
 //
-// Warp roles (18 warps, persistent CTA striding over the tile list):
-//   producers  warps 0-3 and 8-11 share every chunk: warps q and q+8 (lane
-//              quarter q) expand words 0-5 and 6-11 of packed A row 30q+lane
-//              (lane < 30) and of packed B row 32q+lane (q < 3); stages
+// Warp roles (26 warps, persistent CTA striding over the tile list):
+//   producers  warps 0-7 share every chunk: warp q + 4h (lane quarter q)
+//              expands words 6h..6h+5 of packed A row 30q+lane (lane < 30) and
+//              of packed B rows 32q+lane and, for q < 2, 128+32q+lane; stages
 //              alternate between chunks
-//   epilogue   warps 4-7 and 12-15 (two per lane quarter, each half of the B
-//              SNPs): drain an accumulator buffer per tile (tcgen05.ld),
-//              exchange the three A planes of a SNP through shared memory,
-//              bound every SNP pair per row pair (one chi^2 bound covers a
-//              row pair's five tests) and queue the few that may pass; the
-//              warp then runs the per-test bounds and the out-of-line
-//              refinement over its queue densely
-//   MMA        warp 16, one thread: up to 6 x tcgen05.mma per chunk, commits
-//   TMA        warp 17, one thread: two bulk copies per chunk
+//   epilogue   warps 8-23 (four per lane quarter, each 16 B SNPs): load their
+//              part of the accumulator (tcgen05.ld), exchange the three A
+//              planes of a SNP through shared memory, bound every SNP pair per
+//              row pair (one chi^2 bound covers a row pair's five tests) and
+//              queue the few that may pass; the warp then runs the per-test
+//              bounds and the out-of-line refinement over its queue densely
+//   MMA        warp 24, one thread: up to 6 x tcgen05.mma per chunk, commits
+//   TMA        warp 25, one thread: two bulk copies per chunk
 // mbarriers: pfull[j] (copy transaction bytes) / pempty[j] (8 producer warps)
 // per ring slot, full[s] (8 producer warps) / empty[s] (tcgen05.commit) per
-// stage, dfull[b] (commit) / dempty[b] (8 epilogue warps) per accumulator
-// buffer.  Every wait is bounded by a clock budget; on expiry the kernel
-// records an error, drains its own MMAs and tensor loads, frees its tensor
-// memory and returns.
+// stage, dfull (commit) / dempty (16 epilogue warps) for the accumulator.
+// Every wait is bounded by a clock budget; on expiry the kernel records an
+// error, drains its own MMAs and tensor loads, frees its tensor memory and
+// returns.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -64,27 +67,29 @@
 namespace gepi {
 
 constexpr int kTcASnps = 40;
-constexpr int kTcBSnps = 32;
+constexpr int kTcBSnps = 64;
 constexpr int kTcARows = 3 * kTcASnps;             // 120
-constexpr int kTcN = 3 * kTcBSnps;                 // 96
+constexpr int kTcN = 3 * kTcBSnps;                 // 192
 constexpr int kTcChunkWords = 12;                  // 384 samples per chunk (6 MMAs of K = 64)
 constexpr int kTcStages = 2;                       // A/B operand stages
-constexpr int kTcPStages = 6;                      // packed ring depth
+constexpr int kTcPStages = 3;                      // packed ring depth
 constexpr int kTcLbo = 128;                        // k-group stride (bytes)
 constexpr int kTcSbo = kTcChunkWords * kTcLbo;     // 8-row group stride: 1,536 bytes
-constexpr int kTcBStageBytes = (kTcN / 8) * kTcSbo;  // 18,432
+constexpr int kTcBStageBytes = (kTcN / 8) * kTcSbo;  // 36,864
 constexpr int kTcPABytes = kTcARows * kTcChunkWords * 4;  // 5,760
-constexpr int kTcPBBytes = kTcN * kTcChunkWords * 4;      // 4,608
-constexpr int kTcPStageBytes = kTcPABytes + kTcPBBytes;   // 10,368
+constexpr int kTcPBBytes = kTcN * kTcChunkWords * 4;      // 9,216
+constexpr int kTcPStageBytes = kTcPABytes + kTcPBBytes;   // 14,976
 constexpr int kTcXStride = 49;                     // epilogue exchange row pitch (floats)
-constexpr int kTcThreads = 18 * 32;
-constexpr int kTcProducerWarps = 8;
-constexpr int kTcMmaWarp = 16;
-constexpr int kTcTmaWarp = 17;
-constexpr int kTcEpiWarps = 8;
+constexpr int kTcThreads = 26 * 32;
+constexpr int kTcProducerWarps = 8;                // warps 0-7
+constexpr int kTcEpiWarp0 = 8;                     // epilogue warps 8-23
+constexpr int kTcEpiWarps = 16;
+constexpr int kTcMmaWarp = 24;
+constexpr int kTcTmaWarp = 25;
 constexpr uint32_t kTcCols = 512;
-constexpr uint32_t kTcDCols = 2 * kTcN;            // one accumulator buffer
-constexpr uint32_t kTcACol = 2 * kTcDCols;         // 384: first A stage
+constexpr uint32_t kTcDCols = 2 * kTcN;            // the accumulator (both classes): 384
+constexpr int kTcDBufs = 1;                        // one accumulator buffer
+constexpr uint32_t kTcACol = kTcDBufs * kTcDCols;  // 384: first A stage
 constexpr uint32_t kTcAStageCols = kTcChunkWords * 4;  // 48 columns (384 E2M1 per lane)
 constexpr uint32_t kTcSfCol = kTcACol + kTcStages * kTcAStageCols;  // 480: scale factors
 constexpr uint32_t kTcIdesc = (1u << 7) | (1u << 10)           // A, B = E2M1
@@ -409,7 +414,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                    ScanCtx ctx, uint32_t *__restrict__ dump, int *err) {
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     __shared__ uint64_t pfull_bar[kTcPStages], pempty_bar[kTcPStages], full_bar[kTcStages],
-        empty_bar[kTcStages], dfull_bar[2], dempty_bar[2], fin_bar;
+        empty_bar[kTcStages], dfull_bar[kTcDBufs], dempty_bar[kTcDBufs], fin_bar;
     __shared__ uint32_t tmem_slot;
     __shared__ int abort_flag;
 
@@ -434,7 +439,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             mbar_init(&full_bar[s], kTcProducerWarps);
             mbar_init(&empty_bar[s], 1);
         }
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < kTcDBufs; ++b) {
             mbar_init(&dfull_bar[b], 1);
             mbar_init(&dempty_bar[b], kTcEpiWarps);
         }
@@ -466,21 +471,22 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     __syncthreads();
     tc_fence_after();
 
-    if (warp < 4 || (warp >= 8 && warp < 12)) {
+    if (warp < kTcProducerWarps) {
         // ---------------- producers ----------------
         const int q = warp & 3;             // TMEM lane quarter
-        const int h = warp >= 8;            // words 6h .. 6h+5 of each row
-        const int u = q * 32 + lane;        // B row of this thread (q < 3)
-        const bool arow = lane < 30, brow = q < 3;
+        const int h = warp >> 2;            // words 6h .. 6h+5 of each row
+        const int u = q * 32 + lane;        // B rows of this thread: u, and u + 128 when q < 2
+        const bool arow = lane < 30, brow2 = q < 2;
         const int arow_off = (30 * q + (arow ? lane : 29)) * (kTcChunkWords * 4);
         const uint32_t ta0 = tbase + ((uint32_t)(32 * q) << 16) + kTcACol + 24 * h;
         unsigned char *bst0 = tc_smem + (u >> 3) * kTcSbo + (6 * h) * kTcLbo + (u & 7) * 16;
+        unsigned char *bst0b = bst0 + (128 / 8) * kTcSbo;  // row u + 128
         for (int idx = 0; idx < total; ++idx) {
             const uint32_t j = (uint32_t)idx % kTcPStages, s = (uint32_t)idx % kTcStages;
             if (!mbar_wait_warp(&pfull_bar[j], ((uint32_t)idx / kTcPStages) & 1, vabort, err, 5)) break;
             const unsigned char *pk = tc_smem + kTcPOff + (size_t)j * kTcPStageBytes + 24 * h;
             // every lane loads (lanes 30, 31 re-read row 30q+29 and clear it): no divergence
-            uint2 pa[3], pb[3];
+            uint2 pa[3], pb[3], pc[3];
             {
                 const uint2 *r = reinterpret_cast<const uint2 *>(pk + arow_off);
 #pragma unroll
@@ -490,13 +496,19 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     pa[m].y = arow ? pa[m].y : 0u;
                 }
             }
-#pragma unroll
-            for (int m = 0; m < 3; ++m) pb[m] = make_uint2(0, 0);
-            if (brow) {
+            {
                 const uint2 *r =
                     reinterpret_cast<const uint2 *>(pk + kTcPABytes + u * (kTcChunkWords * 4));
 #pragma unroll
                 for (int m = 0; m < 3; ++m) pb[m] = r[m];
+            }
+#pragma unroll
+            for (int m = 0; m < 3; ++m) pc[m] = make_uint2(0, 0);
+            if (brow2) {
+                const uint2 *r = reinterpret_cast<const uint2 *>(pk + kTcPABytes +
+                                                                 (u + 128) * (kTcChunkWords * 4));
+#pragma unroll
+                for (int m = 0; m < 3; ++m) pc[m] = r[m];
             }
             __syncwarp();
             mbar_arrive_warp(&pempty_bar[j]);
@@ -518,8 +530,20 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 tmem_st16(ta, r);
                 tmem_st8(ta + 16, r + 16);
             }
-            if (brow) {
+            {
                 unsigned char *bst = bst0 + (size_t)s * kTcBStageBytes;
+#pragma unroll
+                for (int m = 0; m < 6; ++m)
+                    *reinterpret_cast<uint4 *>(bst + m * kTcLbo) =
+                        make_uint4(o[4 * m], o[4 * m + 1], o[4 * m + 2], o[4 * m + 3]);
+            }
+            if (brow2) {
+#pragma unroll
+                for (int m = 0; m < 3; ++m) {
+                    expand_word(pc[m].x, o + 8 * m);
+                    expand_word(pc[m].y, o + 8 * m + 4);
+                }
+                unsigned char *bst = bst0b + (size_t)s * kTcBStageBytes;
 #pragma unroll
                 for (int m = 0; m < 6; ++m)
                     *reinterpret_cast<uint4 *>(bst + m * kTcLbo) =
@@ -573,8 +597,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             uint32_t gc = 0, lt = 0;
             bool ok = true;
             for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++lt) {
-                const uint32_t b = lt & 1;
-                if (!mbar_wait(&dempty_bar[b], ((lt >> 1) & 1) ^ 1, vabort, err, 2)) break;
+                const uint32_t b = lt % kTcDBufs;
+                if (!mbar_wait(&dempty_bar[b], ((lt / kTcDBufs) & 1) ^ 1, vabort, err, 2)) break;
                 tc_fence_after();
                 const uint32_t dbuf = tbase + b * kTcDCols;
                 for (int c = 0; c < nchunks; ++c, ++gc) {
@@ -605,10 +629,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         __syncwarp();
     } else {
-        // ---------------- epilogue (warps 4-7, 12-15) ----------------
-        const int q = warp & 3;
-        const int eh = warp >= 12;  // which half of the B SNPs
-        const int ew = q + 4 * eh;  // 0..7
+        // ---------------- epilogue (warps 8-23) ----------------
+        const int q = warp & 3;                   // TMEM lane quarter
+        const int ew = warp - kTcEpiWarp0;        // 0..15
+        const int eh = ew >> 2;                   // B SNPs 16 eh .. 16 eh + 15
         float *xb = reinterpret_cast<float *>(tc_smem + kTcXOff) + (size_t)ew * 32 * kTcXStride;
         uint32_t *qu = reinterpret_cast<uint32_t *>(tc_smem + kTcQOff) + (size_t)ew * kTcQueueCap;
         const int i = lane / 3, p = lane % 3;
@@ -616,8 +640,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const float lp_thr = DUMP ? 0.f : ctx.st->lp_thr;
         uint32_t lt = 0;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
-            const uint32_t b = lt & 1;
-            if (!mbar_wait_warp(&dfull_bar[b], (lt >> 1) & 1, vabort, err, 4)) break;
+            const uint32_t b = lt % kTcDBufs;
+            if (!mbar_wait_warp(&dfull_bar[b], (lt / kTcDBufs) & 1, vabort, err, 4)) break;
             tc_fence_after();
             const int2 tl = tiles[t];
             const int sA = a0 + tl.x * kTcASnps + 10 * q + i;
@@ -745,7 +769,7 @@ __global__ void tc_relayout_kernel(const uint32_t *__restrict__ planes, int Wp, 
 void tc_block_shape(int n_snps, int Wp, int W0, int *rows_pad, int *nblk) {
     const int n0 = (W0 + kTcChunkWords - 1) / kTcChunkWords;
     const int n1 = (Wp - W0 + kTcChunkWords - 1) / kTcChunkWords;
-    *rows_pad = 3 * n_snps + kTcARows;  // a box starting at any SNP's first row stays inside
+    *rows_pad = 3 * n_snps + std::max(kTcARows, kTcN);  // a box from any SNP's first row stays inside
     *nblk = n0 + n1;
 }
 

@@ -124,16 +124,23 @@ struct Job {
     int retries = 0;
     float lp_margin = 0.f;
     bool started = false, done = false, final_selected = false;
+    bool oldest = false;  // the oldest unfinished request (Policy::Oldest)
     gepi_status status = GEPI_OK;
     std::string error;
     gepi_scan_stats S{};
     Clock::time_point t_submit, t_admit, t_done;
 };
 
+// Which requests' launches go on the high-priority stream: those with little
+// work left (shortest first), or the oldest unfinished request (first come,
+// first served, with the others filling the SMs it leaves).
+enum class Policy { ShortFirst, Oldest };
+
 class Engine {
    public:
     // quantum_ms > 0 caps each batch at about that much device time.
-    Engine(int device, double quantum_ms) : device_(device), quantum_ms_(quantum_ms) {}
+    Engine(int device, double quantum_ms, Policy policy = Policy::ShortFirst)
+        : device_(device), quantum_ms_(quantum_ms), policy_(policy) {}
     ~Engine();
     gepi_status init();
     // Method choice, plane-set tables and the device tile list: may run on
@@ -159,6 +166,7 @@ class Engine {
 
     int device_ = 0, num_sms_ = 0;
     double quantum_ms_ = 0.0;
+    Policy policy_ = Policy::ShortFirst;
     int prio_lo_ = 0, prio_hi_ = 0;
     std::vector<std::unique_ptr<JobBuffers>> pool_;
     std::vector<JobBuffers *> free_;
@@ -360,17 +368,19 @@ void Engine::fail(Job &j, gepi_status st) {
 }
 
 // Queues the next batch of `j`: counting launch, state read-back, completion
-// event.  A request with little work left goes on the high-priority stream;
-// every earlier operation of the request has completed, so changing streams
-// between operations keeps its order.
+// event.  The policy picks the stream (high priority: a request with little
+// work left, or the oldest request); every earlier operation of the request
+// has completed, so changing streams between operations keeps its order.
 gepi_status Engine::launch(Job &j) {
     JobBuffers *b = j.buf;
     gepi_planes *pl = j.rq.pl;
     const ScanRequest &r = j.rq;
     j.inflight = std::min(j.batch, j.ntiles - j.next);
-    const bool short_job =
-        j.ms_per_tile <= 0.0 || (double)(j.ntiles - j.next) * j.ms_per_tile < kShortMs;
-    j.s = b->stream[short_job ? 1 : 0];
+    const bool high =
+        policy_ == Policy::Oldest
+            ? j.oldest
+            : (j.ms_per_tile <= 0.0 || (double)(j.ntiles - j.next) * j.ms_per_tile < kShortMs);
+    j.s = b->stream[high ? 1 : 0];
     ScanCtx ctx;
     ctx.T = pl->d_T;
     ctx.F = pl->F;
@@ -565,6 +575,14 @@ gepi_status Engine::complete(Job &j) {
 int Engine::poll(std::vector<Job *> &active) {
     DeviceGuard g(device_);
     int progressed = 0;
+    if (policy_ == Policy::Oldest) {
+        Job *old = nullptr;
+        for (Job *j : active) {
+            j->oldest = false;
+            if (!j->done && (!old || j->t_admit < old->t_admit)) old = j;
+        }
+        if (old) old->oldest = true;
+    }
     for (Job *j : active) {
         if (j->done || j->op != Op::None) continue;
         gepi_status st = advance(*j);  // newly admitted, or an empty range
@@ -641,6 +659,14 @@ gepi_status check_request(const gepi_scan_req &r, ScanRequest *out) {
 size_t request_footprint(int k) { return 2 * cand_cap(k) * sizeof(Cand) + sizeof(ScanState); }
 
 void idle_wait() { std::this_thread::sleep_for(std::chrono::microseconds(20)); }
+
+Policy env_policy(Policy dflt) {
+    if (const char *e = std::getenv("GEPI_SERVE_POLICY")) {
+        if (!std::strcmp(e, "oldest")) return Policy::Oldest;
+        if (!std::strcmp(e, "short")) return Policy::ShortFirst;
+    }
+    return dflt;
+}
 
 double env_quantum_ms(double dflt) {
     if (const char *e = std::getenv("GEPI_QUANTUM_MS")) {
@@ -782,7 +808,8 @@ gepi_status gepi_server_create(int32_t device, size_t hbm_budget_bytes, gepi_ser
     auto srv = std::make_unique<gepi_server>();
     srv->device = device;
     srv->budget = hbm_budget_bytes ? hbm_budget_bytes : (16ull << 30);
-    srv->engine = std::make_unique<Engine>(device, env_quantum_ms(10.0));
+    srv->engine =
+        std::make_unique<Engine>(device, env_quantum_ms(4.0), env_policy(Policy::ShortFirst));
     GEPI_TRY(srv->engine->init());
     gepi_server *p = srv.get();
     p->thread = std::thread([p] { p->run(); });

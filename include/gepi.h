@@ -273,7 +273,10 @@ gepi_status gepi_scan_batch(const gepi_scan_req *reqs, int32_t n, gepi_result *c
  * while their device footprint (2 candidate buffers each: 256 MiB at topmost
  * <= 512 Ki) fits `hbm_budget_bytes` (0: 16 GiB; the oldest request is always
  * admitted when nothing runs), and runs all admitted requests together as
- * gepi_scan_batch does, admitting new ones between engine steps.  Plane sets
+ * gepi_scan_batch does, admitting new ones between engine steps.  Batches are
+ * capped at about 4 ms of device time (GEPI_QUANTUM_MS) and requests with little
+ * work left run on a high-priority stream (GEPI_SERVE_POLICY=short, the default;
+ * "oldest" gives the oldest request the high-priority stream).  Plane sets
  * submitted to a server must not be used by other calls until their requests
  * are waited for.  No counterpart in the reference (it runs one scan per
  * process). */

@@ -41,8 +41,9 @@
 // Warp roles (26 warps, persistent CTA striding over the tile list):
 //   producers  warps 0-7 share every chunk: warp q + 4h (lane quarter q)
 //              expands words 6h..6h+5 of packed A row 30q+lane (lane < 30) and
-//              of packed B rows 32q+lane and, for q < 2, 128+32q+lane; stages
-//              alternate between chunks
+//              of packed B row 32q+lane, and three words of one of B rows
+//              128-191 (shared by all eight warps); stages alternate between
+//              chunks
 //   epilogue   warps 8-23 (four per lane quarter, each 16 B SNPs): load their
 //              part of the accumulator (tcgen05.ld), exchange the three A
 //              planes of a SNP through shared memory, bound every SNP pair per
@@ -475,18 +476,24 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         // ---------------- producers ----------------
         const int q = warp & 3;             // TMEM lane quarter
         const int h = warp >> 2;            // words 6h .. 6h+5 of each row
-        const int u = q * 32 + lane;        // B rows of this thread: u, and u + 128 when q < 2
-        const bool arow = lane < 30, brow2 = q < 2;
+        const int u = q * 32 + lane;        // B row u (< 128), words 6h .. 6h+5
+        // B rows 128..191 are shared by all eight warps, three words each:
+        // thread t = 32 warp + lane takes row 128 + (t & 63), words 3 (t >> 6) ..
+        // (consecutive lanes on consecutive rows: conflict-free 16-byte stores)
+        const int t8 = 32 * warp + lane;
+        const int u2 = 128 + (t8 & 63), w2 = 3 * (t8 >> 6);
+        const bool arow = lane < 30;
         const int arow_off = (30 * q + (arow ? lane : 29)) * (kTcChunkWords * 4);
         const uint32_t ta0 = tbase + ((uint32_t)(32 * q) << 16) + kTcACol + 24 * h;
         unsigned char *bst0 = tc_smem + (u >> 3) * kTcSbo + (6 * h) * kTcLbo + (u & 7) * 16;
-        unsigned char *bst0b = bst0 + (128 / 8) * kTcSbo;  // row u + 128
+        unsigned char *bst0b = tc_smem + (u2 >> 3) * kTcSbo + w2 * kTcLbo + (u2 & 7) * 16;
         for (int idx = 0; idx < total; ++idx) {
             const uint32_t j = (uint32_t)idx % kTcPStages, s = (uint32_t)idx % kTcStages;
             if (!mbar_wait_warp(&pfull_bar[j], ((uint32_t)idx / kTcPStages) & 1, vabort, err, 5)) break;
             const unsigned char *pk = tc_smem + kTcPOff + (size_t)j * kTcPStageBytes + 24 * h;
             // every lane loads (lanes 30, 31 re-read row 30q+29 and clear it): no divergence
-            uint2 pa[3], pb[3], pc[3];
+            uint2 pa[3], pb[3];
+            uint32_t pc[3];
             {
                 const uint2 *r = reinterpret_cast<const uint2 *>(pk + arow_off);
 #pragma unroll
@@ -502,11 +509,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
                 for (int m = 0; m < 3; ++m) pb[m] = r[m];
             }
-#pragma unroll
-            for (int m = 0; m < 3; ++m) pc[m] = make_uint2(0, 0);
-            if (brow2) {
-                const uint2 *r = reinterpret_cast<const uint2 *>(pk + kTcPABytes +
-                                                                 (u + 128) * (kTcChunkWords * 4));
+            {
+                const uint32_t *r = reinterpret_cast<const uint32_t *>(
+                    pk - 24 * h + kTcPABytes + u2 * (kTcChunkWords * 4) + 4 * w2);
 #pragma unroll
                 for (int m = 0; m < 3; ++m) pc[m] = r[m];
             }
@@ -537,15 +542,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     *reinterpret_cast<uint4 *>(bst + m * kTcLbo) =
                         make_uint4(o[4 * m], o[4 * m + 1], o[4 * m + 2], o[4 * m + 3]);
             }
-            if (brow2) {
+            {
 #pragma unroll
-                for (int m = 0; m < 3; ++m) {
-                    expand_word(pc[m].x, o + 8 * m);
-                    expand_word(pc[m].y, o + 8 * m + 4);
-                }
+                for (int m = 0; m < 3; ++m) expand_word(pc[m], o + 4 * m);
                 unsigned char *bst = bst0b + (size_t)s * kTcBStageBytes;
 #pragma unroll
-                for (int m = 0; m < 6; ++m)
+                for (int m = 0; m < 3; ++m)
                     *reinterpret_cast<uint4 *>(bst + m * kTcLbo) =
                         make_uint4(o[4 * m], o[4 * m + 1], o[4 * m + 2], o[4 * m + 3]);
             }

@@ -47,9 +47,10 @@
 //   epilogue   warps 8-23 (four per lane quarter, each 16 B SNPs): load their
 //              part of the accumulator (tcgen05.ld), exchange the three A
 //              planes of a SNP through shared memory, bound every SNP pair per
-//              row pair (one chi^2 bound covers a row pair's five tests) and
-//              queue the few that may pass; the warp then runs the per-test
-//              bounds and the out-of-line refinement over its queue densely
+//              row pair (one chi^2 bound covers a row pair's five tests, for
+//              either objective) and queue the few that may pass; the warp then
+//              runs the per-test bounds and the out-of-line refinement over its
+//              queue densely
 //   MMA        warp 24, one thread: up to 6 x tcgen05.mma per chunk, commits
 //   TMA        warp 25, one thread: two bulk copies per chunk
 // mbarriers: pfull[j] (copy transaction bytes) / pempty[j] (8 producer warps)
@@ -281,40 +282,6 @@ __device__ __forceinline__ void mbar_drain(uint64_t *b, uint32_t parity) {
 // score_tests; the tests that pass are refined one by one out of line, which
 // keeps the epilogue's code small (its warps share the instruction cache with
 // the producers).
-// Row-pair bound of an SNP pair for the entropy objective: bit 2i+j set when
-// row pair (2s+i, 2t+j) may hold a test that passes stage 1.  Every function
-// tested for a row pair is a function of the cell (bit of row 2s+i, bit of row
-// 2t+j), so its phi^2 is at most the class x cell table's chi^2 / m =
-// sum_k D_k^2 / (c_k y z m), D_k = a_k z - b_k y over the four cells (data
-// processing for the chi^2 divergence); below theta none of the row pair's
-// five tests passes.  D_k carries the product rounding margin, the sum a 2^-18
-// margin for the approximate reciprocals.  On the diagonal row 2t+j must be
-// <= row 2s+i, which drops (i, j) = (0, 1), bit 1.
-__device__ __forceinline__ uint32_t tc_rowpairs(const float *G0, const float *G1, bool diag,
-                                                float theta) {
-    const float y = G0[8], z = G1[8], yzm = y * z * (y + z);
-    uint32_t ok = 0;
-#pragma unroll
-    for (int i = 0; i < 2; ++i) {
-#pragma unroll
-        for (int j = 0; j < 2; ++j) {
-            const float a11 = G0[i * 3 + j], ar = G0[i * 3 + 2], ac = G0[6 + j];
-            const float b11 = G1[i * 3 + j], br = G1[i * 3 + 2], bc = G1[6 + j];
-            const float a[4] = {a11, ar - a11, ac - a11, y - ar - ac + a11};
-            const float b[4] = {b11, br - b11, bc - b11, z - br - bc + b11};
-            float S = 0.f;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const float az = a[k] * z, by = b[k] * y;
-                const float D = fabsf(az - by) + (az + by) * 2.384185791015625e-07f;  // 2^-22
-                S = fmaf(D * D, __fdividef(1.f, fmaxf(a[k] + b[k], 1.f)), S);
-            }
-            ok |= (uint32_t)(S * 1.0000038146972656f >= theta * yzm) << (2 * i + j);  // 1 + 2^-18
-        }
-    }
-    return ok & (diag ? 0xDu : 0xFu);
-}
-
 // Stage-1 bounds of the five tests of every row pair in `rp` (bit 2i+j) as a
 // bit mask, bit 5 * (2i + j) + f.  Same bounds as score_tests; the tests that
 // pass are refined one by one out of line.
@@ -694,19 +661,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     const int sBt = sB0 + 8 * g8 + jl;
                     uint32_t rp = 0;
                     if (lane < 30 && sA < a1 && jl < 8 && sBt < b1 && sBt <= sA) {
-                        if (OBJ == 0) {
-                            float G[18];
+                        float G[18];
 #pragma unroll
-                            for (int pp = 0; pp < 3; ++pp)
+                        for (int pp = 0; pp < 3; ++pp)
 #pragma unroll
-                                for (int qq = 0; qq < 3; ++qq) {
-                                    G[pp * 3 + qq] = xb[(3 * i + pp) * kTcXStride + 3 * jl + qq];
-                                    G[9 + pp * 3 + qq] = xb[(3 * i + pp) * kTcXStride + 24 + 3 * jl + qq];
-                                }
-                            rp = tc_rowpairs(G, G + 9, sA == sBt, theta);
-                        } else {
-                            rp = sA == sBt ? 0xDu : 0xFu;
-                        }
+                            for (int qq = 0; qq < 3; ++qq) {
+                                G[pp * 3 + qq] = xb[(3 * i + pp) * kTcXStride + 3 * jl + qq];
+                                G[9 + pp * 3 + qq] = xb[(3 * i + pp) * kTcXStride + 24 + 3 * jl + qq];
+                            }
+                        rp = rowpair_bounds(G, G + 9, sA == sBt, OBJ, theta, lp_thr);
                     }
                     const uint32_t bal = __ballot_sync(0xffffffffu, rp != 0);
                     if (rp) qu[qn + __popc(bal & ((1u << lane) - 1u))] = ((uint32_t)lane << 8) | ((uint32_t)jl << 4) | rp;

@@ -252,6 +252,55 @@ static __device__ __noinline__ void exact_test(const ScanCtx &ctx, int rA, int r
 // n * log2(n) in FP32 (0 for n <= 1).
 __device__ __forceinline__ float tlog2f(float n) { return n > 1.f ? n * __log2f(n) : 0.f; }
 
+// Row-pair bounds of an SNP pair: bit 2i+j set when row pair (2s+i, 2t+j) may
+// hold a test that passes stage 1.  Every function tested for a row pair is a
+// function of the cell (bit of row 2s+i, bit of row 2t+j), so its phi^2 is at
+// most the class x cell table's chi^2 / m = sum_k D_k^2 / (c_k y z m), with
+// D_k = a_k z - b_k y over the four cells (data processing for the chi^2
+// divergence).  Entropy: below theta no test of the row pair passes.  Fisher:
+// with C(n, k) >= 2^(n H(k/n)) / sqrt(2n) and C(m, k) <= 2^(m H(k/m))
+// (MacWilliams and Sloane), P(obs) >= 2^(-m I) / (2 sqrt(y z)), and I <= ln(1 +
+// phi^2) nats, so ln P(obs) >= -m ln(1 + chi^2/m) - ln(4 y z) / 2; above
+// lp_thr no test passes.  D_k carries the product rounding margin, the sum a
+// 2^-18 margin for the approximate reciprocals, the Fisher bound a margin of
+// 1e-4 relative plus 0.01.  A class without valid samples leaves every test
+// with w z = x y, which is never ranked.  On the diagonal row 2t+j must be <=
+// row 2s+i, which drops (i, j) = (0, 1), bit 1.
+__device__ __forceinline__ uint32_t rowpair_bounds(const float *G0, const float *G1, bool diag,
+                                                   int objective, float theta, float lp_thr) {
+    const float y = G0[8], z = G1[8], yz = y * z, m = y + z, yzm = yz * m;
+    if (!(yz > 0.f)) return 0u;
+    const float lfix = objective == 0 ? 0.f : 0.5f * logf(4.f * yz);
+    uint32_t ok = 0;
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const float a11 = G0[i * 3 + j], ar = G0[i * 3 + 2], ac = G0[6 + j];
+            const float b11 = G1[i * 3 + j], br = G1[i * 3 + 2], bc = G1[6 + j];
+            const float a[4] = {a11, ar - a11, ac - a11, y - ar - ac + a11};
+            const float b[4] = {b11, br - b11, bc - b11, z - br - bc + b11};
+            float S = 0.f;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const float az = a[k] * z, by = b[k] * y;
+                const float D = fabsf(az - by) + (az + by) * 2.384185791015625e-07f;  // 2^-22
+                S = fmaf(D * D, __fdividef(1.f, fmaxf(a[k] + b[k], 1.f)), S);
+            }
+            S *= 1.0000038146972656f;  // 1 + 2^-18
+            bool pass;
+            if (objective == 0) {
+                pass = S >= theta * yzm;
+            } else {
+                const float lo = -m * log1pf(S / yzm) - lfix;
+                pass = lo - (1e-4f * fabsf(lo) + 1e-2f) <= lp_thr;
+            }
+            ok |= (uint32_t)pass << (2 * i + j);
+        }
+    }
+    return ok & (diag ? 0xDu : 0xFu);
+}
+
 // Scores every test of SNP pair (s >= t) from the Gram counts of both classes
 // (G0 class 0, G1 class 1; float holding exact integers).  Row pairs (2s+i,
 // 2t+j) with 2t+j <= 2s+i, 5 functions each.
@@ -270,13 +319,16 @@ __device__ __forceinline__ void score_tests(const ScanCtx &ctx, const float *G0,
     const float m = y + z;
     const float yz = y * z;
     const bool diag = (s == t);
+    // row pairs that may hold a passing test (almost always none)
+    const uint32_t rp = rowpair_bounds(G0, G1, diag, ctx.objective, theta, lp_thr);
+    if (!rp) return;
     // Pair-level terms of the FP32 entropy estimate (stage 2), made on demand.
     float Tm = -1.f, Ty = 0.f, Tz = 0.f;
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
-            if (diag && j > i) continue;  // row 2t+j must be <= row 2s+i
+            if (!((rp >> (2 * i + j)) & 1u)) continue;  // includes row 2t+j > row 2s+i
             float on0[5], on1[5];
             {
                 float n11 = G0[i * 3 + j], r = G0[i * 3 + 2], c = G0[6 + j];

@@ -93,11 +93,15 @@ def test_batch_exact_under_candidate_overflow(gepi, tmp_path, cap, monkeypatch):
         pl.close()
 
 
+@pytest.mark.parametrize("policy", ["short", "oldest"])
 @pytest.mark.parametrize("budget", [0, 1])
-def test_server_same_result_alone_and_mixed(gepi, tmp_path, budget):
+def test_server_same_result_alone_and_mixed(gepi, tmp_path, budget, policy, monkeypatch):
     """A request gives the same results served alone as among others
     submitted concurrently from several threads (budget 1 byte: one request
-    admitted at a time; 0: the default budget, all together)."""
+    admitted at a time; 0: the default budget, all together), under either
+    scheduling policy and a 1 ms batch quantum."""
+    monkeypatch.setenv("GEPI_SERVE_POLICY", policy)
+    monkeypatch.setenv("GEPI_QUANTUM_MS", "1")
     cohorts = _cohorts(gepi, tmp_path)
     reqs = _requests(gepi, cohorts)
     with gepi.Server(0, budget) as srv:

@@ -261,7 +261,7 @@ __device__ __forceinline__ float tlog2f(float n) { return n > 1.f ? n * __log2f(
 // with C(n, k) >= 2^(n H(k/n)) / sqrt(2n) and C(m, k) <= 2^(m H(k/m))
 // (MacWilliams and Sloane), P(obs) >= 2^(-m I) / (2 sqrt(y z)), and I <= ln(1 +
 // phi^2) nats, so ln P(obs) >= -m ln(1 + chi^2/m) - ln(4 y z) / 2; above
-// lp_thr no test passes.  D_k carries the product rounding margin, the sum a
+// lp_thr no test passes.  |D_k| carries a rounding margin (below), the sum a
 // 2^-18 margin for the approximate reciprocals, the Fisher bound a margin of
 // 1e-4 relative plus 0.01.  A class without valid samples leaves every test
 // with w z = x y, which is never ranked.  On the diagonal row 2t+j must be <=
@@ -271,21 +271,35 @@ __device__ __forceinline__ uint32_t rowpair_bounds(const float *G0, const float 
     const float y = G0[8], z = G1[8], yz = y * z, m = y + z, yzm = yz * m;
     if (!(yz > 0.f)) return 0u;
     const float lfix = objective == 0 ? 0.f : 0.5f * logf(4.f * yz);
+    // The four row-pair tables share their margins: with R_i = a_i2 z - b_i2 y
+    // (row 2s+i carriers) and C_j = a_2j z - b_2j y (row 2t+j carriers), the
+    // cells give D_11 = a_ij z - b_ij y, D_10 = R_i - D_11, D_01 = C_j - D_11
+    // and D_00 = D_11 - R_i - C_j (the D_k sum to 0).  Every D_k is then within
+    // y z 2^-19 of its exact value (each product is at most y z, and at most
+    // four rounded terms enter), the margin E added to |D_k|.
+    const float E = yz * 1.9073486328125e-06f;  // 2^-19
+    float R[2], RT[2], C[2], CT[2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i) {
+        R[i] = G0[i * 3 + 2] * z - G1[i * 3 + 2] * y;
+        RT[i] = G0[i * 3 + 2] + G1[i * 3 + 2];
+        C[i] = G0[6 + i] * z - G1[6 + i] * y;
+        CT[i] = G0[6 + i] + G1[6 + i];
+    }
     uint32_t ok = 0;
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
 #pragma unroll
         for (int j = 0; j < 2; ++j) {
-            const float a11 = G0[i * 3 + j], ar = G0[i * 3 + 2], ac = G0[6 + j];
-            const float b11 = G1[i * 3 + j], br = G1[i * 3 + 2], bc = G1[6 + j];
-            const float a[4] = {a11, ar - a11, ac - a11, y - ar - ac + a11};
-            const float b[4] = {b11, br - b11, bc - b11, z - br - bc + b11};
+            const float a11 = G0[i * 3 + j], b11 = G1[i * 3 + j];
+            const float D11 = a11 * z - b11 * y, c11 = a11 + b11;
+            const float D[4] = {D11, R[i] - D11, C[j] - D11, D11 - R[i] - C[j]};
+            const float c[4] = {c11, RT[i] - c11, CT[j] - c11, m - RT[i] - CT[j] + c11};
             float S = 0.f;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                const float az = a[k] * z, by = b[k] * y;
-                const float D = fabsf(az - by) + (az + by) * 2.384185791015625e-07f;  // 2^-22
-                S = fmaf(D * D, __fdividef(1.f, fmaxf(a[k] + b[k], 1.f)), S);
+                const float t = fabsf(D[k]) + E;
+                S = fmaf(t * t, __fdividef(1.f, fmaxf(c[k], 1.f)), S);
             }
             S *= 1.0000038146972656f;  // 1 + 2^-18
             bool pass;

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -269,15 +270,34 @@ gepi_status resolve_method(gepi_planes *pl, int m, int *out) {
         if (pl->n_snps < 256) {
             pl->auto_method = GEPI_METHOD_POPC;
         } else {
-            GEPI_TRY(ensure_tables(pl));
-            GEPI_TRY(ensure_scan_buffers(pl, 1));
+            // The timing depends only on the shape (class widths, tuning
+            // triangle) and the device, so it is kept for the process: later
+            // plane sets of the same shape reuse the first one's choice.
+            static std::mutex mu;
+            static std::map<std::array<int, 4>, std::array<float, 3>> tuned;
             const int n = std::min(pl->n_snps, 4096);
-            float t_popc = 0.f, t_tc = 0.f;
-            GEPI_TRY(time_count_kernel(pl, false, n, &t_popc));
-            GEPI_TRY(time_count_kernel(pl, true, n, &t_tc));
-            pl->auto_method = t_tc < t_popc ? GEPI_METHOD_TENSOR : GEPI_METHOD_POPC;
-            pl->tune_ms[0] = t_popc;
-            pl->tune_ms[1] = t_tc;
+            const std::array<int, 4> key{pl->device, pl->W0, pl->Wp, n};
+            {
+                std::lock_guard<std::mutex> lk(mu);
+                auto it = tuned.find(key);
+                if (it != tuned.end()) {
+                    pl->auto_method = (int)it->second[0];
+                    pl->tune_ms[0] = it->second[1];
+                    pl->tune_ms[1] = it->second[2];
+                }
+            }
+            if (!pl->auto_method) {
+                GEPI_TRY(ensure_tables(pl));
+                GEPI_TRY(ensure_scan_buffers(pl, 1));
+                float t_popc = 0.f, t_tc = 0.f;
+                GEPI_TRY(time_count_kernel(pl, false, n, &t_popc));
+                GEPI_TRY(time_count_kernel(pl, true, n, &t_tc));
+                pl->auto_method = t_tc < t_popc ? GEPI_METHOD_TENSOR : GEPI_METHOD_POPC;
+                pl->tune_ms[0] = t_popc;
+                pl->tune_ms[1] = t_tc;
+                std::lock_guard<std::mutex> lk(mu);
+                tuned[key] = {(float)pl->auto_method, t_popc, t_tc};
+            }
         }
     }
     *out = pl->auto_method;

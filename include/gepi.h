@@ -230,7 +230,9 @@ gepi_status gepi_last_scan_stats(const gepi_planes *pl, gepi_scan_stats *out);
  * size its batch grid).  GEPI_METHOD_AUTO requests on `pl` use the method this
  * picks: the first call times both counting kernels on the leading triangle
  * of up to 4,096 SNPs at the plane set's full sample width and keeps the
- * faster; later calls return the cached choice.  Sets under 256 SNPs use
+ * faster; later calls return the cached choice, and later plane sets of the
+ * same shape (class widths, tuning triangle, device) in the process reuse it
+ * with the first set's timings.  Sets under 256 SNPs use
  * the popcount kernel untimed (times reported as 0).  Outputs may be NULL. */
 gepi_status gepi_planes_autotune(gepi_planes *pl, int32_t *method, float *popc_ms,
                                  float *tensor_ms);

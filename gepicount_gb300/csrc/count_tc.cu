@@ -11,39 +11,44 @@
 // bits t, t+4, ..., t+28 into nibbles 0..7.  The sample order inside K is the
 // same for both operands, so the dot product is popcount(a & b).
 //
-// Tile: 40 A SNPs x 64 B SNPs.  MMA M = 128 TMEM lanes: lane quarter q holds A
-// SNPs 10q..10q+9, lane 3i+p of the quarter = plane p of SNP i (lanes 30, 31
-// zero).  MMA N = 192: B row 3j+q = plane q of B SNP j.  K = 64 samples per
-// tcgen05.mma (kind::mxf4, scale_vec::2X); a pipeline chunk is up to 384
-// samples of one class (6 MMAs, one barrier wait and one commit).  The
-// expansion of the packed bits bounds this design, so the tile is as wide in B
-// as tensor memory allows: each expanded A chunk serves 64 B SNPs.
+// Tile: 80 A SNPs x 64 B SNPs, computed by a CTA pair (a cluster of two CTAs
+// on two SMs) with tcgen05.mma.cta_group::2, M = 256: CTA r holds A SNPs
+// 40r..40r+39 of the tile in its tensor memory and B SNPs 32r..32r+31 in its
+// shared memory, and receives the 40 x 64 accumulator of its own A SNPs.  Each
+// SM thus expands its 40 A SNPs and half of the 64 B SNPs (216 rows per chunk;
+// 312 for a 40 x 64 tile on one SM).  Lane quarter q of a CTA holds A SNPs
+// 10q..10q+9 of its half, lane 3i+p of the quarter = plane p of SNP i (lanes
+// 30, 31 zero).  MMA N = 192: B row 3j+q = plane q of B SNP j (the even CTA's
+// shared memory holds rows 0..95, the odd CTA's rows 96..191).  K = 64 samples
+// per tcgen05.mma (kind::mxf4, scale_vec::2X); a pipeline chunk is up to 384
+// samples of one class (6 MMAs, one barrier wait and one commit).
 //
 // Operand layout in HBM (built once per plane set by tc_relayout_kernel): the
 // plane words cut into 12-word (384-sample) blocks, block-major --
 // blk[(b * rows_pad + row) * 12 + w] -- with class 0 in blocks [0, n0) and
 // class 1 in [n0, n0 + n1), a short last block of a class zero-filled and
-// rows_pad - 3 * n_snps zero rows at the end.  A chunk of a tile is then two
-// contiguous runs (120 A rows x 48 B, 192 B rows x 48 B) that the bulk-copy
-// engine (cp.async.bulk) lands in a shared-memory ring; producer warps expand
-// them, A into tensor memory (tcgen05.st), B into shared memory; one thread
-// issues the MMAs.  No thread waits on global memory.
+// rows_pad - 3 * n_snps zero rows at the end.  A chunk of a CTA's half tile is
+// then two contiguous runs (120 A rows x 48 B, 96 B rows x 48 B) that the
+// bulk-copy engine (cp.async.bulk) lands in a shared-memory ring; producer
+// warps expand them, A into tensor memory (tcgen05.st), B into shared memory;
+// one thread of the even CTA issues the pair's MMAs.  No thread waits on
+// global memory.
 //
-// Tensor memory (512 columns, one CTA per SM): one accumulator of 384 columns
-// (class 0 at +0, class 1 at +192), two A stages of 48 columns (384 E2M1 per
-// lane) and 32 columns of scale factors (all 0x7F).  The next tile's MMAs wait
-// for the epilogue to have loaded the accumulator (each epilogue warp releases
-// it after loading its second group of 8 B SNPs).  Shared memory: two B stages
-// of 192 rows x 192 bytes in the SWIZZLE_NONE K-major core-matrix layout (8
-// rows x 16 B cores, k-group stride 128 B, row-group stride 1536 B), the packed
-// ring (3 slots), the epilogue exchange rows and pair queues.
+// Tensor memory (512 columns, one CTA per SM, allocated for the pair): one
+// accumulator of 384 columns (class 0 at +0, class 1 at +192), two A stages of
+// 48 columns (384 E2M1 per lane) and 32 columns of scale factors (all 0x7F).
+// The next tile's MMAs wait for both CTAs' epilogues to have loaded the
+// accumulator.  Shared memory: two B stages of 96 rows x 192 bytes in the
+// SWIZZLE_NONE K-major core-matrix layout (8 rows x 16 B cores, k-group stride
+// 128 B, row-group stride 1536 B), the packed ring (8 slots), the epilogue
+// exchange rows and pair queues.
 //
-// Warp roles (26 warps, persistent CTA striding over the tile list):
+// Warp roles (26 warps per CTA, the pair striding over the tile list):
 //   producers  warps 0-7 share every chunk: warp q + 4h (lane quarter q)
-//              expands words 6h..6h+5 of packed A row 30q+lane (lane < 30) and
-//              of packed B row 32q+lane, and three words of one of B rows
-//              128-191 (shared by all eight warps); stages alternate between
-//              chunks
+//              expands words 6h..6h+5 of packed A row 30q+lane (lane < 30);
+//              warps 0-5 also expand six words of one of the 96 B rows
+//              (thread t: row t % 96, words 6 (t / 96) ..); stages alternate
+//              between chunks
 //   epilogue   warps 8-23 (four per lane quarter, each 16 B SNPs): load their
 //              part of the accumulator (tcgen05.ld), exchange the three A
 //              planes of a SNP through shared memory, bound every SNP pair per
@@ -51,39 +56,49 @@
 //              either objective) and queue the few that may pass; the warp then
 //              runs the per-test bounds and the out-of-line refinement over its
 //              queue densely
-//   MMA        warp 24, one thread: up to 6 x tcgen05.mma per chunk, commits
+//   MMA        warp 24 of the even CTA, one thread: up to 6 x tcgen05.mma per
+//              chunk, commits (multicast to both CTAs' barriers)
 //   TMA        warp 25, one thread: two bulk copies per chunk
 // mbarriers: pfull[j] (copy transaction bytes) / pempty[j] (8 producer warps)
-// per ring slot, full[s] (8 producer warps) / empty[s] (tcgen05.commit) per
-// stage, dfull (commit) / dempty (16 epilogue warps) for the accumulator.
+// per ring slot of each CTA; full[s] (even CTA: 16 producer warps of the pair)
+// / empty[s] (commit, both CTAs) per stage; dfull (commit, both CTAs) / dempty
+// (even CTA: 32 epilogue warps of the pair) for the accumulator.
 // Every wait is bounded by a clock budget; on expiry the kernel records an
-// error, drains its own MMAs and tensor loads, frees its tensor memory and
-// returns.
+// error, drains its own MMAs and copies, meets its peer at the final cluster
+// barrier, frees its tensor memory and returns.
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdint>
 
 #include "device.cuh"
 
 namespace gepi {
 
-constexpr int kTcASnps = 40;
+constexpr int kTcASnps = 40;                       // A SNPs per CTA
+constexpr int kTcPairASnps = 2 * kTcASnps;         // A SNPs per tile (CTA pair): 80
 constexpr int kTcBSnps = 64;
 constexpr int kTcARows = 3 * kTcASnps;             // 120
 constexpr int kTcN = 3 * kTcBSnps;                 // 192
+constexpr int kTcBRows = kTcN / 2;                 // B rows per CTA: 96
 constexpr int kTcChunkWords = 12;                  // 384 samples per chunk (6 MMAs of K = 64)
+constexpr int kTcHalfWords = kTcChunkWords / 2;    // words of a row per producer thread
 constexpr int kTcStages = 2;                       // A/B operand stages
-constexpr int kTcPStages = 3;                      // packed ring depth
+constexpr int kTcTmemStages = 2;                   // stages with A in tensor memory (the rest: shared)
+constexpr int kTcPStages = 4;                      // packed ring depth
 constexpr int kTcLbo = 128;                        // k-group stride (bytes)
 constexpr int kTcSbo = kTcChunkWords * kTcLbo;     // 8-row group stride: 1,536 bytes
-constexpr int kTcBStageBytes = (kTcN / 8) * kTcSbo;  // 36,864
+constexpr int kTcBStageBytes = (kTcBRows / 8) * kTcSbo;   // 18,432
+constexpr int kTcAStageBytes = (128 / 8) * kTcSbo;        // 24,576 (M = 128 rows per CTA)
 constexpr int kTcPABytes = kTcARows * kTcChunkWords * 4;  // 5,760
-constexpr int kTcPBBytes = kTcN * kTcChunkWords * 4;      // 9,216
-constexpr int kTcPStageBytes = kTcPABytes + kTcPBBytes;   // 14,976
-constexpr int kTcXStride = 49;                     // epilogue exchange row pitch (floats)
+constexpr int kTcPBBytes = kTcBRows * kTcChunkWords * 4;  // 4,608
+constexpr int kTcPStageBytes = kTcPABytes + kTcPBBytes;   // 10,368
+constexpr int kTcXPitch = 98;                      // exchange row pitch (16-bit counts): 49 words
+constexpr int kTcMaxClass = 65535;                 // class sizes the 16-bit exchange holds
 constexpr int kTcThreads = 26 * 32;
 constexpr int kTcProducerWarps = 8;                // warps 0-7
+constexpr int kTcBWarps = 2 * kTcBRows / 32;       // warps 0-5 also expand B
 constexpr int kTcEpiWarp0 = 8;                     // epilogue warps 8-23
 constexpr int kTcEpiWarps = 16;
 constexpr int kTcMmaWarp = 24;
@@ -93,19 +108,26 @@ constexpr uint32_t kTcDCols = 2 * kTcN;            // the accumulator (both clas
 constexpr int kTcDBufs = 1;                        // one accumulator buffer
 constexpr uint32_t kTcACol = kTcDBufs * kTcDCols;  // 384: first A stage
 constexpr uint32_t kTcAStageCols = kTcChunkWords * 4;  // 48 columns (384 E2M1 per lane)
-constexpr uint32_t kTcSfCol = kTcACol + kTcStages * kTcAStageCols;  // 480: scale factors
+constexpr uint32_t kTcSfCol = kTcACol + kTcTmemStages * kTcAStageCols;  // 480: scale factors
 constexpr uint32_t kTcIdesc = (1u << 7) | (1u << 10)           // A, B = E2M1
                               | ((uint32_t)(kTcN >> 3) << 17)  // N
                               | (1u << 23)                     // scales UE8M0
-                              | ((uint32_t)(128 >> 4) << 24);  // M
-constexpr size_t kTcPOff = kTcStages * (size_t)kTcBStageBytes;               // packed ring
+                              | ((uint32_t)(256 >> 4) << 24);  // M (the pair)
+constexpr size_t kTcAOff = kTcStages * (size_t)kTcBStageBytes;  // A of a shared-memory stage
+constexpr size_t kTcPOff = kTcAOff + (kTcStages - kTcTmemStages) * (size_t)kTcAStageBytes;  // ring
 constexpr size_t kTcXOff = kTcPOff + kTcPStages * (size_t)kTcPStageBytes;    // exchange rows
 constexpr int kTcQueueCap = 3 * 32;                // pairs a warp can queue per 8 B SNPs
-constexpr size_t kTcQOff = kTcXOff + (size_t)kTcEpiWarps * 32 * kTcXStride * 4;  // pair queues
+constexpr size_t kTcQOff = kTcXOff + (size_t)kTcEpiWarps * 32 * kTcXPitch * 2;  // pair queues
 constexpr size_t kTcSmem = kTcQOff + (size_t)kTcEpiWarps * kTcQueueCap * 4;
 static_assert(kTcSfCol + 32 <= kTcCols, "tensor memory budget");
+static_assert(kTcBWarps * 32 == 2 * kTcBRows && kTcBWarps <= kTcProducerWarps, "B pieces");
+static_assert(kTcHalfWords == 4 || kTcHalfWords == 6,
+              "a producer thread stores 16 or 24 tensor-memory columns");
 constexpr long long kTcWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
-static_assert(kTcPStageBytes % 128 == 0 && kTcPABytes % 128 == 0 && kTcPOff % 128 == 0,
+static_assert(kTcStages == kTcTmemStages || kTcStages == kTcTmemStages + 1,
+              "at most one shared-memory A stage");
+static_assert(kTcPStageBytes % 128 == 0 && kTcPABytes % 128 == 0 && kTcPOff % 128 == 0 &&
+                  kTcAOff % 128 == 0,
               "TMA destinations 128-byte aligned");
 static_assert(kTcSmem > 114 * 1024 && kTcSmem <= 227 * 1024,
               "more than half an SM: one CTA (and tensor-memory owner) per SM");
@@ -168,6 +190,37 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, volatile
     return true;
 }
 
+__device__ __forceinline__ uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+// Address of `b` (this CTA's shared memory) in CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t cluster_addr(const void *b, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(su32(b)), "r"(rank));
+    return r;
+}
+
+// One arrival per warp on a barrier given by its cluster address (possibly in
+// the peer CTA).  Default (CTA-scope) semantics: what the arrival publishes is
+// tensor-memory and async-proxy work, ordered by the tcgen05 thread-sync fences
+// and the shared-to-async proxy fence around it; a cluster-scope release would
+// add a memory barrier per chunk.
+__device__ __forceinline__ void mbar_arrive_warp_cl(uint32_t caddr) {
+    asm volatile(
+        "{\n .reg .pred p;\n elect.sync _|p, 0xffffffff;\n"
+        " @p mbarrier.arrive.shared::cluster.b64 _, [%0];\n}\n" ::"r"(caddr)
+        : "memory");
+}
+
+// Every thread of both CTAs of the pair.
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n"
+                 "barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 // Warp-wide bounded wait: every lane polls the same barrier, so the warp
 // never diverges (a lane-0 poll plus a broadcast costs a reconvergence per
 // wait).
@@ -196,13 +249,42 @@ __device__ __forceinline__ uint64_t tc_bdesc(uint32_t saddr) {
            ((uint64_t)(kTcSbo >> 4) << 32) | (1ull << 46);
 }
 
-__device__ __forceinline__ void tc_mma(uint32_t d, uint32_t a, uint64_t bdesc, uint32_t sf,
-                                       uint32_t acc) {
+// One MMA of the pair (issued by the even CTA): D rows of CTA r = its own A
+// (tensor memory at `a`), B = both CTAs' stages at the same shared address.
+__device__ __forceinline__ void tc_mma2(uint32_t d, uint32_t a, uint64_t bdesc, uint32_t sf,
+                                        uint32_t acc) {
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %5, 0;\n"
-        " tcgen05.mma.cta_group::1.kind::mxf4.block_scale.scale_vec::2X [%0], [%1], %2, %3, [%4], "
+        " tcgen05.mma.cta_group::2.kind::mxf4.block_scale.scale_vec::2X [%0], [%1], %2, %3, [%4], "
         "[%4], p;\n}\n" ::"r"(d),
         "r"(a), "l"(bdesc), "r"(kTcIdesc), "r"(sf), "r"(acc));
+}
+
+// ... with A from shared memory (descriptor `adesc`, the same offset in both CTAs).
+__device__ __forceinline__ void tc_mma2_ss(uint32_t d, uint64_t adesc, uint64_t bdesc, uint32_t sf,
+                                           uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %5, 0;\n"
+        " tcgen05.mma.cta_group::2.kind::mxf4.block_scale.scale_vec::2X [%0], %1, %2, %3, [%4], "
+        "[%4], p;\n}\n" ::"r"(d),
+        "l"(adesc), "l"(bdesc), "r"(kTcIdesc), "r"(sf), "r"(acc));
+}
+
+// Completion of the pair's MMAs issued so far arrives on barrier `b` (same
+// offset) in both CTAs.
+__device__ __forceinline__ void tc_commit2_both(uint64_t *b) {
+    asm volatile(
+        "{\n .reg .b16 m;\n mov.b16 m, 3;\n"
+        " tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 "
+        "[%0], m;\n}\n" ::"r"(su32(b))
+        : "memory");
+}
+
+// ... on this CTA's barrier `b` only.
+__device__ __forceinline__ void tc_commit2(uint64_t *b) {
+    asm volatile(
+        "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(b))
+        : "memory");
 }
 
 __device__ __forceinline__ void tc_commit(uint64_t *b) {
@@ -349,6 +431,12 @@ static __device__ __noinline__ void tc_refine(const ScanCtx &ctx, int rA, int rB
     exact_test(ctx, rA, rB, f, w, x, y, z);
 }
 
+// A 16-bit count as a float: 2^23 + v has v in its low mantissa bits (an ALU
+// or and an FMA-pipe subtract instead of a conversion-unit instruction).
+__device__ __forceinline__ float u16f(uint16_t v) {
+    return __uint_as_float(0x4B000000u | (uint32_t)v) - 8388608.0f;
+}
+
 // Count of function f (AND, NAND, ANDN, NANDN, XOR) from n11 and the margins.
 __device__ __forceinline__ int fun_count(int n11, int r, int c, int tot, int f) {
     switch (f) {
@@ -376,7 +464,7 @@ struct ChunkMap {
 };
 
 template <bool DUMP, int OBJ>
-__global__ void __launch_bounds__(kTcThreads, 1)
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
     tc_tile_kernel(const uint32_t *__restrict__ blk, int rows_pad, int Wp, int W0,
                    const int2 *__restrict__ tiles, int ntiles, int a0, int a1, int b0, int b1,
                    ScanCtx ctx, uint32_t *__restrict__ dump, int *err) {
@@ -387,16 +475,18 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     __shared__ int abort_flag;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t rank = cluster_rank();  // 0: the CTA that issues the pair's MMAs
+    int pair, npairs;
+    asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(pair));
+    asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(npairs));
     ChunkMap cm;
     cm.W0 = W0;
     cm.W1 = Wp - W0;
     cm.n0 = (W0 + kTcChunkWords - 1) / kTcChunkWords;
     cm.nchunks = cm.n0 + (cm.W1 + kTcChunkWords - 1) / kTcChunkWords;
     const int nchunks = cm.nchunks;
-    const int my_tiles = (int)blockIdx.x < ntiles
-                             ? (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x
-                             : 0;
-    const int total = my_tiles * nchunks;  // this CTA's (tile, chunk) sequence, walked flat
+    const int my_tiles = pair < ntiles ? (ntiles - pair + npairs - 1) / npairs : 0;
+    const int total = my_tiles * nchunks;  // the pair's (tile, chunk) sequence, walked flat
 
     if (tid == 0) {
         for (int j = 0; j < kTcPStages; ++j) {
@@ -404,23 +494,24 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             mbar_init(&pempty_bar[j], kTcProducerWarps);
         }
         for (int s = 0; s < kTcStages; ++s) {
-            mbar_init(&full_bar[s], kTcProducerWarps);
+            mbar_init(&full_bar[s], 2 * kTcProducerWarps);  // both CTAs' producers (even CTA's)
             mbar_init(&empty_bar[s], 1);
         }
         for (int b = 0; b < kTcDBufs; ++b) {
             mbar_init(&dfull_bar[b], 1);
-            mbar_init(&dempty_bar[b], kTcEpiWarps);
+            mbar_init(&dempty_bar[b], 2 * kTcEpiWarps);  // both CTAs' epilogues (even CTA's)
         }
         mbar_init(&fin_bar, 1);
         abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+        // one warp of each CTA of the pair, collectively
+        asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          su32(&tmem_slot)),
                      "r"(kTcCols)
                      : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
     }
     tc_fence_before();
     __syncthreads();
@@ -437,84 +528,84 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     }
     tc_fence_before();
     __syncthreads();
+    // both CTAs' barriers are initialised and scale factors written before any
+    // arrival from the peer or any MMA
+    cluster_sync_all();
     tc_fence_after();
 
     if (warp < kTcProducerWarps) {
         // ---------------- producers ----------------
+        constexpr int HW = kTcHalfWords;
         const int q = warp & 3;             // TMEM lane quarter
-        const int h = warp >> 2;            // words 6h .. 6h+5 of each row
-        const int u = q * 32 + lane;        // B row u (< 128), words 6h .. 6h+5
-        // B rows 128..191 are shared by all eight warps, three words each:
-        // thread t = 32 warp + lane takes row 128 + (t & 63), words 3 (t >> 6) ..
-        // (consecutive lanes on consecutive rows: conflict-free 16-byte stores)
-        const int t8 = 32 * warp + lane;
-        const int u2 = 128 + (t8 & 63), w2 = 3 * (t8 >> 6);
+        const int h = warp >> 2;            // words HW h .. HW h + HW - 1 of each A row
         const bool arow = lane < 30;
         const int arow_off = (30 * q + (arow ? lane : 29)) * (kTcChunkWords * 4);
-        const uint32_t ta0 = tbase + ((uint32_t)(32 * q) << 16) + kTcACol + 24 * h;
-        unsigned char *bst0 = tc_smem + (u >> 3) * kTcSbo + (6 * h) * kTcLbo + (u & 7) * 16;
-        unsigned char *bst0b = tc_smem + (u2 >> 3) * kTcSbo + w2 * kTcLbo + (u2 & 7) * 16;
+        const uint32_t ta0 = tbase + ((uint32_t)(32 * q) << 16) + kTcACol + 4 * HW * h;
+        // B piece of warps 0-5: row u = t % 96, words HW hb .. HW hb + HW - 1
+        // (consecutive lanes on consecutive rows: conflict-free 16-byte stores)
+        const bool has_b = warp < kTcBWarps;
+        const int t8 = 32 * warp + lane;
+        const int u = t8 % kTcBRows, hb = t8 / kTcBRows;
+        unsigned char *bst0 = tc_smem + (u >> 3) * kTcSbo + (HW * hb) * kTcLbo + (u & 7) * 16;
+        // the shared-memory A stage: row 32q + lane (the tensor-memory lane of
+        // the other stages; rows 30, 31 of each quarter zero), words HW h ..
+        const int arow_sm = 32 * q + lane;
+        unsigned char *ast0 = tc_smem + kTcAOff + (arow_sm >> 3) * kTcSbo + (HW * h) * kTcLbo +
+                              (arow_sm & 7) * 16;
         for (int idx = 0; idx < total; ++idx) {
             const uint32_t j = (uint32_t)idx % kTcPStages, s = (uint32_t)idx % kTcStages;
             if (!mbar_wait_warp(&pfull_bar[j], ((uint32_t)idx / kTcPStages) & 1, vabort, err, 5)) break;
-            const unsigned char *pk = tc_smem + kTcPOff + (size_t)j * kTcPStageBytes + 24 * h;
+            const unsigned char *pk = tc_smem + kTcPOff + (size_t)j * kTcPStageBytes;
             // every lane loads (lanes 30, 31 re-read row 30q+29 and clear it): no divergence
-            uint2 pa[3], pb[3];
-            uint32_t pc[3];
+            uint2 pa[HW / 2], pb[HW / 2];
             {
-                const uint2 *r = reinterpret_cast<const uint2 *>(pk + arow_off);
+                const uint2 *r = reinterpret_cast<const uint2 *>(pk + 4 * HW * h + arow_off);
 #pragma unroll
-                for (int m = 0; m < 3; ++m) {
+                for (int m = 0; m < HW / 2; ++m) {
                     pa[m] = r[m];
                     pa[m].x = arow ? pa[m].x : 0u;
                     pa[m].y = arow ? pa[m].y : 0u;
                 }
             }
-            {
-                const uint2 *r =
-                    reinterpret_cast<const uint2 *>(pk + kTcPABytes + u * (kTcChunkWords * 4));
+            if (has_b) {
+                const uint2 *r = reinterpret_cast<const uint2 *>(pk + kTcPABytes +
+                                                                 u * (kTcChunkWords * 4) + 4 * HW * hb);
 #pragma unroll
-                for (int m = 0; m < 3; ++m) pb[m] = r[m];
-            }
-            {
-                const uint32_t *r = reinterpret_cast<const uint32_t *>(
-                    pk - 24 * h + kTcPABytes + u2 * (kTcChunkWords * 4) + 4 * w2);
-#pragma unroll
-                for (int m = 0; m < 3; ++m) pc[m] = r[m];
+                for (int m = 0; m < HW / 2; ++m) pb[m] = r[m];
             }
             __syncwarp();
             mbar_arrive_warp(&pempty_bar[j]);
             // expand into registers before waiting for the stage: the wait is
-            // on the MMAs two chunks back, and only the stores follow it
-            uint32_t r[24], o[24];
+            // on the MMAs kTcStages chunks back, and only the stores follow it
+            uint32_t r[4 * HW], o[4 * HW];
 #pragma unroll
-            for (int m = 0; m < 3; ++m) {
+            for (int m = 0; m < HW / 2; ++m) {
                 expand_word(pa[m].x, r + 8 * m);
                 expand_word(pa[m].y, r + 8 * m + 4);
-                expand_word(pb[m].x, o + 8 * m);
-                expand_word(pb[m].y, o + 8 * m + 4);
+            }
+            if (has_b) {
+#pragma unroll
+                for (int m = 0; m < HW / 2; ++m) {
+                    expand_word(pb[m].x, o + 8 * m);
+                    expand_word(pb[m].y, o + 8 * m + 4);
+                }
             }
             if (!mbar_wait_warp(&empty_bar[s], (((uint32_t)idx / kTcStages) & 1) ^ 1, vabort, err, 1))
                 break;
             tc_fence_after();
-            {
-                const uint32_t ta = ta0 + s * kTcAStageCols;
-                tmem_st16(ta, r);
-                tmem_st8(ta + 16, r + 16);
+            if (s < kTcTmemStages) {
+                tmem_st16(ta0 + s * kTcAStageCols, r);
+                if constexpr (HW == 6) tmem_st8(ta0 + s * kTcAStageCols + 16, r + 16);
+            } else {
+#pragma unroll
+                for (int m = 0; m < HW; ++m)
+                    *reinterpret_cast<uint4 *>(ast0 + m * kTcLbo) =
+                        make_uint4(r[4 * m], r[4 * m + 1], r[4 * m + 2], r[4 * m + 3]);
             }
-            {
+            if (has_b) {
                 unsigned char *bst = bst0 + (size_t)s * kTcBStageBytes;
 #pragma unroll
-                for (int m = 0; m < 6; ++m)
-                    *reinterpret_cast<uint4 *>(bst + m * kTcLbo) =
-                        make_uint4(o[4 * m], o[4 * m + 1], o[4 * m + 2], o[4 * m + 3]);
-            }
-            {
-#pragma unroll
-                for (int m = 0; m < 3; ++m) expand_word(pc[m], o + 4 * m);
-                unsigned char *bst = bst0b + (size_t)s * kTcBStageBytes;
-#pragma unroll
-                for (int m = 0; m < 3; ++m)
+                for (int m = 0; m < HW; ++m)
                     *reinterpret_cast<uint4 *>(bst + m * kTcLbo) =
                         make_uint4(o[4 * m], o[4 * m + 1], o[4 * m + 2], o[4 * m + 3]);
             }
@@ -522,32 +613,32 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             tc_fence_before();
             __syncwarp();
-            mbar_arrive_warp(&full_bar[s]);
+            mbar_arrive_warp_cl(cluster_addr(&full_bar[s], 0));
         }
     } else if (warp == kTcTmaWarp) {
         // ---------------- bulk-copy issuer ----------------
         if (lane == 0) {
             int issued = 0;
             int2 tl = make_int2(0, 0), tl_next = make_int2(0, 0);
-            if (my_tiles > 0) tl_next = tiles[blockIdx.x];
+            if (my_tiles > 0) tl_next = tiles[pair];
             int k = -1, c = nchunks;
             for (int idx = 0; idx < total; ++idx) {
                 if (++c >= nchunks) {
                     c = 0;
                     ++k;
                     tl = tl_next;
-                    if (k + 1 < my_tiles) tl_next = tiles[blockIdx.x + (k + 1) * gridDim.x];
+                    if (k + 1 < my_tiles) tl_next = tiles[pair + (k + 1) * npairs];
                 }
                 const uint32_t j = (uint32_t)idx % kTcPStages;
                 if (!mbar_wait(&pempty_bar[j], (((uint32_t)idx / kTcPStages) & 1) ^ 1, vabort, err, 6))
                     break;
                 unsigned char *pk = tc_smem + kTcPOff + (size_t)j * kTcPStageBytes;
                 const uint32_t *base = blk + (size_t)c * rows_pad * kTcChunkWords;
+                const size_t arow = (size_t)3 * (a0 + tl.x * kTcPairASnps + kTcASnps * (int)rank);
+                const size_t brow = (size_t)3 * (b0 + tl.y * kTcBSnps) + kTcBRows * rank;
                 mbar_expect_tx(&pfull_bar[j], kTcPStageBytes);
-                bulk_load(pk, base + (size_t)3 * (a0 + tl.x * kTcASnps) * kTcChunkWords, kTcPABytes,
-                          &pfull_bar[j]);
-                bulk_load(pk + kTcPABytes, base + (size_t)3 * (b0 + tl.y * kTcBSnps) * kTcChunkWords,
-                          kTcPBBytes, &pfull_bar[j]);
+                bulk_load(pk, base + arow * kTcChunkWords, kTcPABytes, &pfull_bar[j]);
+                bulk_load(pk + kTcPABytes, base + brow * kTcChunkWords, kTcPBBytes, &pfull_bar[j]);
                 issued = idx + 1;
             }
             // every copy this thread issued lands before the CTA exits
@@ -556,16 +647,17 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
         __syncwarp();
     } else if (warp == kTcMmaWarp) {
-        // ---------------- MMA issuer ----------------
-        if (lane == 0) {
+        // ---------------- MMA issuer (even CTA) ----------------
+        if (rank == 0 && lane == 0) {
             // stage s's descriptor: the start-address field (address >> 4) moves by
             // s * kTcBStageBytes >> 4 (no per-stage array: a runtime-indexed one
             // would live in local memory, one load per chunk on the issue path)
             const uint64_t bdesc0 = tc_bdesc(su32(tc_smem));
+            const uint64_t adesc_sm = tc_bdesc(su32(tc_smem + kTcAOff));
             const uint32_t sf = tbase + kTcSfCol;
             uint32_t gc = 0, lt = 0;
             bool ok = true;
-            for (int t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++lt) {
+            for (int t = pair; t < ntiles && ok; t += npairs, ++lt) {
                 const uint32_t b = lt % kTcDBufs;
                 if (!mbar_wait(&dempty_bar[b], ((lt / kTcDBufs) & 1) ^ 1, vabort, err, 2)) break;
                 tc_fence_after();
@@ -584,16 +676,24 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     tc_fence_after();
                     // MMA kk reads A columns 8kk.. and the k-group pair 2kk (256 B further
                     // each: +16 in the descriptor's address field)
+                    if (s < kTcTmemStages) {
 #pragma unroll
-                    for (int kk = 0; kk < kTcChunkWords / 2; ++kk)
-                        if (kk < nm) tc_mma(d, a + kk * 8, bd + (uint64_t)(16 * kk), sf, kk == 0 ? acc0 : 1u);
-                    tc_commit(&empty_bar[s]);
+                        for (int kk = 0; kk < kTcChunkWords / 2; ++kk)
+                            if (kk < nm) tc_mma2(d, a + kk * 8, bd + (uint64_t)(16 * kk), sf, kk == 0 ? acc0 : 1u);
+                    } else {
+#pragma unroll
+                        for (int kk = 0; kk < kTcChunkWords / 2; ++kk)
+                            if (kk < nm)
+                                tc_mma2_ss(d, adesc_sm + (uint64_t)(16 * kk), bd + (uint64_t)(16 * kk), sf,
+                                           kk == 0 ? acc0 : 1u);
+                    }
+                    tc_commit2_both(&empty_bar[s]);
                 }
                 if (!ok) break;
-                tc_commit(&dfull_bar[b]);
+                tc_commit2_both(&dfull_bar[b]);
             }
-            // drain every MMA this thread issued before tensor memory is freed
-            tc_commit(&fin_bar);
+            // drain every MMA this thread issued before either CTA frees tensor memory
+            tc_commit2(&fin_bar);
             mbar_drain(&fin_bar, 0);
         }
         __syncwarp();
@@ -602,37 +702,37 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         const int q = warp & 3;                   // TMEM lane quarter
         const int ew = warp - kTcEpiWarp0;        // 0..15
         const int eh = ew >> 2;                   // B SNPs 16 eh .. 16 eh + 15
-        float *xb = reinterpret_cast<float *>(tc_smem + kTcXOff) + (size_t)ew * 32 * kTcXStride;
+        // this warp's accumulator region as 16-bit counts: row = TMEM lane,
+        // [group 0: class 0 (24), class 1 (24) | group 1: ...] (odd word pitch)
+        uint16_t *xh = reinterpret_cast<uint16_t *>(tc_smem + kTcXOff) + (size_t)ew * 32 * kTcXPitch;
         uint32_t *qu = reinterpret_cast<uint32_t *>(tc_smem + kTcQOff) + (size_t)ew * kTcQueueCap;
         const int i = lane / 3, p = lane % 3;
         const float theta = DUMP ? 0.f : ctx.st->theta;
         const float lp_thr = DUMP ? 0.f : ctx.st->lp_thr;
+        const int aoff = kTcASnps * (int)rank + 10 * q;  // this warp's first A SNP in the tile
         uint32_t lt = 0;
-        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
+        for (int t = pair; t < ntiles; t += npairs, ++lt) {
             const uint32_t b = lt % kTcDBufs;
             if (!mbar_wait_warp(&dfull_bar[b], (lt / kTcDBufs) & 1, vabort, err, 4)) break;
             tc_fence_after();
             const int2 tl = tiles[t];
-            const int sA = a0 + tl.x * kTcASnps + 10 * q + i;
-            const int sB0 = b0 + tl.y * kTcBSnps;
-            const uint32_t tq = tbase + ((uint32_t)(32 * q) << 16) + b * kTcDCols;
-            for (int g8 = 2 * eh; g8 < 2 * eh + 2; ++g8) {
+            const int sA = a0 + tl.x * kTcPairASnps + aoff + i;
+            const int sB0 = b0 + tl.y * kTcBSnps + 16 * eh;
+            const uint32_t tq = tbase + ((uint32_t)(32 * q) << 16) + b * kTcDCols + 48 * eh;
+            // copy both groups of 8 B SNPs out, then hand the accumulator back:
+            // the next tile's MMAs run while this warp scores
+            for (int gl = 0; gl < 2; ++gl) {
                 uint32_t v0[24], v1[24];
-                tmem_ld16(tq + 24 * g8, *reinterpret_cast<uint32_t(*)[16]>(v0));
-                tmem_ld8(tq + 24 * g8 + 16, *reinterpret_cast<uint32_t(*)[8]>(v0 + 16));
-                tmem_ld16(tq + kTcN + 24 * g8, *reinterpret_cast<uint32_t(*)[16]>(v1));
-                tmem_ld8(tq + kTcN + 24 * g8 + 16, *reinterpret_cast<uint32_t(*)[8]>(v1 + 16));
+                tmem_ld16(tq + 24 * gl, *reinterpret_cast<uint32_t(*)[16]>(v0));
+                tmem_ld8(tq + 24 * gl + 16, *reinterpret_cast<uint32_t(*)[8]>(v0 + 16));
+                tmem_ld16(tq + kTcN + 24 * gl, *reinterpret_cast<uint32_t(*)[16]>(v1));
+                tmem_ld8(tq + kTcN + 24 * gl + 16, *reinterpret_cast<uint32_t(*)[8]>(v1 + 16));
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                if (g8 == 2 * eh + 1) {
-                    tc_fence_before();
-                    __syncwarp();
-                    mbar_arrive_warp(&dempty_bar[b]);
-                }
-                if (DUMP) {
+                if constexpr (DUMP) {
                     if (lane < 30 && sA < a1) {
 #pragma unroll
                         for (int jl = 0; jl < 8; ++jl) {
-                            const int sBt = sB0 + 8 * g8 + jl;
+                            const int sBt = sB0 + 8 * gl + jl;
                             if (sBt >= b1) continue;
                             uint32_t *o = dump + ((size_t)(sA - a0) * (b1 - b0) + (sBt - b0)) * 18;
 #pragma unroll
@@ -644,13 +744,20 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     }
                     continue;
                 }
-                float *row = xb + lane * kTcXStride;
+                uint32_t *row = reinterpret_cast<uint32_t *>(xh + lane * kTcXPitch + 48 * gl);
 #pragma unroll
-                for (int k = 0; k < 24; ++k) {
-                    row[k] = __uint_as_float(v0[k]);
-                    row[24 + k] = __uint_as_float(v1[k]);
+                for (int k = 0; k < 12; ++k) {
+                    row[k] = __float2uint_rn(__uint_as_float(v0[2 * k])) |
+                             (__float2uint_rn(__uint_as_float(v0[2 * k + 1])) << 16);
+                    row[12 + k] = __float2uint_rn(__uint_as_float(v1[2 * k])) |
+                                  (__float2uint_rn(__uint_as_float(v1[2 * k + 1])) << 16);
                 }
-                __syncwarp();
+            }
+            tc_fence_before();
+            __syncwarp();
+            mbar_arrive_warp_cl(cluster_addr(&dempty_bar[b], 0));
+            for (int gl = 0; gl < 2 && !DUMP; ++gl) {
+                const uint16_t *xg = xh + 48 * gl;
                 // Phase 1: every lane bounds its SNP pairs (i, jl), jl = p + 3r, and
                 // queues those with a row pair that may pass.  Phase 2: the warp
                 // runs stage 1 and the refinement over the queue, densely.
@@ -658,7 +765,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
                 for (int r = 0; r < 3; ++r) {
                     const int jl = p + 3 * r;
-                    const int sBt = sB0 + 8 * g8 + jl;
+                    const int sBt = sB0 + 8 * gl + jl;
                     uint32_t rp = 0;
                     if (lane < 30 && sA < a1 && jl < 8 && sBt < b1 && sBt <= sA) {
                         float G[18];
@@ -666,8 +773,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                         for (int pp = 0; pp < 3; ++pp)
 #pragma unroll
                             for (int qq = 0; qq < 3; ++qq) {
-                                G[pp * 3 + qq] = xb[(3 * i + pp) * kTcXStride + 3 * jl + qq];
-                                G[9 + pp * 3 + qq] = xb[(3 * i + pp) * kTcXStride + 24 + 3 * jl + qq];
+                                G[pp * 3 + qq] = u16f(xg[(3 * i + pp) * kTcXPitch + 3 * jl + qq]);
+                                G[9 + pp * 3 + qq] = u16f(xg[(3 * i + pp) * kTcXPitch + 24 + 3 * jl + qq]);
                             }
                         rp = rowpair_bounds(G, G + 9, sA == sBt, OBJ, theta, lp_thr);
                     }
@@ -679,14 +786,14 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 for (int e = lane; e < qn; e += 32) {
                     const uint32_t ent = qu[e];
                     const int il = (int)(ent >> 8) / 3, jl = (int)(ent >> 4) & 15;
-                    const int sAe = a0 + tl.x * kTcASnps + 10 * q + il, sBt = sB0 + 8 * g8 + jl;
+                    const int sAe = a0 + tl.x * kTcPairASnps + aoff + il, sBt = sB0 + 8 * gl + jl;
                     float G[18];
 #pragma unroll
                     for (int pp = 0; pp < 3; ++pp)
 #pragma unroll
                         for (int qq = 0; qq < 3; ++qq) {
-                            G[pp * 3 + qq] = xb[(3 * il + pp) * kTcXStride + 3 * jl + qq];
-                            G[9 + pp * 3 + qq] = xb[(3 * il + pp) * kTcXStride + 24 + 3 * jl + qq];
+                            G[pp * 3 + qq] = u16f(xg[(3 * il + pp) * kTcXPitch + 3 * jl + qq]);
+                            G[9 + pp * 3 + qq] = u16f(xg[(3 * il + pp) * kTcXPitch + 24 + 3 * jl + qq]);
                         }
                     uint32_t mask = tc_stage1<OBJ>(ctx, G, G + 9, ent & 15u, theta, lp_thr);
                     const int y = (int)G[8], z = (int)G[17];
@@ -707,9 +814,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
     tc_fence_before();
     __syncthreads();
+    // the pair's MMAs have drained (the even CTA's issuer waited for them) and
+    // no thread arrives on the peer's barriers any more
+    cluster_sync_all();
     if (warp == 0) {
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(kTcCols)
+        asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(kTcCols)
                      : "memory");
     }
 }
@@ -734,7 +844,8 @@ __global__ void tc_relayout_kernel(const uint32_t *__restrict__ planes, int Wp, 
 void tc_block_shape(int n_snps, int Wp, int W0, int *rows_pad, int *nblk) {
     const int n0 = (W0 + kTcChunkWords - 1) / kTcChunkWords;
     const int n1 = (Wp - W0 + kTcChunkWords - 1) / kTcChunkWords;
-    *rows_pad = 3 * n_snps + std::max(kTcARows, kTcN);  // a box from any SNP's first row stays inside
+    // a copy from any SNP's first row (A: up to 80 SNPs on, 120 rows; B: 192 rows) stays inside
+    *rows_pad = 3 * n_snps + std::max(3 * kTcPairASnps, kTcN);
     *nblk = n0 + n1;
 }
 
@@ -754,37 +865,59 @@ cudaError_t launch_tc_relayout(const uint32_t *planes, int Wp, int W0, int n_snp
     return cudaGetLastError();
 }
 
+// Pairs of CTAs the GPU holds at once (each pair on two SMs of one GPC): the
+// persistent grid, asked of the occupancy calculator once per device.
+template <bool DUMP, int OBJ>
+static cudaError_t launch_tc_pairs(const uint32_t *blk, int rows_pad, int Wp, int W0,
+                                   const int2 *tiles, int ntiles, int a0, int a1, int b0, int b1,
+                                   const ScanCtx &ctx, uint32_t *dump, int *err, int num_sms,
+                                   cudaStream_t stream) {
+    static std::atomic<int> resident[64];
+    auto kern = tc_tile_kernel<DUMP, OBJ>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+    if (e != cudaSuccess) return e;
+    int dev = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    int pairs = dev < 64 ? resident[dev].load() : 0;
+    if (pairs <= 0) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(2 * (num_sms / 2));
+        cfg.blockDim = dim3(kTcThreads);
+        cfg.dynamicSmemBytes = kTcSmem;
+        cfg.stream = stream;
+        int nc = 0;
+        if (cudaOccupancyMaxActiveClusters(&nc, (const void *)kern, &cfg) != cudaSuccess || nc <= 0) {
+            (void)cudaGetLastError();
+            nc = num_sms / 2;
+        }
+        pairs = std::min(nc, num_sms / 2);
+        if (dev < 64) resident[dev].store(pairs);
+    }
+    pairs = std::max(1, std::min(pairs, ntiles));
+    kern<<<2 * pairs, kTcThreads, kTcSmem, stream>>>(blk, rows_pad, Wp, W0, tiles, ntiles, a0, a1,
+                                                    b0, b1, ctx, dump, err);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_tc_tiles(const uint32_t *blk, int n_snps, int Wp, int W0, const int2 *tiles,
                             int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
                             uint32_t *dump, int *err, int num_sms, cudaStream_t stream) {
     if (ntiles <= 0) return cudaSuccess;
-    // whole K = 64 MMAs per class, 16-byte aligned copies
-    if ((W0 & 1) || (Wp & 1) || W0 <= 0 || Wp <= W0 || (reinterpret_cast<uintptr_t>(blk) & 15))
+    // whole K = 64 MMAs per class, 16-byte aligned copies, counts that fit the
+    // scoring warps' 16-bit exchange
+    if ((W0 & 1) || (Wp & 1) || W0 <= 0 || Wp <= W0 || (reinterpret_cast<uintptr_t>(blk) & 15) ||
+        32 * W0 > kTcMaxClass + 31 + 32 || 32 * (Wp - W0) > kTcMaxClass + 31 + 32)
         return cudaErrorInvalidValue;
     int rows_pad, nblk;
     tc_block_shape(n_snps, Wp, W0, &rows_pad, &nblk);
-    const int grid = ntiles < num_sms ? ntiles : num_sms;
-    cudaError_t e;
-    if (dump) {
-        e = cudaFuncSetAttribute(tc_tile_kernel<true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)kTcSmem);
-        if (e != cudaSuccess) return e;
-        tc_tile_kernel<true, 0><<<grid, kTcThreads, kTcSmem, stream>>>(
-            blk, rows_pad, Wp, W0, tiles, ntiles, a0, a1, b0, b1, ctx, dump, err);
-    } else if (ctx.objective == 0) {
-        e = cudaFuncSetAttribute(tc_tile_kernel<false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)kTcSmem);
-        if (e != cudaSuccess) return e;
-        tc_tile_kernel<false, 0><<<grid, kTcThreads, kTcSmem, stream>>>(
-            blk, rows_pad, Wp, W0, tiles, ntiles, a0, a1, b0, b1, ctx, nullptr, err);
-    } else {
-        e = cudaFuncSetAttribute(tc_tile_kernel<false, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)kTcSmem);
-        if (e != cudaSuccess) return e;
-        tc_tile_kernel<false, 1><<<grid, kTcThreads, kTcSmem, stream>>>(
-            blk, rows_pad, Wp, W0, tiles, ntiles, a0, a1, b0, b1, ctx, nullptr, err);
-    }
-    return cudaGetLastError();
+    if (dump)
+        return launch_tc_pairs<true, 0>(blk, rows_pad, Wp, W0, tiles, ntiles, a0, a1, b0, b1, ctx,
+                                        dump, err, num_sms, stream);
+    if (ctx.objective == 0)
+        return launch_tc_pairs<false, 0>(blk, rows_pad, Wp, W0, tiles, ntiles, a0, a1, b0, b1, ctx,
+                                         nullptr, err, num_sms, stream);
+    return launch_tc_pairs<false, 1>(blk, rows_pad, Wp, W0, tiles, ntiles, a0, a1, b0, b1, ctx,
+                                     nullptr, err, num_sms, stream);
 }
 
 // Dense kind::mxf4 MMA rate of this GPU, the roofline denominator of the
@@ -892,7 +1025,8 @@ cudaError_t tc_measure_peak(int num_sms, int reps, double *tflops, int *err, cud
     return e;
 }
 
-int tc_tile_a_snps() { return kTcASnps; }
+int tc_tile_a_snps() { return kTcPairASnps; }
 int tc_tile_b_snps() { return kTcBSnps; }
+int tc_max_class() { return kTcMaxClass; }
 
 }  // namespace gepi

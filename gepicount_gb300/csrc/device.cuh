@@ -286,6 +286,13 @@ __device__ __forceinline__ uint32_t rowpair_bounds(const float *G0, const float 
         C[i] = G0[6 + i] * z - G1[6 + i] * y;
         CT[i] = G0[6 + i] + G1[6 + i];
     }
+    // S = sum_k t_k^2 / c_k is compared in product form, sum_k t_k^2 P_k with
+    // P_k the product of the other three c_l (c_l clamped to 1), against
+    // theta y z m prod c_l: no reciprocals.  Every quantity is positive; each
+    // side carries at most seven float roundings (products below 2^128: t_k^2
+    // <= (y z)^2, prod c_l <= (m / 4)^4), so a 1 + 2^-18 factor on the sum keeps
+    // the comparison conservative.
+    const float th = theta * yzm;
     uint32_t ok = 0;
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
@@ -294,19 +301,24 @@ __device__ __forceinline__ uint32_t rowpair_bounds(const float *G0, const float 
             const float a11 = G0[i * 3 + j], b11 = G1[i * 3 + j];
             const float D11 = a11 * z - b11 * y, c11 = a11 + b11;
             const float D[4] = {D11, R[i] - D11, C[j] - D11, D11 - R[i] - C[j]};
-            const float c[4] = {c11, RT[i] - c11, CT[j] - c11, m - RT[i] - CT[j] + c11};
+            const float c0 = fmaxf(c11, 1.f), c1 = fmaxf(RT[i] - c11, 1.f),
+                        c2 = fmaxf(CT[j] - c11, 1.f), c3 = fmaxf(m - RT[i] - CT[j] + c11, 1.f);
+            const float c01 = c0 * c1, c23 = c2 * c3;
+            const float P[4] = {c1 * c23, c0 * c23, c3 * c01, c2 * c01};
             float S = 0.f;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
                 const float t = fabsf(D[k]) + E;
-                S = fmaf(t * t, __fdividef(1.f, fmaxf(c[k], 1.f)), S);
+                S = fmaf(t * t, P[k], S);
             }
             S *= 1.0000038146972656f;  // 1 + 2^-18
+            const float pc = c01 * c23;
             bool pass;
             if (objective == 0) {
-                pass = S >= theta * yzm;
+                pass = S >= th * pc;
             } else {
-                const float lo = -m * log1pf(S / yzm) - lfix;
+                // chi^2 itself (one division, its error inside the same factor)
+                const float lo = -m * log1pf(__fdividef(S, pc) / yzm) - lfix;
                 pass = lo - (1e-4f * fabsf(lo) + 1e-2f) <= lp_thr;
             }
             ok |= (uint32_t)pass << (2 * i + j);

@@ -238,7 +238,7 @@ gepi_status Engine::prepare(Job &j) {
     if (!j.tl) {
         // only this thread inserts (prep_mu_ held), so the key is still absent
         std::vector<int2> tiles;
-        pl_build_tiles(key[0], key[1], key[2], key[3], j.TA, j.TB, true, 8, tiles);
+        pl_build_tiles(key[0], key[1], key[2], key[3], j.TA, j.TB, true, tile_band(j.TA), tiles);
         TileList t;
         t.n = tiles.size();
         if (t.n) {
@@ -549,7 +549,7 @@ gepi_status Engine::complete(Job &j) {
         j.next += nbt;
         j.retries = 0;
         j.S.batches += 1;
-        if (j.next < j.ntiles && j.count > j.budget)
+        if (j.next < j.ntiles && j.count > select_trigger(j.budget, j.rq.k))
             return select_async(j, -1, 0xFFFFFFFFu, Op::SelBudget);
         if (j.next < j.ntiles) size_next_batch(j);
         return advance(j);

@@ -31,6 +31,7 @@ size_t tc_block_words(int n_snps, int Wp, int W0);
 cudaError_t tc_measure_peak(int num_sms, int reps, double *tflops, int *err, cudaStream_t stream);
 int tc_tile_a_snps();
 int tc_tile_b_snps();
+int tc_max_class();  // samples per class the tensor-core kernel takes
 cudaError_t run_select_compact(Cand *in, Cand *out, ScanState *st, void *sel, uint32_t cap,
                                uint32_t k, int n_override, uint32_t n_compact, int objective,
                                float lp_margin, int num_sms, cudaStream_t stream);
@@ -42,11 +43,22 @@ constexpr int kSelectLaunches = 20;  // init + 8 x (histogram, pick) + apply + c
 // threshold: 16 k (at least 64 Ki), at most half the buffer.  Raising the
 // threshold early keeps the bound passes -- and the exact scoring they cost --
 // for the few tests near the final top-k; the results do not depend on it.
+// A tiles per band of a tile list (build_tiles): bands of about 320 A SNPs
+// whatever the tile height.
+inline int tile_band(int TA) { return std::max(1, 320 / TA); }
+
 inline uint32_t select_budget(uint32_t cap, int k) {
     const uint64_t want = std::max<uint64_t>(65536u, 16ull * (uint64_t)k);
     return (uint32_t)std::min<uint64_t>(cap / 2, want);
 }
 // Tests in a scan's first batch: half the select budget (Fisher: 64 Ki).
+// The threshold is raised to the k-th best candidate after every batch that
+// leaves more than this many: a stale threshold lets every later test above it
+// through the bounds and into the candidate buffer (one global atomic each),
+// which costs far more than the select.
+inline uint32_t select_trigger(uint32_t budget, int k) {
+    return (uint32_t)std::min<uint64_t>(budget, std::max<uint64_t>(1024u, 2ull * (uint64_t)k));
+}
 inline double pilot_tests(int objective, uint32_t budget) {
     return objective == GEPI_ENTROPY ? budget / 2.0 : 1.0 * (1 << 16);
 }

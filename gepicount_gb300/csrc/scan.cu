@@ -213,7 +213,7 @@ gepi_status time_count_kernel(gepi_planes *pl, bool tc, int n, float *ms) {
     std::vector<int2> tiles;
     const int T0 = tc ? tc_tile_a_snps() : popc_tile_snps();
     const int T1 = tc ? tc_tile_b_snps() : popc_tile_snps();
-    build_tiles(0, n, 0, n, T0, T1, true, 8, tiles);
+    build_tiles(0, n, 0, n, T0, T1, true, tile_band(T0), tiles);
     GEPI_TRY(upload_tiles(pl, tiles));
     GEPI_TRY(ensure_events(pl, 4));
     ScanState st{};
@@ -262,12 +262,18 @@ gepi_status time_count_kernel(gepi_planes *pl, bool tc, int n, float *ms) {
 // and the faster one is kept.  Plane sets of fewer than 256 SNPs use the
 // popcount kernel without timing.
 gepi_status resolve_method(gepi_planes *pl, int m, int *out) {
+    // the tensor-core kernel hands counts to its scoring warps as 16-bit values
+    const bool tc_ok = pl->S0 <= tc_max_class() && pl->S1 <= tc_max_class();
+    if (m == GEPI_METHOD_TENSOR && !tc_ok)
+        return set_error(GEPI_ERR_ARG, "the tensor-core counting kernel takes at most " +
+                                           std::to_string(tc_max_class()) +
+                                           " samples per class; use the popcount method");
     if (m == GEPI_METHOD_POPC || m == GEPI_METHOD_TENSOR) {
         *out = m;
         return GEPI_OK;
     }
     if (!pl->auto_method) {
-        if (pl->n_snps < 256) {
+        if (pl->n_snps < 256 || !tc_ok) {
             pl->auto_method = GEPI_METHOD_POPC;
         } else {
             // The timing depends only on the shape (class widths, tuning
@@ -328,7 +334,6 @@ void rank_candidates(std::vector<Cand> &host, gepi_result *tops, int k) {
 }
 
 // Progress reporting at tile-band ends (gepi_scan_progress).
-constexpr int kTileBand = 8;  // A-tile rows per band of the tile list (build_tiles)
 
 struct Progress {
     gepi_progress_fn fn = nullptr;
@@ -336,13 +341,14 @@ struct Progress {
     int points = 0;
     bool with_tops = false;
     const std::vector<int2> *tiles = nullptr;
+    int band = 1;         // A tiles per band of the tile list
     size_t next_end = 0;  // tile index (a band end) at which the next callback fires
     int next_point = 1;
     std::chrono::steady_clock::time_point t0;
 
     bool band_end(size_t t) const {
         const auto &T = *tiles;
-        return t == 0 || t >= T.size() || T[t].x / kTileBand != T[t - 1].x / kTileBand;
+        return t == 0 || t >= T.size() || T[t].x / band != T[t - 1].x / band;
     }
     // first band end at or after tile index `thr`
     size_t end_at_or_after(size_t thr) const {
@@ -355,8 +361,9 @@ struct Progress {
     size_t threshold(int point) const {
         return (size_t)std::ceil((double)point * (double)tiles->size() / (double)points);
     }
-    void start(const std::vector<int2> &T) {
+    void start(const std::vector<int2> &T, int band_tiles) {
         tiles = &T;
+        band = band_tiles;
         t0 = std::chrono::steady_clock::now();
         next_point = 1;
         next_end = points > 0 ? end_at_or_after(threshold(1)) : end_at_or_after(1);
@@ -396,7 +403,7 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
     const int TA = tc ? tc_tile_a_snps() : popc_tile_snps();
     const int TB = tc ? tc_tile_b_snps() : popc_tile_snps();
     std::vector<int2> tiles;
-    build_tiles(a0, a0 + na, b0, b0 + nb, TA, TB, true, 8, tiles);
+    build_tiles(a0, a0 + na, b0, b0 + nb, TA, TB, true, tile_band(TA), tiles);
     GEPI_TRY(upload_tiles(pl, tiles));
     GEPI_TRY(ensure_events(pl, 4));
     gepi_scan_stats &S = pl->stats;
@@ -417,7 +424,7 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
         S.diag_snps = hi > lo ? (uint64_t)(hi - lo) : 0;
     }
     GEPI_CUDA(cudaEventRecord(pl->ev[0], pl->stream));
-    if (prog && prog->fn) prog->start(tiles);
+    if (prog && prog->fn) prog->start(tiles, tile_band(TA));
     else prog = nullptr;
 
     ScanState init{};
@@ -444,6 +451,7 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
     const size_t ntiles = tiles.size();
     const double tests_per_tile = 20.0 * TA * TB;
     const uint32_t budget = select_budget(pl->cap, k);
+    const uint32_t trigger = select_trigger(budget, k);
     size_t batch =
         (size_t)std::max(1.0, std::floor(pilot_tests(par->objective, budget) / tests_per_tile));
     size_t t = 0;
@@ -502,7 +510,7 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
         t += nbt;
         retries = 0;
         S.batches += 1;
-        if (count > budget && t < ntiles) {
+        if (count > trigger && t < ntiles) {
             S.other_launches += kSelectLaunches;
             GEPI_CUDA(run_select_compact(pl->d_cand[cur], pl->d_cand[cur ^ 1], pl->d_state,
                                          pl->d_sel, pl->cap, (uint32_t)k, -1, 0xFFFFFFFFu,
@@ -519,8 +527,9 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
             pr.tiles_done = t;
             pr.tiles_total = ntiles;
             // bands before the one in progress are complete
-            const int bands_done = t < ntiles ? tiles[t].x / kTileBand : (na + TA - 1) / TA;
-            pr.snps_done = a0 + std::min(na, bands_done * kTileBand * TA);
+            const int band = prog->band;
+            const int bands_done = t < ntiles ? tiles[t].x / band : (na + TA - 1) / TA;
+            pr.snps_done = a0 + std::min(na, bands_done * band * TA);
             std::vector<gepi_result> snap;
             if (prog->with_tops) {
                 std::vector<Cand> host(count);

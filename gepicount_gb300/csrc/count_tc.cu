@@ -105,8 +105,7 @@ constexpr int kTcMmaWarp = 24;
 constexpr int kTcTmaWarp = 25;
 constexpr uint32_t kTcCols = 512;
 constexpr uint32_t kTcDCols = 2 * kTcN;            // the accumulator (both classes): 384
-constexpr int kTcDBufs = 1;                        // one accumulator buffer
-constexpr uint32_t kTcACol = kTcDBufs * kTcDCols;  // 384: first A stage
+constexpr uint32_t kTcACol = kTcDCols;             // 384: first A stage
 constexpr uint32_t kTcAStageCols = kTcChunkWords * 4;  // 48 columns (384 E2M1 per lane)
 constexpr uint32_t kTcSfCol = kTcACol + kTcTmemStages * kTcAStageCols;  // 480: scale factors
 constexpr uint32_t kTcIdesc = (1u << 7) | (1u << 10)           // A, B = E2M1
@@ -470,7 +469,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
                    ScanCtx ctx, uint32_t *__restrict__ dump, int *err) {
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     __shared__ uint64_t pfull_bar[kTcPStages], pempty_bar[kTcPStages], full_bar[kTcStages],
-        empty_bar[kTcStages], dfull_bar[kTcDBufs], dempty_bar[kTcDBufs], fin_bar;
+        empty_bar[kTcStages], dfull_bar[2], dempty_bar[2], fin_bar;
     __shared__ uint32_t tmem_slot;
     __shared__ int abort_flag;
 
@@ -497,9 +496,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
             mbar_init(&full_bar[s], 2 * kTcProducerWarps);  // both CTAs' producers (even CTA's)
             mbar_init(&empty_bar[s], 1);
         }
-        for (int b = 0; b < kTcDBufs; ++b) {
-            mbar_init(&dfull_bar[b], 1);
-            mbar_init(&dempty_bar[b], 2 * kTcEpiWarps);  // both CTAs' epilogues (even CTA's)
+        for (int cls = 0; cls < 2; ++cls) {  // the accumulator's class halves
+            mbar_init(&dfull_bar[cls], 1);
+            mbar_init(&dempty_bar[cls], 2 * kTcEpiWarps);  // both CTAs' epilogues (even CTA's)
         }
         mbar_init(&fin_bar, 1);
         abort_flag = 0;
@@ -658,14 +657,21 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
             uint32_t gc = 0, lt = 0;
             bool ok = true;
             for (int t = pair; t < ntiles && ok; t += npairs, ++lt) {
-                const uint32_t b = lt % kTcDBufs;
-                if (!mbar_wait(&dempty_bar[b], ((lt / kTcDBufs) & 1) ^ 1, vabort, err, 2)) break;
-                tc_fence_after();
-                const uint32_t dbuf = tbase + b * kTcDCols;
                 for (int c = 0; c < nchunks; ++c, ++gc) {
+                    const int cls = c < cm.n0 ? 0 : 1;
+                    if (c == 0 || c == cm.n0) {
+                        // both CTAs' epilogues have copied this class half of the
+                        // previous tile's accumulator out (while the other half was
+                        // being accumulated): the tensor pipe never drains between tiles
+                        if (!mbar_wait(&dempty_bar[cls], (lt & 1) ^ 1, vabort, err, 2)) {
+                            ok = false;
+                            break;
+                        }
+                        tc_fence_after();
+                    }
                     const uint32_t s = gc % kTcStages;
                     const int nm = cm.mmas(c);
-                    const uint32_t d = dbuf + (c < cm.n0 ? 0u : (uint32_t)kTcN);
+                    const uint32_t d = tbase + (uint32_t)(cls * kTcN);
                     const uint32_t acc0 = (c == 0 || c == cm.n0) ? 0u : 1u;
                     const uint32_t a = tbase + kTcACol + s * kTcAStageCols;
                     const uint64_t bd = bdesc0 + (uint64_t)((s * (uint32_t)kTcBStageBytes) >> 4);
@@ -688,9 +694,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
                                            kk == 0 ? acc0 : 1u);
                     }
                     tc_commit2_both(&empty_bar[s]);
+                    if (c == cm.n0 - 1 || c == nchunks - 1) tc_commit2_both(&dfull_bar[cls]);
                 }
-                if (!ok) break;
-                tc_commit2_both(&dfull_bar[b]);
             }
             // drain every MMA this thread issued before either CTA frees tensor memory
             tc_commit2(&fin_bar);
@@ -711,51 +716,54 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
         const float lp_thr = DUMP ? 0.f : ctx.st->lp_thr;
         const int aoff = kTcASnps * (int)rank + 10 * q;  // this warp's first A SNP in the tile
         uint32_t lt = 0;
-        for (int t = pair; t < ntiles; t += npairs, ++lt) {
-            const uint32_t b = lt % kTcDBufs;
-            if (!mbar_wait_warp(&dfull_bar[b], (lt / kTcDBufs) & 1, vabort, err, 4)) break;
-            tc_fence_after();
+        bool live = true;
+        for (int t = pair; t < ntiles && live; t += npairs, ++lt) {
             const int2 tl = tiles[t];
             const int sA = a0 + tl.x * kTcPairASnps + aoff + i;
             const int sB0 = b0 + tl.y * kTcBSnps + 16 * eh;
-            const uint32_t tq = tbase + ((uint32_t)(32 * q) << 16) + b * kTcDCols + 48 * eh;
-            // copy both groups of 8 B SNPs out, then hand the accumulator back:
-            // the next tile's MMAs run while this warp scores
-            for (int gl = 0; gl < 2; ++gl) {
-                uint32_t v0[24], v1[24];
-                tmem_ld16(tq + 24 * gl, *reinterpret_cast<uint32_t(*)[16]>(v0));
-                tmem_ld8(tq + 24 * gl + 16, *reinterpret_cast<uint32_t(*)[8]>(v0 + 16));
-                tmem_ld16(tq + kTcN + 24 * gl, *reinterpret_cast<uint32_t(*)[16]>(v1));
-                tmem_ld8(tq + kTcN + 24 * gl + 16, *reinterpret_cast<uint32_t(*)[8]>(v1 + 16));
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                if constexpr (DUMP) {
-                    if (lane < 30 && sA < a1) {
+            const uint32_t tq = tbase + ((uint32_t)(32 * q) << 16) + 48 * eh;
+            // copy each class half out as soon as its MMAs are done and hand it
+            // back: the tensor pipe goes on with the other half, then the next tile
+            for (int cls = 0; cls < 2; ++cls) {
+                if (!mbar_wait_warp(&dfull_bar[cls], lt & 1, vabort, err, 4)) {
+                    live = false;
+                    break;
+                }
+                tc_fence_after();
 #pragma unroll
-                        for (int jl = 0; jl < 8; ++jl) {
-                            const int sBt = sB0 + 8 * gl + jl;
-                            if (sBt >= b1) continue;
-                            uint32_t *o = dump + ((size_t)(sA - a0) * (b1 - b0) + (sBt - b0)) * 18;
+                for (int gl = 0; gl < 2; ++gl) {
+                    uint32_t v[24];
+                    tmem_ld16(tq + cls * kTcN + 24 * gl, *reinterpret_cast<uint32_t(*)[16]>(v));
+                    tmem_ld8(tq + cls * kTcN + 24 * gl + 16, *reinterpret_cast<uint32_t(*)[8]>(v + 16));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    uint32_t *row = reinterpret_cast<uint32_t *>(xh + lane * kTcXPitch + 48 * gl + 24 * cls);
 #pragma unroll
-                            for (int qq = 0; qq < 3; ++qq) {
-                                o[p * 3 + qq] = (uint32_t)__uint_as_float(v0[3 * jl + qq]);
-                                o[9 + p * 3 + qq] = (uint32_t)__uint_as_float(v1[3 * jl + qq]);
-                            }
+                    for (int k = 0; k < 12; ++k)
+                        row[k] = __float2uint_rn(__uint_as_float(v[2 * k])) |
+                                 (__float2uint_rn(__uint_as_float(v[2 * k + 1])) << 16);
+                }
+                tc_fence_before();
+                __syncwarp();
+                mbar_arrive_warp_cl(cluster_addr(&dempty_bar[cls], 0));
+            }
+            if (!live) break;
+            if constexpr (DUMP) {
+                if (lane < 30 && sA < a1) {
+                    const uint16_t *xr = xh + lane * kTcXPitch;
+                    for (int jb = 0; jb < 16; ++jb) {
+                        const int sBt = sB0 + jb;
+                        if (sBt >= b1) continue;
+                        const int gl = jb >> 3, jl = jb & 7;
+                        uint32_t *o = dump + ((size_t)(sA - a0) * (b1 - b0) + (sBt - b0)) * 18;
+#pragma unroll
+                        for (int qq = 0; qq < 3; ++qq) {
+                            o[p * 3 + qq] = xr[48 * gl + 3 * jl + qq];
+                            o[9 + p * 3 + qq] = xr[48 * gl + 24 + 3 * jl + qq];
                         }
                     }
-                    continue;
                 }
-                uint32_t *row = reinterpret_cast<uint32_t *>(xh + lane * kTcXPitch + 48 * gl);
-#pragma unroll
-                for (int k = 0; k < 12; ++k) {
-                    row[k] = __float2uint_rn(__uint_as_float(v0[2 * k])) |
-                             (__float2uint_rn(__uint_as_float(v0[2 * k + 1])) << 16);
-                    row[12 + k] = __float2uint_rn(__uint_as_float(v1[2 * k])) |
-                                  (__float2uint_rn(__uint_as_float(v1[2 * k + 1])) << 16);
-                }
+                __syncwarp();
             }
-            tc_fence_before();
-            __syncwarp();
-            mbar_arrive_warp_cl(cluster_addr(&dempty_bar[b], 0));
             for (int gl = 0; gl < 2 && !DUMP; ++gl) {
                 const uint16_t *xg = xh + 48 * gl;
                 // Phase 1: every lane bounds its SNP pairs (i, jl), jl = p + 3r, and

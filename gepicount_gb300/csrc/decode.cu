@@ -155,4 +155,50 @@ cudaError_t launch_decode_rows(const uint64_t *bits, const uint64_t *valid, int 
     return cudaGetLastError();
 }
 
+// Marginal association of every SNP with the class: the larger phi^2 of its
+// two allele rows' carrier x class tables (D^2 / ((a + b)(m - a - b) y z),
+// D = a z - b y; a, b carriers and y, z valid samples of class 0, 1).  One
+// warp per SNP.  The scan uses it only to order its tiles.
+__global__ void marginal_kernel(const uint32_t *__restrict__ planes, int n_snps, int Wp, int W0,
+                                float *__restrict__ score) {
+    const int lane = threadIdx.x & 31;
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarp = (gridDim.x * blockDim.x) >> 5;
+    for (int s = gwarp; s < n_snps; s += nwarp) {
+        const uint32_t *r = planes + (size_t)s * 3 * Wp;
+        int c[3][2] = {{0, 0}, {0, 0}, {0, 0}};
+        for (int w = lane; w < Wp; w += 32) {
+            const int cls = w < W0 ? 0 : 1;
+#pragma unroll
+            for (int p = 0; p < 3; ++p) c[p][cls] += __popc(__ldg(r + (size_t)p * Wp + w));
+        }
+#pragma unroll
+        for (int p = 0; p < 3; ++p)
+#pragma unroll
+            for (int k = 0; k < 2; ++k)
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) c[p][k] += __shfl_xor_sync(0xffffffffu, c[p][k], o);
+        if (lane == 0) {
+            const double y = c[2][0], z = c[2][1], m = y + z;
+            double best = 0.0;
+            for (int p = 0; p < 2; ++p) {
+                const double a = c[p][0], b = c[p][1], n = a + b;
+                const double den = n * (m - n) * y * z;
+                if (den > 0.0) {
+                    const double d = a * z - b * y;
+                    best = fmax(best, d * d / den);
+                }
+            }
+            score[s] = (float)best;
+        }
+    }
+}
+
+cudaError_t launch_marginal(const uint32_t *planes, int n_snps, int Wp, int W0, float *score,
+                            int num_sms, cudaStream_t stream) {
+    if (n_snps <= 0) return cudaSuccess;
+    marginal_kernel<<<num_sms * 4, 256, 0, stream>>>(planes, n_snps, Wp, W0, score);
+    return cudaGetLastError();
+}
+
 }  // namespace gepi

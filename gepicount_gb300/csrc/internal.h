@@ -16,6 +16,8 @@ namespace gepi {
 
 cudaError_t launch_decode_bed(const uint8_t *bed_payload, size_t bps, int n_snps,
                               const int32_t *perm, int Wp, uint32_t *planes, cudaStream_t stream);
+cudaError_t launch_marginal(const uint32_t *planes, int n_snps, int Wp, int W0, float *score,
+                            int num_sms, cudaStream_t stream);
 cudaError_t launch_decode_rows(const uint64_t *bits, const uint64_t *valid, int nw, int n_snps,
                                const int32_t *perm, int Wp, uint32_t *planes,
                                cudaStream_t stream, int num_sms);
@@ -94,6 +96,7 @@ struct gepi_planes {
     int n_snps = 0, S0 = 0, S1 = 0, W0 = 0, W1 = 0, Wp = 0;
     uint32_t *d_planes = nullptr;
     uint32_t *d_tc_blocks = nullptr;  // block-major copy for the tensor-core kernel (lazy)
+    std::vector<float> marginal;      // per-SNP marginal phi^2 (lazy; orders scan tiles)
     cudaStream_t stream = nullptr;
     uint64_t *d_T = nullptr;
     int F = 0;

@@ -195,6 +195,67 @@ void build_tiles(int a0, int a1, int b0, int b1, int TA, int TB, bool triangle, 
     }
 }
 
+// Per-SNP marginal association (computed once per plane set).
+gepi_status ensure_marginal(gepi_planes *pl) {
+    if (!pl->marginal.empty() || pl->n_snps <= 0) return GEPI_OK;
+    float *d = nullptr;
+    GEPI_CUDA(cudaMalloc(&d, sizeof(float) * (size_t)pl->n_snps));
+    std::vector<float> h((size_t)pl->n_snps);
+    cudaError_t e = launch_marginal(pl->d_planes, pl->n_snps, pl->Wp, pl->W0, d, pl->num_sms, pl->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h.data(), d, sizeof(float) * h.size(), cudaMemcpyDeviceToHost, pl->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(pl->stream);
+    cudaFree(d);
+    GEPI_CUDA(e);
+    pl->marginal.swap(h);
+    return GEPI_OK;
+}
+
+// Tiles holding a pair of one of the kHotSnps SNPs with the strongest marginal
+// association go first: tests of such pairs tend to rank high (a function of
+// two rows follows the stronger row), so the threshold reaches close to its
+// final value within a few percent of the tiles and the bounds reject most of
+// the rest.  The hot A tiles run B-tile-major (each B tile fetched once for
+// all of them), then the hot B tiles, then every other tile in band order.
+// The ranked result does not depend on the order.
+constexpr int kHotSnps = 16;
+constexpr size_t kHotMinTiles = 4096;  // smaller scans keep the band order
+
+void hot_first_tiles(std::vector<int2> &tiles, const std::vector<float> &score, int a0, int a1,
+                     int b0, int b1, int TA, int TB) {
+    const int lo = std::min(a0, b0), hi = std::max(a1, b1);
+    std::vector<int> idx;
+    for (int snp = lo; snp < hi; ++snp)
+        if (score[(size_t)snp] > 0.f) idx.push_back(snp);
+    if (idx.empty()) return;
+    const size_t P = std::min<size_t>(kHotSnps, idx.size());
+    std::nth_element(idx.begin(), idx.begin() + (P - 1), idx.end(), [&](int x, int y) {
+        return score[(size_t)x] != score[(size_t)y] ? score[(size_t)x] > score[(size_t)y] : x < y;
+    });
+    std::vector<char> hotA((size_t)(a1 - a0 + TA - 1) / TA, 0), hotB((size_t)(b1 - b0 + TB - 1) / TB, 0);
+    for (size_t q = 0; q < P; ++q) {
+        const int snp = idx[q];
+        if (snp >= a0 && snp < a1) hotA[(size_t)((snp - a0) / TA)] = 1;
+        if (snp >= b0 && snp < b1) hotB[(size_t)((snp - b0) / TB)] = 1;
+    }
+    std::vector<int2> rows, cols, rest;
+    for (const int2 &t : tiles) {
+        if (hotA[(size_t)t.x]) rows.push_back(t);
+        else if (hotB[(size_t)t.y]) cols.push_back(t);
+        else rest.push_back(t);
+    }
+    std::sort(rows.begin(), rows.end(), [](const int2 &p, const int2 &q) {
+        return p.y != q.y ? p.y < q.y : p.x < q.x;
+    });
+    std::sort(cols.begin(), cols.end(), [](const int2 &p, const int2 &q) {
+        return p.x != q.x ? p.x < q.x : p.y < q.y;
+    });
+    tiles.clear();
+    tiles.insert(tiles.end(), rows.begin(), rows.end());
+    tiles.insert(tiles.end(), cols.begin(), cols.end());
+    tiles.insert(tiles.end(), rest.begin(), rest.end());
+}
+
 gepi_status ensure_events(gepi_planes *pl, size_t n) {
     while (pl->ev.size() < n) {
         cudaEvent_t e;
@@ -404,6 +465,12 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
     const int TB = tc ? tc_tile_b_snps() : popc_tile_snps();
     std::vector<int2> tiles;
     build_tiles(a0, a0 + na, b0, b0 + nb, TA, TB, true, tile_band(TA), tiles);
+    // progress snapshots cover band prefixes, so they keep the band order
+    const bool with_snapshots = prog && prog->fn;
+    if (!with_snapshots && tiles.size() >= kHotMinTiles) {
+        GEPI_TRY(ensure_marginal(pl));
+        hot_first_tiles(tiles, pl->marginal, a0, a0 + na, b0, b0 + nb, TA, TB);
+    }
     GEPI_TRY(upload_tiles(pl, tiles));
     GEPI_TRY(ensure_events(pl, 4));
     gepi_scan_stats &S = pl->stats;

@@ -43,26 +43,27 @@
 // 128 B, row-group stride 1536 B), the packed ring (8 slots), the epilogue
 // exchange rows and pair queues.
 //
-// Warp roles (26 warps per CTA, the pair striding over the tile list):
+// Warp roles (18 warps per CTA, the pair striding over the tile list):
 //   producers  warps 0-7 share every chunk: warp q + 4h (lane quarter q)
 //              expands words 6h..6h+5 of packed A row 30q+lane (lane < 30);
 //              warps 0-5 also expand six words of one of the 96 B rows
 //              (thread t: row t % 96, words 6 (t / 96) ..); stages alternate
 //              between chunks
-//   epilogue   warps 8-23 (four per lane quarter, each 16 B SNPs): load their
+//   epilogue   warps 8-15 (two per lane quarter, each 32 B SNPs): load their
 //              part of the accumulator (tcgen05.ld), exchange the three A
 //              planes of a SNP through shared memory, bound every SNP pair per
 //              row pair (one chi^2 bound covers a row pair's five tests, for
 //              either objective) and queue the few that may pass; the warp then
 //              runs the per-test bounds and the out-of-line refinement over its
 //              queue densely
-//   MMA        warp 24 of the even CTA, one thread: up to 6 x tcgen05.mma per
+//   MMA        warp 16 of the even CTA, one thread: up to 6 x tcgen05.mma per
 //              chunk, commits (multicast to both CTAs' barriers)
-//   TMA        warp 25, one thread: two bulk copies per chunk
+//   TMA        warp 17, one thread: two bulk copies per chunk
 // mbarriers: pfull[j] (copy transaction bytes) / pempty[j] (8 producer warps)
 // per ring slot of each CTA; full[s] (even CTA: 16 producer warps of the pair)
-// / empty[s] (commit, both CTAs) per stage; dfull (commit, both CTAs) / dempty
-// (even CTA: 32 epilogue warps of the pair) for the accumulator.
+// / empty[s] (commit, both CTAs) per stage; dfull[c] (commit, both CTAs) /
+// dempty[c] (even CTA: 16 epilogue warps of the pair) per class half c of the
+// accumulator: the scoring warps copy class 0 out while class 1 accumulates.
 // Every wait is bounded by a clock budget; on expiry the kernel records an
 // error, drains its own MMAs and copies, meets its peer at the final cluster
 // barrier, frees its tensor memory and returns.
@@ -94,15 +95,16 @@ constexpr int kTcAStageBytes = (128 / 8) * kTcSbo;        // 24,576 (M = 128 row
 constexpr int kTcPABytes = kTcARows * kTcChunkWords * 4;  // 5,760
 constexpr int kTcPBBytes = kTcBRows * kTcChunkWords * 4;  // 4,608
 constexpr int kTcPStageBytes = kTcPABytes + kTcPBBytes;   // 10,368
-constexpr int kTcXPitch = 98;                      // exchange row pitch (16-bit counts): 49 words
 constexpr int kTcMaxClass = 65535;                 // class sizes the 16-bit exchange holds
-constexpr int kTcThreads = 26 * 32;
+constexpr int kTcEpiWarps = 8;                     // scoring warps: two per lane quarter
+constexpr int kTcThreads = (8 + kTcEpiWarps + 2) * 32;
 constexpr int kTcProducerWarps = 8;                // warps 0-7
 constexpr int kTcBWarps = 2 * kTcBRows / 32;       // warps 0-5 also expand B
-constexpr int kTcEpiWarp0 = 8;                     // epilogue warps 8-23
-constexpr int kTcEpiWarps = 16;
-constexpr int kTcMmaWarp = 24;
-constexpr int kTcTmaWarp = 25;
+constexpr int kTcEpiWarp0 = 8;                     // epilogue warps 8-15
+constexpr int kTcEpiGroups = kTcBSnps / 8 / (kTcEpiWarps / 4);  // groups of 8 B SNPs a warp scores: 4
+constexpr int kTcMmaWarp = kTcEpiWarp0 + kTcEpiWarps;          // 16
+constexpr int kTcTmaWarp = kTcMmaWarp + 1;                     // 17
+constexpr int kTcXPitch = 48 * kTcEpiGroups + 2;   // exchange row pitch (16-bit counts): 97 words
 constexpr uint32_t kTcCols = 512;
 constexpr uint32_t kTcDCols = 2 * kTcN;            // the accumulator (both classes): 384
 constexpr uint32_t kTcACol = kTcDCols;             // 384: first A stage
@@ -703,10 +705,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
         }
         __syncwarp();
     } else {
-        // ---------------- epilogue (warps 8-23) ----------------
+        // ---------------- epilogue (warps 8-15) ----------------
         const int q = warp & 3;                   // TMEM lane quarter
-        const int ew = warp - kTcEpiWarp0;        // 0..15
-        const int eh = ew >> 2;                   // B SNPs 16 eh .. 16 eh + 15
+        const int ew = warp - kTcEpiWarp0;        // 0..7
+        const int eh = ew >> 2;                   // B SNPs 32 eh .. 32 eh + 31
         // this warp's accumulator region as 16-bit counts: row = TMEM lane,
         // [group 0: class 0 (24), class 1 (24) | group 1: ...] (odd word pitch)
         uint16_t *xh = reinterpret_cast<uint16_t *>(tc_smem + kTcXOff) + (size_t)ew * 32 * kTcXPitch;
@@ -720,8 +722,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
         for (int t = pair; t < ntiles && live; t += npairs, ++lt) {
             const int2 tl = tiles[t];
             const int sA = a0 + tl.x * kTcPairASnps + aoff + i;
-            const int sB0 = b0 + tl.y * kTcBSnps + 16 * eh;
-            const uint32_t tq = tbase + ((uint32_t)(32 * q) << 16) + 48 * eh;
+            const int sB0 = b0 + tl.y * kTcBSnps + 8 * kTcEpiGroups * eh;
+            const uint32_t tq = tbase + ((uint32_t)(32 * q) << 16) + 24 * kTcEpiGroups * eh;
             // copy each class half out as soon as its MMAs are done and hand it
             // back: the tensor pipe goes on with the other half, then the next tile
             for (int cls = 0; cls < 2; ++cls) {
@@ -731,7 +733,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
                 }
                 tc_fence_after();
 #pragma unroll
-                for (int gl = 0; gl < 2; ++gl) {
+                for (int gl = 0; gl < kTcEpiGroups; ++gl) {
                     uint32_t v[24];
                     tmem_ld16(tq + cls * kTcN + 24 * gl, *reinterpret_cast<uint32_t(*)[16]>(v));
                     tmem_ld8(tq + cls * kTcN + 24 * gl + 16, *reinterpret_cast<uint32_t(*)[8]>(v + 16));
@@ -750,7 +752,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
             if constexpr (DUMP) {
                 if (lane < 30 && sA < a1) {
                     const uint16_t *xr = xh + lane * kTcXPitch;
-                    for (int jb = 0; jb < 16; ++jb) {
+                    for (int jb = 0; jb < 8 * kTcEpiGroups; ++jb) {
                         const int sBt = sB0 + jb;
                         if (sBt >= b1) continue;
                         const int gl = jb >> 3, jl = jb & 7;
@@ -764,7 +766,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
                 }
                 __syncwarp();
             }
-            for (int gl = 0; gl < 2 && !DUMP; ++gl) {
+            for (int gl = 0; gl < kTcEpiGroups && !DUMP; ++gl) {
                 const uint16_t *xg = xh + 48 * gl;
                 // Phase 1: every lane bounds its SNP pairs (i, jl), jl = p + 3r, and
                 // queues those with a row pair that may pass.  Phase 2: the warp

@@ -83,7 +83,9 @@ struct TileList {
     int refs = 0;
     uint64_t stamp = 0;  // last use, for eviction
 };
-using TileKey = std::array<int, 6>;
+// (a0, a1, b0, b1, TA, TB, plane-set serial): the order puts the plane set's
+// strongest marginal SNPs first, so lists are kept per plane set
+using TileKey = std::array<int64_t, 7>;
 
 // Device resources of one request, pooled by candidate capacity.
 struct JobBuffers {
@@ -225,7 +227,8 @@ gepi_status Engine::prepare(Job &j) {
     j.TA = j.tc ? tc_tile_a_snps() : popc_tile_snps();
     j.TB = j.tc ? tc_tile_b_snps() : popc_tile_snps();
 
-    const TileKey key{rq.a0, rq.a0 + rq.na, rq.b0, rq.b0 + rq.nb, j.TA, j.TB};
+    const TileKey key{rq.a0, (int64_t)rq.a0 + rq.na, rq.b0, (int64_t)rq.b0 + rq.nb, j.TA, j.TB,
+                      (int64_t)pl->serial};
     {
         std::lock_guard<std::mutex> ck(cache_mu_);
         auto it = tiles_.find(key);
@@ -238,7 +241,7 @@ gepi_status Engine::prepare(Job &j) {
     if (!j.tl) {
         // only this thread inserts (prep_mu_ held), so the key is still absent
         std::vector<int2> tiles;
-        pl_build_tiles(key[0], key[1], key[2], key[3], j.TA, j.TB, true, tile_band(j.TA), tiles);
+        GEPI_TRY(pl_scan_tiles(pl, rq.a0, rq.a0 + rq.na, rq.b0, rq.b0 + rq.nb, j.TA, j.TB, true, tiles));
         TileList t;
         t.n = tiles.size();
         if (t.n) {

@@ -90,6 +90,7 @@ gepi_status pl_check_mem(size_t bytes, const char *what);
 
 // The plane-set handle of the C ABI.
 struct gepi_planes {
+    uint64_t serial = 0;  // unique per plane set in the process (keys cached tile orders)
     int device = 0, num_sms = 0;
     int auto_method = 0;  // AUTO's choice for this plane set (0 = not tuned yet)
     float tune_ms[2] = {0.f, 0.f};  // autotuner timings: popcount, tensor core
@@ -120,6 +121,10 @@ namespace gepi {
 gepi_status pl_ensure_tables(gepi_planes *pl);
 gepi_status pl_ensure_tc_blocks(gepi_planes *pl);
 gepi_status pl_resolve_method(gepi_planes *pl, int m, int *out);
+// The tile list of a triangle scan: bands of about 320 A SNPs, and with `hot`
+// the tiles of the strongest marginal SNPs first (large lists only).
+gepi_status pl_scan_tiles(gepi_planes *pl, int a0, int a1, int b0, int b1, int TA, int TB, bool hot,
+                          std::vector<int2> &out);
 void pl_build_tiles(int a0, int a1, int b0, int b1, int TA, int TB, bool triangle, int band,
                     std::vector<int2> &out);
 

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <array>
 #include <chrono>
 #include <cmath>
@@ -193,6 +194,11 @@ void build_tiles(int a0, int a1, int b0, int b1, int TA, int TB, bool triangle, 
             if (triangle && !any) break;
         }
     }
+}
+
+uint64_t next_serial() {
+    static std::atomic<uint64_t> n{0};
+    return ++n;
 }
 
 // Per-SNP marginal association (computed once per plane set).
@@ -464,13 +470,8 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
     const int TA = tc ? tc_tile_a_snps() : popc_tile_snps();
     const int TB = tc ? tc_tile_b_snps() : popc_tile_snps();
     std::vector<int2> tiles;
-    build_tiles(a0, a0 + na, b0, b0 + nb, TA, TB, true, tile_band(TA), tiles);
     // progress snapshots cover band prefixes, so they keep the band order
-    const bool with_snapshots = prog && prog->fn;
-    if (!with_snapshots && tiles.size() >= kHotMinTiles) {
-        GEPI_TRY(ensure_marginal(pl));
-        hot_first_tiles(tiles, pl->marginal, a0, a0 + na, b0, b0 + nb, TA, TB);
-    }
+    GEPI_TRY(pl_scan_tiles(pl, a0, a0 + na, b0, b0 + nb, TA, TB, !(prog && prog->fn), tiles));
     GEPI_TRY(upload_tiles(pl, tiles));
     GEPI_TRY(ensure_events(pl, 4));
     gepi_scan_stats &S = pl->stats;
@@ -670,6 +671,16 @@ gepi_status pl_check_mem(size_t bytes, const char *what) { return check_mem(byte
 gepi_status pl_ensure_tables(gepi_planes *pl) { return ensure_tables(pl); }
 gepi_status pl_ensure_tc_blocks(gepi_planes *pl) { return ensure_tc_blocks(pl); }
 gepi_status pl_resolve_method(gepi_planes *pl, int m, int *out) { return resolve_method(pl, m, out); }
+gepi_status pl_scan_tiles(gepi_planes *pl, int a0, int a1, int b0, int b1, int TA, int TB, bool hot,
+                          std::vector<int2> &out) {
+    build_tiles(a0, a1, b0, b1, TA, TB, true, tile_band(TA), out);
+    if (hot && out.size() >= kHotMinTiles) {
+        GEPI_TRY(ensure_marginal(pl));
+        hot_first_tiles(out, pl->marginal, a0, a1, b0, b1, TA, TB);
+    }
+    return GEPI_OK;
+}
+
 void pl_build_tiles(int a0, int a1, int b0, int b1, int TA, int TB, bool triangle, int band,
                     std::vector<int2> &out) {
     build_tiles(a0, a1, b0, b1, TA, TB, triangle, band, out);
@@ -722,6 +733,7 @@ gepi_status gepi_planes_from_bed(const uint8_t *bed, size_t bed_bytes, int n_bim
     DeviceGuard g(device);
     if (!g.ok) return set_error(GEPI_ERR_CUDA, "cudaSetDevice failed");
     gepi_planes *pl = new gepi_planes();
+    pl->serial = next_serial();
     gepi_status st = planes_alloc(pl, device, n_bim_snps, (int)c0.size(), (int)c1.size());
     uint8_t *d_bed = nullptr;
     int32_t *d_perm = nullptr;
@@ -778,6 +790,7 @@ gepi_status gepi_planes_from_rows(const uint64_t *bits, const uint64_t *valid, i
     DeviceGuard g(device);
     if (!g.ok) return set_error(GEPI_ERR_CUDA, "cudaSetDevice failed");
     gepi_planes *pl = new gepi_planes();
+    pl->serial = next_serial();
     gepi_status st = planes_alloc(pl, device, n_snps, (int)c0.size(), (int)c1.size());
     uint64_t *d_bits = nullptr, *d_valid = nullptr;
     int32_t *d_perm = nullptr;

@@ -227,10 +227,72 @@ gepi_status ensure_marginal(gepi_planes *pl) {
 constexpr int kHotSnps = 16;
 constexpr size_t kHotMinTiles = 4096;  // smaller scans keep the band order
 
-void hot_first_tiles(std::vector<int2> &tiles, const std::vector<float> &score, int a0, int a1,
-                     int b0, int b1, int TA, int TB) {
+// The triangle scan's tile list in that order, generated directly (counted
+// and reserved first: no sort, no partition).  Empty hot sets give the plain
+// band order of build_tiles.
+void scan_tile_order(int a0, int a1, int b0, int b1, int TA, int TB, int band,
+                     const std::vector<int> &hot_a, const std::vector<int> &hot_b,
+                     std::vector<int2> &out) {
+    out.clear();
+    const int nat = (a1 - a0 + TA - 1) / TA, nbt = (b1 - b0 + TB - 1) / TB;
+    if (nat <= 0 || nbt <= 0) return;
+    if (band < 1) band = 1;
+    // B tiles j < jend[i] pair with A tile i (t <= s somewhere in the tile)
+    std::vector<int> jend((size_t)nat);
+    size_t total = 0;
+    for (int i = 0; i < nat; ++i) {
+        const int smax = std::min(a0 + i * TA + TA - 1, a1 - 1);
+        const int e = smax < b0 ? 0 : (smax - b0) / TB + 1;
+        jend[(size_t)i] = std::min(nbt, e);
+        total += (size_t)jend[(size_t)i];
+    }
+    out.reserve(total);
+    std::vector<char> isa((size_t)nat, 0), isb((size_t)nbt, 0);
+    for (int i : hot_a) isa[(size_t)i] = 1;
+    for (int j : hot_b) isb[(size_t)j] = 1;
+    for (int j = 0; j < nbt; ++j)
+        for (int i : hot_a)
+            if (j < jend[(size_t)i]) out.push_back(make_int2(i, j));
+    for (int i = 0; i < nat; ++i)
+        if (!isa[(size_t)i])
+            for (int j : hot_b)
+                if (j < jend[(size_t)i]) out.push_back(make_int2(i, j));
+    // the remaining tiles, band by band: counted, then filled in parallel
+    const int nbands = (nat + band - 1) / band;
+    std::vector<size_t> off((size_t)nbands + 1, 0);
+    for (int b = 0; b < nbands; ++b) {
+        size_t c = 0;
+        for (int i = b * band; i < std::min(nat, (b + 1) * band); ++i) {
+            if (isa[(size_t)i]) continue;
+            const int e = jend[(size_t)i];
+            c += (size_t)(e - (int)(std::lower_bound(hot_b.begin(), hot_b.end(), e) - hot_b.begin()));
+        }
+        off[(size_t)b + 1] = off[(size_t)b] + c;
+    }
+    const size_t base = out.size();
+    out.resize(base + off[(size_t)nbands]);
+    int2 *dst = out.data() + base;
+#pragma omp parallel for schedule(dynamic, 16) if (nbands >= 64)
+    for (int b = 0; b < nbands; ++b) {
+        const int i0 = b * band, i1 = std::min(nat, i0 + band);
+        const int jmax = jend[(size_t)(i1 - 1)];  // the band's last A tile reaches furthest
+        size_t w = off[(size_t)b];
+        for (int j = 0; j < jmax; ++j) {
+            if (isb[(size_t)j]) continue;
+            for (int i = i0; i < i1; ++i)
+                if (!isa[(size_t)i] && j < jend[(size_t)i]) dst[w++] = make_int2(i, j);
+        }
+    }
+}
+
+// The A and B tiles of the kHotSnps strongest marginal SNPs (ascending).
+void hot_tiles(const std::vector<float> &score, int a0, int a1, int b0, int b1, int TA, int TB,
+               std::vector<int> &hot_a, std::vector<int> &hot_b) {
+    hot_a.clear();
+    hot_b.clear();
     const int lo = std::min(a0, b0), hi = std::max(a1, b1);
     std::vector<int> idx;
+    idx.reserve((size_t)(hi - lo));
     for (int snp = lo; snp < hi; ++snp)
         if (score[(size_t)snp] > 0.f) idx.push_back(snp);
     if (idx.empty()) return;
@@ -238,28 +300,15 @@ void hot_first_tiles(std::vector<int2> &tiles, const std::vector<float> &score, 
     std::nth_element(idx.begin(), idx.begin() + (P - 1), idx.end(), [&](int x, int y) {
         return score[(size_t)x] != score[(size_t)y] ? score[(size_t)x] > score[(size_t)y] : x < y;
     });
-    std::vector<char> hotA((size_t)(a1 - a0 + TA - 1) / TA, 0), hotB((size_t)(b1 - b0 + TB - 1) / TB, 0);
     for (size_t q = 0; q < P; ++q) {
         const int snp = idx[q];
-        if (snp >= a0 && snp < a1) hotA[(size_t)((snp - a0) / TA)] = 1;
-        if (snp >= b0 && snp < b1) hotB[(size_t)((snp - b0) / TB)] = 1;
+        if (snp >= a0 && snp < a1) hot_a.push_back((snp - a0) / TA);
+        if (snp >= b0 && snp < b1) hot_b.push_back((snp - b0) / TB);
     }
-    std::vector<int2> rows, cols, rest;
-    for (const int2 &t : tiles) {
-        if (hotA[(size_t)t.x]) rows.push_back(t);
-        else if (hotB[(size_t)t.y]) cols.push_back(t);
-        else rest.push_back(t);
+    for (auto *v : {&hot_a, &hot_b}) {
+        std::sort(v->begin(), v->end());
+        v->erase(std::unique(v->begin(), v->end()), v->end());
     }
-    std::sort(rows.begin(), rows.end(), [](const int2 &p, const int2 &q) {
-        return p.y != q.y ? p.y < q.y : p.x < q.x;
-    });
-    std::sort(cols.begin(), cols.end(), [](const int2 &p, const int2 &q) {
-        return p.x != q.x ? p.x < q.x : p.y < q.y;
-    });
-    tiles.clear();
-    tiles.insert(tiles.end(), rows.begin(), rows.end());
-    tiles.insert(tiles.end(), cols.begin(), cols.end());
-    tiles.insert(tiles.end(), rest.begin(), rest.end());
 }
 
 gepi_status ensure_events(gepi_planes *pl, size_t n) {
@@ -673,11 +722,14 @@ gepi_status pl_ensure_tc_blocks(gepi_planes *pl) { return ensure_tc_blocks(pl); 
 gepi_status pl_resolve_method(gepi_planes *pl, int m, int *out) { return resolve_method(pl, m, out); }
 gepi_status pl_scan_tiles(gepi_planes *pl, int a0, int a1, int b0, int b1, int TA, int TB, bool hot,
                           std::vector<int2> &out) {
-    build_tiles(a0, a1, b0, b1, TA, TB, true, tile_band(TA), out);
-    if (hot && out.size() >= kHotMinTiles) {
+    std::vector<int> hot_a, hot_b;
+    // at least about kHotMinTiles tiles in the triangle
+    const double est = 0.5 * (double)(a1 - a0) * (double)(b1 - b0) / ((double)TA * TB);
+    if (hot && est >= (double)kHotMinTiles) {
         GEPI_TRY(ensure_marginal(pl));
-        hot_first_tiles(out, pl->marginal, a0, a1, b0, b1, TA, TB);
+        hot_tiles(pl->marginal, a0, a1, b0, b1, TA, TB, hot_a, hot_b);
     }
+    scan_tile_order(a0, a1, b0, b1, TA, TB, tile_band(TA), hot_a, hot_b, out);
     return GEPI_OK;
 }
 

@@ -83,6 +83,21 @@ void dfree(T *&p) {
     p = nullptr;
 }
 
+// Plane-set memory (planes, operand blocks, candidate buffers, staging) comes
+// from one stream-ordered pool per device that keeps freed memory for reuse
+// (scan.cu): building plane sets over and over (one per cohort, request or
+// step) then costs no cudaMalloc / cudaFree of hundreds of MB each time.
+cudaError_t pool_alloc(int device, void **p, size_t bytes, cudaStream_t s);
+template <class T>
+cudaError_t pool_alloc(int device, T **p, size_t bytes, cudaStream_t s) {
+    return pool_alloc(device, reinterpret_cast<void **>(p), bytes, s);
+}
+template <class T>
+void pool_free(T *&p, cudaStream_t s) {
+    if (p) cudaFreeAsync(p, s);
+    p = nullptr;
+}
+
 
 // Plane-set helpers (scan.cu).
 gepi_status pl_check_mem(size_t bytes, const char *what);

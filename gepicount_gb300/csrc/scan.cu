@@ -42,9 +42,45 @@ using namespace gepi;
 
 namespace {
 
+// Bytes the pool keeps after frees (kPoolKeep at most).
+constexpr uint64_t kPoolKeep = 8ull << 30;
+
+cudaMemPool_t device_pool(int device) {
+    static std::mutex mu;
+    static std::map<int, cudaMemPool_t> pools;
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = pools.find(device);
+    if (it != pools.end()) return it->second;
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    cudaMemPool_t p = nullptr;
+    if (cudaMemPoolCreate(&p, &props) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    uint64_t keep = kPoolKeep;
+    cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+    pools[device] = p;
+    return p;
+}
+
+// Memory the pool holds unused (counts as free).
+size_t pool_idle_bytes(int device) {
+    cudaMemPool_t p = device_pool(device);
+    uint64_t res = 0, used = 0;
+    if (!p || cudaMemPoolGetAttribute(p, cudaMemPoolAttrReservedMemCurrent, &res) != cudaSuccess ||
+        cudaMemPoolGetAttribute(p, cudaMemPoolAttrUsedMemCurrent, &used) != cudaSuccess)
+        return 0;
+    return res > used ? (size_t)(res - used) : 0;
+}
+
 gepi_status check_mem(size_t bytes, const char *what) {
     size_t fr = 0, tot = 0;
     if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return GEPI_OK;
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess) fr += pool_idle_bytes(dev);
     if (bytes + (64u << 20) > fr)
         return set_error(GEPI_ERR_OOM, std::string(what) + ": needs " + std::to_string(bytes >> 20) +
                                            " MiB, " + std::to_string(fr >> 20) + " MiB free");
@@ -73,21 +109,23 @@ gepi_status planes_alloc(gepi_planes *pl, int device, int n_snps, int S0, int S1
     GEPI_CUDA(cudaStreamCreateWithFlags(&pl->stream, cudaStreamNonBlocking));
     size_t bytes = (size_t)n_snps * 3 * pl->Wp * 4;
     GEPI_TRY(check_mem(bytes, "genotype planes"));
-    GEPI_CUDA(cudaMalloc(&pl->d_planes, bytes));
+    GEPI_CUDA(pool_alloc(device, &pl->d_planes, bytes, pl->stream));
     return GEPI_OK;
 }
 
 void planes_free(gepi_planes *pl) {
     if (!pl) return;
     DeviceGuard g(pl->device);
-    if (pl->stream) cudaStreamSynchronize(pl->stream);
-    dfree(pl->d_planes);
-    dfree(pl->d_tc_blocks);
+    if (pl->stream) {
+        pool_free(pl->d_planes, pl->stream);
+        pool_free(pl->d_tc_blocks, pl->stream);
+        pool_free(pl->d_cand[0], pl->stream);
+        pool_free(pl->d_cand[1], pl->stream);
+        cudaStreamSynchronize(pl->stream);
+    }
     dfree(pl->d_T);
     dfree(pl->d_lf);
     dfree(pl->d_lf32);
-    dfree(pl->d_cand[0]);
-    dfree(pl->d_cand[1]);
     dfree(pl->d_state);
     dfree(pl->d_sel);
     dfree(pl->d_tiles);
@@ -126,18 +164,18 @@ gepi_status ensure_scan_buffers(gepi_planes *pl, int k) {
         long long v = std::atoll(e);
         if (v > 0) want = std::max<uint64_t>((uint64_t)v, 4ull * (uint64_t)k);
         if (pl->cap != want) {
-            dfree(pl->d_cand[0]);
-            dfree(pl->d_cand[1]);
+            pool_free(pl->d_cand[0], pl->stream);
+            pool_free(pl->d_cand[1], pl->stream);
             pl->cap = 0;
         }
     }
     if (want > (1ull << 31)) return set_error(GEPI_ERR_LIMIT, "topmost too large");
     if (pl->cap < want) {
-        dfree(pl->d_cand[0]);
-        dfree(pl->d_cand[1]);
+        pool_free(pl->d_cand[0], pl->stream);
+        pool_free(pl->d_cand[1], pl->stream);
         GEPI_TRY(check_mem(2 * want * sizeof(Cand), "candidate buffers"));
-        GEPI_CUDA(cudaMalloc(&pl->d_cand[0], want * sizeof(Cand)));
-        GEPI_CUDA(cudaMalloc(&pl->d_cand[1], want * sizeof(Cand)));
+        GEPI_CUDA(pool_alloc(pl->device, &pl->d_cand[0], want * sizeof(Cand), pl->stream));
+        GEPI_CUDA(pool_alloc(pl->device, &pl->d_cand[1], want * sizeof(Cand), pl->stream));
         pl->cap = (uint32_t)want;
     }
     if (!pl->d_state) GEPI_CUDA(cudaMalloc(&pl->d_state, sizeof(ScanState)));
@@ -169,7 +207,7 @@ gepi_status ensure_tc_blocks(gepi_planes *pl) {
     if (pl->d_tc_blocks) return GEPI_OK;
     const size_t bytes = tc_block_words(pl->n_snps, pl->Wp, pl->W0) * 4;
     GEPI_TRY(check_mem(bytes, "tensor-core operand blocks"));
-    GEPI_CUDA(cudaMalloc(&pl->d_tc_blocks, bytes));
+    GEPI_CUDA(pool_alloc(pl->device, &pl->d_tc_blocks, bytes, pl->stream));
     GEPI_CUDA(launch_tc_relayout(pl->d_planes, pl->Wp, pl->W0, pl->n_snps, pl->d_tc_blocks,
                                  pl->num_sms, pl->stream));
     return GEPI_OK;
@@ -715,6 +753,12 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
 }  // namespace
 
 namespace gepi {
+cudaError_t pool_alloc(int device, void **ptr, size_t bytes, cudaStream_t s) {
+    cudaMemPool_t p = device_pool(device);
+    if (!p) return cudaErrorMemoryAllocation;
+    return cudaMallocFromPoolAsync(ptr, bytes, p, s);
+}
+
 
 gepi_status pl_check_mem(size_t bytes, const char *what) { return check_mem(bytes, what); }
 gepi_status pl_ensure_tables(gepi_planes *pl) { return ensure_tables(pl); }
@@ -790,8 +834,8 @@ gepi_status gepi_planes_from_bed(const uint8_t *bed, size_t bed_bytes, int n_bim
     uint8_t *d_bed = nullptr;
     int32_t *d_perm = nullptr;
     auto fail = [&](gepi_status s) {
-        if (d_bed) cudaFree(d_bed);
-        if (d_perm) cudaFree(d_perm);
+        pool_free(d_bed, pl->stream);
+        pool_free(d_perm, pl->stream);
         planes_free(pl);
         delete pl;
         return s;
@@ -801,8 +845,9 @@ gepi_status gepi_planes_from_bed(const uint8_t *bed, size_t bed_bytes, int n_bim
     build_perm(c0, c1, pl->W0, pl->Wp, perm);
     const size_t payload = bed_bytes - 3;
     if ((st = check_mem(payload + perm.size() * 4, ".bed staging")) != GEPI_OK) return fail(st);
-    if (cudaMalloc(&d_bed, payload) != cudaSuccess || cudaMalloc(&d_perm, perm.size() * 4) != cudaSuccess)
-        return fail(set_error(GEPI_ERR_OOM, "cudaMalloc .bed staging failed"));
+    if (pool_alloc(device, &d_bed, payload, pl->stream) != cudaSuccess ||
+        pool_alloc(device, &d_perm, perm.size() * 4, pl->stream) != cudaSuccess)
+        return fail(set_error(GEPI_ERR_OOM, ".bed staging allocation failed"));
     cudaError_t e = cudaMemcpyAsync(d_bed, bed + 3, payload, cudaMemcpyHostToDevice, pl->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(d_perm, perm.data(), perm.size() * 4, cudaMemcpyHostToDevice, pl->stream);
@@ -811,8 +856,8 @@ gepi_status gepi_planes_from_bed(const uint8_t *bed, size_t bed_bytes, int n_bim
     if (e == cudaSuccess) e = cudaStreamSynchronize(pl->stream);
     if (e != cudaSuccess)
         return fail(set_error(GEPI_ERR_CUDA, std::string("decode: ") + cudaGetErrorString(e)));
-    cudaFree(d_bed);
-    cudaFree(d_perm);
+    pool_free(d_bed, pl->stream);
+    pool_free(d_perm, pl->stream);
     *out = pl;
     return GEPI_OK;
 }
@@ -847,9 +892,9 @@ gepi_status gepi_planes_from_rows(const uint64_t *bits, const uint64_t *valid, i
     uint64_t *d_bits = nullptr, *d_valid = nullptr;
     int32_t *d_perm = nullptr;
     auto fail = [&](gepi_status s) {
-        if (d_bits) cudaFree(d_bits);
-        if (d_valid) cudaFree(d_valid);
-        if (d_perm) cudaFree(d_perm);
+        pool_free(d_bits, pl->stream);
+        pool_free(d_valid, pl->stream);
+        pool_free(d_perm, pl->stream);
         planes_free(pl);
         delete pl;
         return s;
@@ -859,9 +904,10 @@ gepi_status gepi_planes_from_rows(const uint64_t *bits, const uint64_t *valid, i
     build_perm(c0, c1, pl->W0, pl->Wp, perm);
     const size_t rb = (size_t)n_rows * n_words * 8;
     if ((st = check_mem(2 * rb + perm.size() * 4, "row staging")) != GEPI_OK) return fail(st);
-    if (cudaMalloc(&d_bits, rb) != cudaSuccess || cudaMalloc(&d_valid, rb) != cudaSuccess ||
-        cudaMalloc(&d_perm, perm.size() * 4) != cudaSuccess)
-        return fail(set_error(GEPI_ERR_OOM, "cudaMalloc row staging failed"));
+    if (pool_alloc(device, &d_bits, rb, pl->stream) != cudaSuccess ||
+        pool_alloc(device, &d_valid, rb, pl->stream) != cudaSuccess ||
+        pool_alloc(device, &d_perm, perm.size() * 4, pl->stream) != cudaSuccess)
+        return fail(set_error(GEPI_ERR_OOM, "row staging allocation failed"));
     cudaError_t e = cudaMemcpyAsync(d_bits, bits, rb, cudaMemcpyHostToDevice, pl->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_valid, valid, rb, cudaMemcpyHostToDevice, pl->stream);
     if (e == cudaSuccess)
@@ -872,9 +918,9 @@ gepi_status gepi_planes_from_rows(const uint64_t *bits, const uint64_t *valid, i
     if (e == cudaSuccess) e = cudaStreamSynchronize(pl->stream);
     if (e != cudaSuccess)
         return fail(set_error(GEPI_ERR_CUDA, std::string("decode rows: ") + cudaGetErrorString(e)));
-    cudaFree(d_bits);
-    cudaFree(d_valid);
-    cudaFree(d_perm);
+    pool_free(d_bits, pl->stream);
+    pool_free(d_valid, pl->stream);
+    pool_free(d_perm, pl->stream);
     *out = pl;
     return GEPI_OK;
 }

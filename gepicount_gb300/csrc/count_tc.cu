@@ -44,21 +44,21 @@
 // exchange rows and pair queues.
 //
 // Warp roles (18 warps per CTA, the pair striding over the tile list):
-//   producers  warps 0-7 share every chunk: warp q + 4h (lane quarter q)
-//              expands words 6h..6h+5 of packed A row 30q+lane (lane < 30);
-//              warps 0-5 also expand six words of one of the 96 B rows
+//   MMA        warp 0 of the even CTA, one thread: up to 6 x tcgen05.mma per
+//              chunk, commits (multicast to both CTAs' barriers)
+//   TMA        warp 1, one thread: two bulk copies per chunk
+//   producers  warps 2-9 share every chunk: the warp of lane quarter q and half
+//              h expands words 6h..6h+5 of packed A row 30q+lane (lane < 30);
+//              the first six also expand six words of one of the 96 B rows
 //              (thread t: row t % 96, words 6 (t / 96) ..); stages alternate
 //              between chunks
-//   epilogue   warps 8-15 (two per lane quarter, each 32 B SNPs): load their
+//   epilogue   warps 10-17 (two per lane quarter, each 32 B SNPs): load their
 //              part of the accumulator (tcgen05.ld), exchange the three A
 //              planes of a SNP through shared memory, bound every SNP pair per
 //              row pair (one chi^2 bound covers a row pair's five tests, for
 //              either objective) and queue the few that may pass; the warp then
 //              runs the per-test bounds and the out-of-line refinement over its
 //              queue densely
-//   MMA        warp 16 of the even CTA, one thread: up to 6 x tcgen05.mma per
-//              chunk, commits (multicast to both CTAs' barriers)
-//   TMA        warp 17, one thread: two bulk copies per chunk
 // mbarriers: pfull[j] (copy transaction bytes) / pempty[j] (8 producer warps)
 // per ring slot of each CTA; full[s] (even CTA: 16 producer warps of the pair)
 // / empty[s] (commit, both CTAs) per stage; dfull[c] (commit, both CTAs) /
@@ -98,12 +98,15 @@ constexpr int kTcPStageBytes = kTcPABytes + kTcPBBytes;   // 10,368
 constexpr int kTcMaxClass = 65535;                 // class sizes the 16-bit exchange holds
 constexpr int kTcEpiWarps = 8;                     // scoring warps: two per lane quarter
 constexpr int kTcThreads = (8 + kTcEpiWarps + 2) * 32;
-constexpr int kTcProducerWarps = 8;                // warps 0-7
-constexpr int kTcBWarps = 2 * kTcBRows / 32;       // warps 0-5 also expand B
-constexpr int kTcEpiWarp0 = 8;                     // epilogue warps 8-15
+constexpr int kTcProducerWarps = 8;
+constexpr int kTcBWarps = 2 * kTcBRows / 32;       // the first 6 producer warps also expand B
+// The issuing warps come first: the schedulers favour lower-numbered (older)
+// warps, and the single MMA thread is on every chunk's critical path.
+constexpr int kTcMmaWarp = 0;
+constexpr int kTcTmaWarp = 1;
+constexpr int kTcProdWarp0 = 2;                    // producer warps 2-9
+constexpr int kTcEpiWarp0 = kTcProdWarp0 + kTcProducerWarps;  // epilogue warps 10-17
 constexpr int kTcEpiGroups = kTcBSnps / 8 / (kTcEpiWarps / 4);  // groups of 8 B SNPs a warp scores: 4
-constexpr int kTcMmaWarp = kTcEpiWarp0 + kTcEpiWarps;          // 16
-constexpr int kTcTmaWarp = kTcMmaWarp + 1;                     // 17
 constexpr int kTcXPitch = 48 * kTcEpiGroups + 2;   // exchange row pitch (16-bit counts): 97 words
 constexpr uint32_t kTcCols = 512;
 constexpr uint32_t kTcDCols = 2 * kTcN;            // the accumulator (both classes): 384
@@ -534,18 +537,18 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
     cluster_sync_all();
     tc_fence_after();
 
-    if (warp < kTcProducerWarps) {
+    if (warp >= kTcProdWarp0 && warp < kTcEpiWarp0) {
         // ---------------- producers ----------------
         constexpr int HW = kTcHalfWords;
         const int q = warp & 3;             // TMEM lane quarter
-        const int h = warp >> 2;            // words HW h .. HW h + HW - 1 of each A row
+        const int h = (warp - kTcProdWarp0) >> 2;  // words HW h .. HW h + HW - 1 of each A row
         const bool arow = lane < 30;
         const int arow_off = (30 * q + (arow ? lane : 29)) * (kTcChunkWords * 4);
         const uint32_t ta0 = tbase + ((uint32_t)(32 * q) << 16) + kTcACol + 4 * HW * h;
         // B piece of warps 0-5: row u = t % 96, words HW hb .. HW hb + HW - 1
         // (consecutive lanes on consecutive rows: conflict-free 16-byte stores)
-        const bool has_b = warp < kTcBWarps;
-        const int t8 = 32 * warp + lane;
+        const bool has_b = warp - kTcProdWarp0 < kTcBWarps;
+        const int t8 = 32 * (warp - kTcProdWarp0) + lane;
         const int u = t8 % kTcBRows, hb = t8 / kTcBRows;
         unsigned char *bst0 = tc_smem + (u >> 3) * kTcSbo + (HW * hb) * kTcLbo + (u & 7) * 16;
         // the shared-memory A stage: row 32q + lane (the tensor-memory lane of
@@ -705,7 +708,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
         }
         __syncwarp();
     } else {
-        // ---------------- epilogue (warps 8-15) ----------------
+        // ---------------- epilogue (warps 10-17) ----------------
         const int q = warp & 3;                   // TMEM lane quarter
         const int ew = warp - kTcEpiWarp0;        // 0..7
         const int eh = ew >> 2;                   // B SNPs 32 eh .. 32 eh + 31
@@ -716,6 +719,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
         const int i = lane / 3, p = lane % 3;
         const float theta = DUMP ? 0.f : ctx.st->theta;
         const float lp_thr = DUMP ? 0.f : ctx.st->lp_thr;
+        const int geno = ctx.geno;
         const int aoff = kTcASnps * (int)rank + 10 * q;  // this warp's first A SNP in the tile
         uint32_t lt = 0;
         bool live = true;
@@ -786,7 +790,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
                                 G[pp * 3 + qq] = u16f(xg[(3 * i + pp) * kTcXPitch + 3 * jl + qq]);
                                 G[9 + pp * 3 + qq] = u16f(xg[(3 * i + pp) * kTcXPitch + 24 + 3 * jl + qq]);
                             }
-                        rp = rowpair_bounds(G, G + 9, sA == sBt, OBJ, theta, lp_thr);
+                        rp = rowpair_bounds(G, G + 9, sA == sBt, OBJ, theta, lp_thr, geno);
                     }
                     const uint32_t bal = __ballot_sync(0xffffffffu, rp != 0);
                     if (rp) qu[qn + __popc(bal & ((1u << lane) - 1u))] = ((uint32_t)lane << 8) | ((uint32_t)jl << 4) | rp;

@@ -385,6 +385,7 @@ gepi_status time_count_kernel(gepi_planes *pl, bool tc, int n, float *ms) {
     ctx.lf = pl->d_lf;
     ctx.lf32 = pl->d_lf32;
     ctx.objective = GEPI_ENTROPY;
+    ctx.geno = pl->geno;
     ctx.cap = pl->cap;
     ctx.st = pl->d_state;
     ctx.cand = pl->d_cand[0];
@@ -600,6 +601,7 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
     ctx.lf = pl->d_lf;
     ctx.lf32 = pl->d_lf32;
     ctx.objective = par->objective;
+    ctx.geno = pl->geno;
     ctx.cap = pl->cap;
     ctx.st = pl->d_state;
 
@@ -858,6 +860,7 @@ gepi_status gepi_planes_from_bed(const uint8_t *bed, size_t bed_bytes, int n_bim
         return fail(set_error(GEPI_ERR_CUDA, std::string("decode: ") + cudaGetErrorString(e)));
     pool_free(d_bed, pl->stream);
     pool_free(d_perm, pl->stream);
+    pl->geno = 1;  // .bed calls always set an allele row of a valid sample
     *out = pl;
     return GEPI_OK;
 }
@@ -915,7 +918,16 @@ gepi_status gepi_planes_from_rows(const uint64_t *bits, const uint64_t *valid, i
     if (e == cudaSuccess)
         e = launch_decode_rows(d_bits, d_valid, n_words, n_snps, d_perm, pl->Wp, pl->d_planes,
                                pl->stream, pl->num_sms);
+    // rows handed in need not set an allele row for every valid sample
+    int *d_unc = nullptr;
+    if (e == cudaSuccess) e = pool_alloc(device, &d_unc, sizeof(int), pl->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(d_unc, 0, sizeof(int), pl->stream);
+    if (e == cudaSuccess) e = launch_allele_cover(pl->d_planes, n_snps, pl->Wp, d_unc, pl->num_sms, pl->stream);
+    int h_unc = 1;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h_unc, d_unc, sizeof(int), cudaMemcpyDeviceToHost, pl->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(pl->stream);
+    pool_free(d_unc, pl->stream);
+    pl->geno = h_unc == 0;
     if (e != cudaSuccess)
         return fail(set_error(GEPI_ERR_CUDA, std::string("decode rows: ") + cudaGetErrorString(e)));
     pool_free(d_bits, pl->stream);

@@ -37,10 +37,12 @@
 // Tensor memory (512 columns, one CTA per SM, allocated for the pair): one
 // accumulator of 384 columns (class 0 at +0, class 1 at +192), two A stages of
 // 48 columns (384 E2M1 per lane) and 32 columns of scale factors (all 0x7F).
-// The next tile's MMAs wait for both CTAs' epilogues to have loaded the
-// accumulator.  Shared memory: two B stages of 96 rows x 192 bytes in the
-// SWIZZLE_NONE K-major core-matrix layout (8 rows x 16 B cores, k-group stride
-// 128 B, row-group stride 1536 B), the packed ring (8 slots), the epilogue
+// The accumulator's class halves ping-pong: the scoring warps copy a tile's
+// class-0 half out as soon as its MMAs are done and hand it back while class 1
+// accumulates, so the next tile's MMAs start without draining the tensor pipe.
+// Shared memory: two B stages of 96 rows x 192 bytes in the SWIZZLE_NONE
+// K-major core-matrix layout (8 rows x 16 B cores, k-group stride 128 B,
+// row-group stride 1536 B), the packed ring (4 slots), the scoring warps'
 // exchange rows and pair queues.
 //
 // Warp roles (18 warps per CTA, the pair striding over the tile list):
@@ -52,13 +54,14 @@
 //              the first six also expand six words of one of the 96 B rows
 //              (thread t: row t % 96, words 6 (t / 96) ..); stages alternate
 //              between chunks
-//   epilogue   warps 10-17 (two per lane quarter, each 32 B SNPs): load their
-//              part of the accumulator (tcgen05.ld), exchange the three A
-//              planes of a SNP through shared memory, bound every SNP pair per
-//              row pair (one chi^2 bound covers a row pair's five tests, for
-//              either objective) and queue the few that may pass; the warp then
-//              runs the per-test bounds and the out-of-line refinement over its
-//              queue densely
+//   epilogue   warps 10-17 (two per lane quarter, each 32 B SNPs): copy their
+//              part of each class half of the accumulator (tcgen05.ld) to
+//              shared memory as 16-bit counts and hand it back, then bound
+//              every SNP pair per row pair (one chi^2 bound covers a row
+//              pair's five tests, for either objective; a genotype-cell chi^2
+//              covers all four row pairs first) and queue the few that may
+//              pass; the warp then runs the per-test bounds and the
+//              out-of-line refinement over its queue densely
 // mbarriers: pfull[j] (copy transaction bytes) / pempty[j] (8 producer warps)
 // per ring slot of each CTA; full[s] (even CTA: 16 producer warps of the pair)
 // / empty[s] (commit, both CTAs) per stage; dfull[c] (commit, both CTAs) /
@@ -86,19 +89,17 @@ constexpr int kTcBRows = kTcN / 2;                 // B rows per CTA: 96
 constexpr int kTcChunkWords = 12;                  // 384 samples per chunk (6 MMAs of K = 64)
 constexpr int kTcHalfWords = kTcChunkWords / 2;    // words of a row per producer thread
 constexpr int kTcStages = 2;                       // A/B operand stages
-constexpr int kTcTmemStages = 2;                   // stages with A in tensor memory (the rest: shared)
 constexpr int kTcPStages = 4;                      // packed ring depth
 constexpr int kTcLbo = 128;                        // k-group stride (bytes)
 constexpr int kTcSbo = kTcChunkWords * kTcLbo;     // 8-row group stride: 1,536 bytes
 constexpr int kTcBStageBytes = (kTcBRows / 8) * kTcSbo;   // 18,432
-constexpr int kTcAStageBytes = (128 / 8) * kTcSbo;        // 24,576 (M = 128 rows per CTA)
 constexpr int kTcPABytes = kTcARows * kTcChunkWords * 4;  // 5,760
 constexpr int kTcPBBytes = kTcBRows * kTcChunkWords * 4;  // 4,608
 constexpr int kTcPStageBytes = kTcPABytes + kTcPBBytes;   // 10,368
 constexpr int kTcMaxClass = 65535;                 // class sizes the 16-bit exchange holds
 constexpr int kTcEpiWarps = 8;                     // scoring warps: two per lane quarter
-constexpr int kTcThreads = (8 + kTcEpiWarps + 2) * 32;
 constexpr int kTcProducerWarps = 8;
+constexpr int kTcThreads = (2 + kTcProducerWarps + kTcEpiWarps) * 32;
 constexpr int kTcBWarps = 2 * kTcBRows / 32;       // the first 6 producer warps also expand B
 // The issuing warps come first: the schedulers favour lower-numbered (older)
 // warps, and the single MMA thread is on every chunk's critical path.
@@ -112,15 +113,14 @@ constexpr uint32_t kTcCols = 512;
 constexpr uint32_t kTcDCols = 2 * kTcN;            // the accumulator (both classes): 384
 constexpr uint32_t kTcACol = kTcDCols;             // 384: first A stage
 constexpr uint32_t kTcAStageCols = kTcChunkWords * 4;  // 48 columns (384 E2M1 per lane)
-constexpr uint32_t kTcSfCol = kTcACol + kTcTmemStages * kTcAStageCols;  // 480: scale factors
+constexpr uint32_t kTcSfCol = kTcACol + kTcStages * kTcAStageCols;  // 480: scale factors
 constexpr uint32_t kTcIdesc = (1u << 7) | (1u << 10)           // A, B = E2M1
                               | ((uint32_t)(kTcN >> 3) << 17)  // N
                               | (1u << 23)                     // scales UE8M0
                               | ((uint32_t)(256 >> 4) << 24);  // M (the pair)
-constexpr size_t kTcAOff = kTcStages * (size_t)kTcBStageBytes;  // A of a shared-memory stage
-constexpr size_t kTcPOff = kTcAOff + (kTcStages - kTcTmemStages) * (size_t)kTcAStageBytes;  // ring
+constexpr size_t kTcPOff = kTcStages * (size_t)kTcBStageBytes;               // packed ring
 constexpr size_t kTcXOff = kTcPOff + kTcPStages * (size_t)kTcPStageBytes;    // exchange rows
-constexpr int kTcQueueCap = 3 * 32;                // pairs a warp can queue per 8 B SNPs
+constexpr int kTcQueueCap = 3 * 32;                // pairs a warp can queue per group of 8 B SNPs
 constexpr size_t kTcQOff = kTcXOff + (size_t)kTcEpiWarps * 32 * kTcXPitch * 2;  // pair queues
 constexpr size_t kTcSmem = kTcQOff + (size_t)kTcEpiWarps * kTcQueueCap * 4;
 static_assert(kTcSfCol + 32 <= kTcCols, "tensor memory budget");
@@ -128,10 +128,7 @@ static_assert(kTcBWarps * 32 == 2 * kTcBRows && kTcBWarps <= kTcProducerWarps, "
 static_assert(kTcHalfWords == 4 || kTcHalfWords == 6,
               "a producer thread stores 16 or 24 tensor-memory columns");
 constexpr long long kTcWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
-static_assert(kTcStages == kTcTmemStages || kTcStages == kTcTmemStages + 1,
-              "at most one shared-memory A stage");
-static_assert(kTcPStageBytes % 128 == 0 && kTcPABytes % 128 == 0 && kTcPOff % 128 == 0 &&
-                  kTcAOff % 128 == 0,
+static_assert(kTcPStageBytes % 128 == 0 && kTcPABytes % 128 == 0 && kTcPOff % 128 == 0,
               "TMA destinations 128-byte aligned");
 static_assert(kTcSmem > 114 * 1024 && kTcSmem <= 227 * 1024,
               "more than half an SM: one CTA (and tensor-memory owner) per SM");
@@ -262,16 +259,6 @@ __device__ __forceinline__ void tc_mma2(uint32_t d, uint32_t a, uint64_t bdesc, 
         " tcgen05.mma.cta_group::2.kind::mxf4.block_scale.scale_vec::2X [%0], [%1], %2, %3, [%4], "
         "[%4], p;\n}\n" ::"r"(d),
         "r"(a), "l"(bdesc), "r"(kTcIdesc), "r"(sf), "r"(acc));
-}
-
-// ... with A from shared memory (descriptor `adesc`, the same offset in both CTAs).
-__device__ __forceinline__ void tc_mma2_ss(uint32_t d, uint64_t adesc, uint64_t bdesc, uint32_t sf,
-                                           uint32_t acc) {
-    asm volatile(
-        "{\n .reg .pred p;\n setp.ne.b32 p, %5, 0;\n"
-        " tcgen05.mma.cta_group::2.kind::mxf4.block_scale.scale_vec::2X [%0], %1, %2, %3, [%4], "
-        "[%4], p;\n}\n" ::"r"(d),
-        "l"(adesc), "l"(bdesc), "r"(kTcIdesc), "r"(sf), "r"(acc));
 }
 
 // Completion of the pair's MMAs issued so far arrives on barrier `b` (same
@@ -551,11 +538,6 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
         const int t8 = 32 * (warp - kTcProdWarp0) + lane;
         const int u = t8 % kTcBRows, hb = t8 / kTcBRows;
         unsigned char *bst0 = tc_smem + (u >> 3) * kTcSbo + (HW * hb) * kTcLbo + (u & 7) * 16;
-        // the shared-memory A stage: row 32q + lane (the tensor-memory lane of
-        // the other stages; rows 30, 31 of each quarter zero), words HW h ..
-        const int arow_sm = 32 * q + lane;
-        unsigned char *ast0 = tc_smem + kTcAOff + (arow_sm >> 3) * kTcSbo + (HW * h) * kTcLbo +
-                              (arow_sm & 7) * 16;
         for (int idx = 0; idx < total; ++idx) {
             const uint32_t j = (uint32_t)idx % kTcPStages, s = (uint32_t)idx % kTcStages;
             if (!mbar_wait_warp(&pfull_bar[j], ((uint32_t)idx / kTcPStages) & 1, vabort, err, 5)) break;
@@ -597,15 +579,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
             if (!mbar_wait_warp(&empty_bar[s], (((uint32_t)idx / kTcStages) & 1) ^ 1, vabort, err, 1))
                 break;
             tc_fence_after();
-            if (s < kTcTmemStages) {
-                tmem_st16(ta0 + s * kTcAStageCols, r);
-                if constexpr (HW == 6) tmem_st8(ta0 + s * kTcAStageCols + 16, r + 16);
-            } else {
-#pragma unroll
-                for (int m = 0; m < HW; ++m)
-                    *reinterpret_cast<uint4 *>(ast0 + m * kTcLbo) =
-                        make_uint4(r[4 * m], r[4 * m + 1], r[4 * m + 2], r[4 * m + 3]);
-            }
+            tmem_st16(ta0 + s * kTcAStageCols, r);
+            if constexpr (HW == 6) tmem_st8(ta0 + s * kTcAStageCols + 16, r + 16);
             if (has_b) {
                 unsigned char *bst = bst0 + (size_t)s * kTcBStageBytes;
 #pragma unroll
@@ -657,7 +632,6 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
             // s * kTcBStageBytes >> 4 (no per-stage array: a runtime-indexed one
             // would live in local memory, one load per chunk on the issue path)
             const uint64_t bdesc0 = tc_bdesc(su32(tc_smem));
-            const uint64_t adesc_sm = tc_bdesc(su32(tc_smem + kTcAOff));
             const uint32_t sf = tbase + kTcSfCol;
             uint32_t gc = 0, lt = 0;
             bool ok = true;
@@ -687,17 +661,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
                     tc_fence_after();
                     // MMA kk reads A columns 8kk.. and the k-group pair 2kk (256 B further
                     // each: +16 in the descriptor's address field)
-                    if (s < kTcTmemStages) {
 #pragma unroll
-                        for (int kk = 0; kk < kTcChunkWords / 2; ++kk)
-                            if (kk < nm) tc_mma2(d, a + kk * 8, bd + (uint64_t)(16 * kk), sf, kk == 0 ? acc0 : 1u);
-                    } else {
-#pragma unroll
-                        for (int kk = 0; kk < kTcChunkWords / 2; ++kk)
-                            if (kk < nm)
-                                tc_mma2_ss(d, adesc_sm + (uint64_t)(16 * kk), bd + (uint64_t)(16 * kk), sf,
-                                           kk == 0 ? acc0 : 1u);
-                    }
+                    for (int kk = 0; kk < kTcChunkWords / 2; ++kk)
+                        if (kk < nm) tc_mma2(d, a + kk * 8, bd + (uint64_t)(16 * kk), sf, kk == 0 ? acc0 : 1u);
                     tc_commit2_both(&empty_bar[s]);
                     if (c == cm.n0 - 1 || c == nchunks - 1) tc_commit2_both(&dfull_bar[cls]);
                 }

@@ -152,7 +152,7 @@ gepi_status gepi_scan_range(gepi_planes *pl, const gepi_params *par, int a0, int
                             int b0, int nb, gepi_result *tops, int k);
 
 /* Progress of a scan, reported at tile-band ends.  Tiles are walked in bands of
- * 8 A-tile rows (320 SNPs for the tensor-core kernel, 256 for the popcount
+ * about 320 A SNPs (4 A-tile rows of the tensor-core kernel, 10 of the popcount
  * kernel); when a callback fires, every band before the current one is done,
  * so for a whole-genome scan all pairs (s, t), t <= s < snps_done, are tested.
  * Replaces the reference's progress block at diagonal points
@@ -221,7 +221,7 @@ typedef struct gepi_scan_stats {
     uint64_t tiles;           /* SNP tile pairs processed                               */
     uint64_t candidates;      /* candidates left for the final host sort                */
     int32_t method;           /* GEPI_METHOD_POPC or GEPI_METHOD_TENSOR actually used   */
-    int32_t tile_snps;        /* SNPs per tile side                                     */
+    int32_t tile_snps;        /* A SNPs per tile (80 tensor core, 32 popcount)          */
 } gepi_scan_stats;
 gepi_status gepi_last_scan_stats(const gepi_planes *pl, gepi_scan_stats *out);
 

@@ -58,9 +58,8 @@
 //              part of each class half of the accumulator (tcgen05.ld) to
 //              shared memory as 16-bit counts and hand it back, then bound
 //              every SNP pair per row pair (one chi^2 bound covers a row
-//              pair's five tests, for either objective; a genotype-cell chi^2
-//              covers all four row pairs first) and queue the few that may
-//              pass; the warp then runs the per-test bounds and the
+//              pair's five tests, for either objective) and queue the few
+//              that may pass; the warp then runs the per-test bounds and the
 //              out-of-line refinement over its queue densely
 // mbarriers: pfull[j] (copy transaction bytes) / pempty[j] (8 producer warps)
 // per ring slot of each CTA; full[s] (even CTA: 16 producer warps of the pair)
@@ -685,7 +684,6 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
         const int i = lane / 3, p = lane % 3;
         const float theta = DUMP ? 0.f : ctx.st->theta;
         const float lp_thr = DUMP ? 0.f : ctx.st->lp_thr;
-        const int geno = ctx.geno;
         const int aoff = kTcASnps * (int)rank + 10 * q;  // this warp's first A SNP in the tile
         uint32_t lt = 0;
         bool live = true;
@@ -756,7 +754,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
                                 G[pp * 3 + qq] = u16f(xg[(3 * i + pp) * kTcXPitch + 3 * jl + qq]);
                                 G[9 + pp * 3 + qq] = u16f(xg[(3 * i + pp) * kTcXPitch + 24 + 3 * jl + qq]);
                             }
-                        rp = rowpair_bounds(G, G + 9, sA == sBt, OBJ, theta, lp_thr, geno);
+                        rp = rowpair_bounds(G, G + 9, sA == sBt, OBJ, theta, lp_thr);
                     }
                     const uint32_t bal = __ballot_sync(0xffffffffu, rp != 0);
                     if (rp) qu[qn + __popc(bal & ((1u << lane) - 1u))] = ((uint32_t)lane << 8) | ((uint32_t)jl << 4) | rp;

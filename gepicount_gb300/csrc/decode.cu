@@ -155,26 +155,6 @@ cudaError_t launch_decode_rows(const uint64_t *bits, const uint64_t *valid, int 
     return cudaGetLastError();
 }
 
-// Sets *uncovered when some valid sample of some SNP sets neither allele row
-// (possible only for rows handed in directly, never for .bed calls).
-__global__ void allele_cover_kernel(const uint32_t *__restrict__ planes, int n_snps, int Wp,
-                                    int *uncovered) {
-    const size_t total = (size_t)n_snps * Wp;
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total;
-         i += (size_t)gridDim.x * blockDim.x) {
-        const size_t s = i / Wp, w = i - s * Wp;
-        const uint32_t *r = planes + s * 3 * Wp + w;
-        if (__ldg(r + 2 * (size_t)Wp) & ~(__ldg(r) | __ldg(r + Wp))) *uncovered = 1;
-    }
-}
-
-cudaError_t launch_allele_cover(const uint32_t *planes, int n_snps, int Wp, int *uncovered,
-                                int num_sms, cudaStream_t stream) {
-    if (n_snps <= 0) return cudaSuccess;
-    allele_cover_kernel<<<num_sms * 4, 256, 0, stream>>>(planes, n_snps, Wp, uncovered);
-    return cudaGetLastError();
-}
-
 // Marginal association of every SNP with the class: the larger phi^2 of its
 // two allele rows' carrier x class tables (D^2 / ((a + b)(m - a - b) y z),
 // D = a z - b y; a, b carriers and y, z valid samples of class 0, 1).  One

@@ -53,7 +53,6 @@ struct ScanCtx {
     const double *lf;    // log(n!) table (Fisher exact path)
     const float *lf32;   // log(n!) as float (Fisher bound)
     int objective;       // 0 entropy, 1 Fisher
-    int geno;            // every valid sample sets an allele row (genotype-cell prefilter)
     Cand *cand;
     uint32_t cap;
     ScanState *st;
@@ -267,59 +266,11 @@ __device__ __forceinline__ float tlog2f(float n) { return n > 1.f ? n * __log2f(
 // 1e-4 relative plus 0.01.  A class without valid samples leaves every test
 // with w z = x y, which is never ranked.  On the diagonal row 2t+j must be <=
 // row 2s+i, which drops (i, j) = (0, 1), bit 1.
-// Genotype cells of an SNP pair in one class from its plane Gram G (planes A,
-// a, V; A = carries allele 1, a = carries allele 2, both masked by V).  When
-// every valid sample sets A or a (a .bed's calls: 00 -> A, 10 -> A and a, 11
-// -> a), the genotypes are AA = V - a, Aa = A + a - V, aa = V - A, and the 3 x
-// 3 genotype table is L G L^T with those rows of L (exact small integers).
-__device__ __forceinline__ void genotype_cells(const float *G, float *N) {
-    float M[9];
-#pragma unroll
-    for (int q = 0; q < 3; ++q) {
-        M[q] = G[6 + q] - G[3 + q];
-        M[3 + q] = G[q] + G[3 + q] - G[6 + q];
-        M[6 + q] = G[6 + q] - G[q];
-    }
-#pragma unroll
-    for (int g = 0; g < 3; ++g) {
-        N[3 * g] = M[3 * g + 2] - M[3 * g + 1];
-        N[3 * g + 1] = M[3 * g] + M[3 * g + 1] - M[3 * g + 2];
-        N[3 * g + 2] = M[3 * g + 2] - M[3 * g];
-    }
-}
-
 __device__ __forceinline__ uint32_t rowpair_bounds(const float *G0, const float *G1, bool diag,
-                                                   int objective, float theta, float lp_thr,
-                                                   int geno) {
+                                                   int objective, float theta, float lp_thr) {
     const float y = G0[8], z = G1[8], yz = y * z, m = y + z, yzm = yz * m;
     if (!(yz > 0.f)) return 0u;
     const float lfix = objective == 0 ? 0.f : 0.5f * logf(4.f * yz);
-    if (geno) {
-        // Every row-pair cell is a union of genotype cells, so the class x 9
-        // genotype-cell table's chi^2 bounds all four row-pair tables' (data
-        // processing): one 9-term sum rejects the whole SNP pair.  Each D is two
-        // rounded products apart from exact (within y z 2^-19), the reciprocals
-        // and the sum within the 1 + 2^-18 factor.
-        float N0[9], N1[9];
-        genotype_cells(G0, N0);
-        genotype_cells(G1, N1);
-        const float E9 = yz * 1.9073486328125e-06f;  // 2^-19
-        float S9 = 0.f;
-#pragma unroll
-        for (int c = 0; c < 9; ++c) {
-            const float t = fabsf(N0[c] * z - N1[c] * y) + E9;
-            S9 = fmaf(t * t, __fdividef(1.f, fmaxf(N0[c] + N1[c], 1.f)), S9);
-        }
-        S9 *= 1.0000038146972656f;  // 1 + 2^-18
-        bool pass;
-        if (objective == 0) {
-            pass = S9 >= theta * yzm;
-        } else {
-            const float lo = -m * log1pf(S9 / yzm) - lfix;
-            pass = lo - (1e-4f * fabsf(lo) + 1e-2f) <= lp_thr;
-        }
-        if (!pass) return 0u;
-    }
     // The four row-pair tables share their margins: with R_i = a_i2 z - b_i2 y
     // (row 2s+i carriers) and C_j = a_2j z - b_2j y (row 2t+j carriers), the
     // cells give D_11 = a_ij z - b_ij y, D_10 = R_i - D_11, D_01 = C_j - D_11
@@ -395,7 +346,7 @@ __device__ __forceinline__ void score_tests(const ScanCtx &ctx, const float *G0,
     const float yz = y * z;
     const bool diag = (s == t);
     // row pairs that may hold a passing test (almost always none)
-    const uint32_t rp = rowpair_bounds(G0, G1, diag, ctx.objective, theta, lp_thr, ctx.geno);
+    const uint32_t rp = rowpair_bounds(G0, G1, diag, ctx.objective, theta, lp_thr);
     if (!rp) return;
     // Pair-level terms of the FP32 entropy estimate (stage 2), made on demand.
     float Tm = -1.f, Ty = 0.f, Tz = 0.f;

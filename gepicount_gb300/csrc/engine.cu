@@ -390,7 +390,6 @@ gepi_status Engine::launch(Job &j) {
     ctx.lf = pl->d_lf;
     ctx.lf32 = pl->d_lf32;
     ctx.objective = r.objective;
-    ctx.geno = pl->geno;
     ctx.cap = b->cap;
     ctx.st = b->state;
     ctx.cand = b->cand[j.cur];

@@ -16,8 +16,6 @@ namespace gepi {
 
 cudaError_t launch_decode_bed(const uint8_t *bed_payload, size_t bps, int n_snps,
                               const int32_t *perm, int Wp, uint32_t *planes, cudaStream_t stream);
-cudaError_t launch_allele_cover(const uint32_t *planes, int n_snps, int Wp, int *uncovered,
-                                int num_sms, cudaStream_t stream);
 cudaError_t launch_marginal(const uint32_t *planes, int n_snps, int Wp, int W0, float *score,
                             int num_sms, cudaStream_t stream);
 cudaError_t launch_decode_rows(const uint64_t *bits, const uint64_t *valid, int nw, int n_snps,
@@ -108,7 +106,6 @@ gepi_status pl_check_mem(size_t bytes, const char *what);
 // The plane-set handle of the C ABI.
 struct gepi_planes {
     uint64_t serial = 0;  // unique per plane set in the process (keys cached tile orders)
-    int geno = 0;         // every valid sample sets an allele row (ScanCtx::geno)
     int device = 0, num_sms = 0;
     int auto_method = 0;  // AUTO's choice for this plane set (0 = not tuned yet)
     float tune_ms[2] = {0.f, 0.f};  // autotuner timings: popcount, tensor core

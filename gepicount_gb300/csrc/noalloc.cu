@@ -336,7 +336,6 @@ extern "C" gepi_status gepi_process_gpu_1_noalloc(const uint64_t *bits, const ui
     ctx.lf = d_lf;
     ctx.lf32 = d_lf32;
     ctx.objective = par->objective;
-    ctx.geno = 0;  // rows as handed in: no genotype-cell prefilter
     ctx.cap = kNoAllocCap;
     ctx.st = d_state;
     const float lp_margin = 2e-6f * (float)std::lgamma((double)nmax + 1.0) + 1e-3f;

@@ -121,14 +121,14 @@ void planes_free(gepi_planes *pl) {
         pool_free(pl->d_tc_blocks, pl->stream);
         pool_free(pl->d_cand[0], pl->stream);
         pool_free(pl->d_cand[1], pl->stream);
+        pool_free(pl->d_T, pl->stream);
+        pool_free(pl->d_lf, pl->stream);
+        pool_free(pl->d_lf32, pl->stream);
+        pool_free(pl->d_state, pl->stream);
+        pool_free(pl->d_sel, pl->stream);
+        pool_free(pl->d_tiles, pl->stream);
         cudaStreamSynchronize(pl->stream);
     }
-    dfree(pl->d_T);
-    dfree(pl->d_lf);
-    dfree(pl->d_lf32);
-    dfree(pl->d_state);
-    dfree(pl->d_sel);
-    dfree(pl->d_tiles);
     if (pl->h_state) cudaFreeHost(pl->h_state);
     pl->h_state = nullptr;
     for (cudaEvent_t e : pl->ev) cudaEventDestroy(e);
@@ -147,12 +147,14 @@ gepi_status ensure_tables(gepi_planes *pl) {
     std::vector<float> lf32;
     build_lfact(nmax, lf, lf32);
     pl->lf_max = (float)lf.back();
-    GEPI_CUDA(cudaMalloc(&pl->d_T, T.size() * 8));
-    GEPI_CUDA(cudaMalloc(&pl->d_lf, lf.size() * 8));
-    GEPI_CUDA(cudaMalloc(&pl->d_lf32, lf32.size() * 4));
-    GEPI_CUDA(cudaMemcpy(pl->d_T, T.data(), T.size() * 8, cudaMemcpyHostToDevice));
-    GEPI_CUDA(cudaMemcpy(pl->d_lf, lf.data(), lf.size() * 8, cudaMemcpyHostToDevice));
-    GEPI_CUDA(cudaMemcpy(pl->d_lf32, lf32.data(), lf32.size() * 4, cudaMemcpyHostToDevice));
+    GEPI_CUDA(pool_alloc(pl->device, &pl->d_T, T.size() * 8, pl->stream));
+    GEPI_CUDA(pool_alloc(pl->device, &pl->d_lf, lf.size() * 8, pl->stream));
+    GEPI_CUDA(pool_alloc(pl->device, &pl->d_lf32, lf32.size() * 4, pl->stream));
+    GEPI_CUDA(cudaMemcpyAsync(pl->d_T, T.data(), T.size() * 8, cudaMemcpyHostToDevice, pl->stream));
+    GEPI_CUDA(cudaMemcpyAsync(pl->d_lf, lf.data(), lf.size() * 8, cudaMemcpyHostToDevice, pl->stream));
+    GEPI_CUDA(cudaMemcpyAsync(pl->d_lf32, lf32.data(), lf32.size() * 4, cudaMemcpyHostToDevice,
+                              pl->stream));
+    GEPI_CUDA(cudaStreamSynchronize(pl->stream));  // the host tables go out of scope
     return GEPI_OK;
 }
 
@@ -178,16 +180,16 @@ gepi_status ensure_scan_buffers(gepi_planes *pl, int k) {
         GEPI_CUDA(pool_alloc(pl->device, &pl->d_cand[1], want * sizeof(Cand), pl->stream));
         pl->cap = (uint32_t)want;
     }
-    if (!pl->d_state) GEPI_CUDA(cudaMalloc(&pl->d_state, sizeof(ScanState)));
+    if (!pl->d_state) GEPI_CUDA(pool_alloc(pl->device, &pl->d_state, sizeof(ScanState), pl->stream));
     if (!pl->h_state) GEPI_CUDA(cudaMallocHost(&pl->h_state, sizeof(ScanState)));
-    if (!pl->d_sel) GEPI_CUDA(cudaMalloc(&pl->d_sel, sel_state_bytes()));
+    if (!pl->d_sel) GEPI_CUDA(pool_alloc(pl->device, &pl->d_sel, sel_state_bytes(), pl->stream));
     return GEPI_OK;
 }
 
 gepi_status upload_tiles(gepi_planes *pl, const std::vector<int2> &tiles) {
     if (tiles.size() > pl->tiles_cap) {
-        dfree(pl->d_tiles);
-        GEPI_CUDA(cudaMalloc(&pl->d_tiles, tiles.size() * sizeof(int2)));
+        pool_free(pl->d_tiles, pl->stream);
+        GEPI_CUDA(pool_alloc(pl->device, &pl->d_tiles, tiles.size() * sizeof(int2), pl->stream));
         pl->tiles_cap = tiles.size();
     }
     if (!tiles.empty())
@@ -243,13 +245,13 @@ uint64_t next_serial() {
 gepi_status ensure_marginal(gepi_planes *pl) {
     if (!pl->marginal.empty() || pl->n_snps <= 0) return GEPI_OK;
     float *d = nullptr;
-    GEPI_CUDA(cudaMalloc(&d, sizeof(float) * (size_t)pl->n_snps));
+    GEPI_CUDA(pool_alloc(pl->device, &d, sizeof(float) * (size_t)pl->n_snps, pl->stream));
     std::vector<float> h((size_t)pl->n_snps);
     cudaError_t e = launch_marginal(pl->d_planes, pl->n_snps, pl->Wp, pl->W0, d, pl->num_sms, pl->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(h.data(), d, sizeof(float) * h.size(), cudaMemcpyDeviceToHost, pl->stream);
+    pool_free(d, pl->stream);  // stream-ordered: no device-wide synchronization
     if (e == cudaSuccess) e = cudaStreamSynchronize(pl->stream);
-    cudaFree(d);
     GEPI_CUDA(e);
     pl->marginal.swap(h);
     return GEPI_OK;
@@ -295,30 +297,15 @@ void scan_tile_order(int a0, int a1, int b0, int b1, int TA, int TB, int band,
         if (!isa[(size_t)i])
             for (int j : hot_b)
                 if (j < jend[(size_t)i]) out.push_back(make_int2(i, j));
-    // the remaining tiles, band by band: counted, then filled in parallel
-    const int nbands = (nat + band - 1) / band;
-    std::vector<size_t> off((size_t)nbands + 1, 0);
-    for (int b = 0; b < nbands; ++b) {
-        size_t c = 0;
-        for (int i = b * band; i < std::min(nat, (b + 1) * band); ++i) {
-            if (isa[(size_t)i]) continue;
-            const int e = jend[(size_t)i];
-            c += (size_t)(e - (int)(std::lower_bound(hot_b.begin(), hot_b.end(), e) - hot_b.begin()));
-        }
-        off[(size_t)b + 1] = off[(size_t)b] + c;
-    }
-    const size_t base = out.size();
-    out.resize(base + off[(size_t)nbands]);
-    int2 *dst = out.data() + base;
-#pragma omp parallel for schedule(dynamic, 16) if (nbands >= 64)
-    for (int b = 0; b < nbands; ++b) {
-        const int i0 = b * band, i1 = std::min(nat, i0 + band);
+    // the remaining tiles, band by band (one thread: the fill is bound by the
+    // stores, and a thread team would keep spinning beside the scan's host loop)
+    for (int i0 = 0; i0 < nat; i0 += band) {
+        const int i1 = std::min(nat, i0 + band);
         const int jmax = jend[(size_t)(i1 - 1)];  // the band's last A tile reaches furthest
-        size_t w = off[(size_t)b];
         for (int j = 0; j < jmax; ++j) {
             if (isb[(size_t)j]) continue;
             for (int i = i0; i < i1; ++i)
-                if (!isa[(size_t)i] && j < jend[(size_t)i]) dst[w++] = make_int2(i, j);
+                if (!isa[(size_t)i] && j < jend[(size_t)i]) out.push_back(make_int2(i, j));
         }
     }
 }
@@ -385,7 +372,6 @@ gepi_status time_count_kernel(gepi_planes *pl, bool tc, int n, float *ms) {
     ctx.lf = pl->d_lf;
     ctx.lf32 = pl->d_lf32;
     ctx.objective = GEPI_ENTROPY;
-    ctx.geno = pl->geno;
     ctx.cap = pl->cap;
     ctx.st = pl->d_state;
     ctx.cand = pl->d_cand[0];
@@ -601,7 +587,6 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
     ctx.lf = pl->d_lf;
     ctx.lf32 = pl->d_lf32;
     ctx.objective = par->objective;
-    ctx.geno = pl->geno;
     ctx.cap = pl->cap;
     ctx.st = pl->d_state;
 
@@ -860,7 +845,6 @@ gepi_status gepi_planes_from_bed(const uint8_t *bed, size_t bed_bytes, int n_bim
         return fail(set_error(GEPI_ERR_CUDA, std::string("decode: ") + cudaGetErrorString(e)));
     pool_free(d_bed, pl->stream);
     pool_free(d_perm, pl->stream);
-    pl->geno = 1;  // .bed calls always set an allele row of a valid sample
     *out = pl;
     return GEPI_OK;
 }
@@ -918,16 +902,7 @@ gepi_status gepi_planes_from_rows(const uint64_t *bits, const uint64_t *valid, i
     if (e == cudaSuccess)
         e = launch_decode_rows(d_bits, d_valid, n_words, n_snps, d_perm, pl->Wp, pl->d_planes,
                                pl->stream, pl->num_sms);
-    // rows handed in need not set an allele row for every valid sample
-    int *d_unc = nullptr;
-    if (e == cudaSuccess) e = pool_alloc(device, &d_unc, sizeof(int), pl->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(d_unc, 0, sizeof(int), pl->stream);
-    if (e == cudaSuccess) e = launch_allele_cover(pl->d_planes, n_snps, pl->Wp, d_unc, pl->num_sms, pl->stream);
-    int h_unc = 1;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&h_unc, d_unc, sizeof(int), cudaMemcpyDeviceToHost, pl->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(pl->stream);
-    pool_free(d_unc, pl->stream);
-    pl->geno = h_unc == 0;
     if (e != cudaSuccess)
         return fail(set_error(GEPI_ERR_CUDA, std::string("decode rows: ") + cudaGetErrorString(e)));
     pool_free(d_bits, pl->stream);

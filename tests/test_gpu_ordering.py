@@ -3,9 +3,9 @@
 - Hot tiles first: large scans visit the tiles of the strongest marginal SNPs
   before the rest.  The ranked list must equal the band-order scan's (a scan
   with progress callbacks keeps band order) and the other counting kernel's.
-- Genotype-cell prefilter: it is valid only when every valid sample sets an
-  allele row.  Rows handed in directly may break that, and the scan must then
-  fall back to the per-row-pair bound and still equal the oracle.
+- Arbitrary allele rows: rows handed in directly may leave a valid sample with
+  neither allele set (a .bed never does); the bounds assume nothing about the
+  rows, so the scan must still equal the oracle.
 - Class size: the tensor-core kernel passes counts as 16-bit values, so it
   refuses classes above 65,535 samples; AUTO then picks the popcount kernel.
 """

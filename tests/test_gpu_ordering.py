@@ -71,3 +71,18 @@ def test_tensor_kernel_refuses_classes_above_16_bits(gepi):
         popc = pl.scan(100, method=1)
         assert auto.tobytes() == popc.tobytes()
         assert pl.last_stats()["method"] == 1
+
+
+def test_fisher_auto_choice_matches_both_kernels(gepi):
+    # AUTO times the two kernels on a short Fisher scan for Fisher requests;
+    # whichever it picks, the ranked list is the same
+    spec = gepi.SynthSpec(n_snps=700, n_cases=260, n_controls=240, maf_lo=0.05, maf_hi=0.5,
+                          missing=0.02, n_planted=2, odds_ratio=3.0, seed=4242)
+    bed, ph, _ = gepi.synth_bed(spec)
+    with gepi.Planes.from_bed(bed, spec.n_snps, ph) as pl:
+        auto = pl.scan(300, objective=1, method=0)
+        chosen = pl.last_stats()["method"]
+        popc = pl.scan(300, objective=1, method=1)
+        tc = pl.scan(300, objective=1, method=2)
+    assert chosen in (1, 2)
+    assert auto.tobytes() == popc.tobytes() == tc.tobytes()

@@ -133,6 +133,10 @@ gepi_status gepi_planes_from_bed(const uint8_t *bed, size_t bed_bytes, int n_bim
 gepi_status gepi_planes_from_rows(const uint64_t *bits, const uint64_t *valid, int n_rows,
                                   int n_words, const uint64_t *mask1, const uint64_t *mask2,
                                   int device, gepi_planes **out);
+/* Frees the plane set.  Its device buffers (planes, operand blocks, candidate
+ * buffers, tables) come from a stream-ordered pool per device that keeps up to
+ * 8 GiB of freed memory for the next plane set, so building one plane set per
+ * cohort, request or step costs no cudaMalloc / cudaFree of the large buffers. */
 void gepi_planes_destroy(gepi_planes *pl);
 int gepi_planes_num_snps(const gepi_planes *pl);
 /* Samples per class (class 0 = phenotype 1, class 1 = phenotype 2). */

@@ -42,8 +42,8 @@
 // accumulates, so the next tile's MMAs start without draining the tensor pipe.
 // Shared memory: two B stages of 96 rows x 192 bytes in the SWIZZLE_NONE
 // K-major core-matrix layout (8 rows x 16 B cores, k-group stride 128 B,
-// row-group stride 1536 B), the packed ring (4 slots), the scoring warps'
-// exchange rows and pair queues.
+// row-group stride 1536 B), the packed ring (4 slots) and the scoring warps'
+// exchange rows.
 //
 // Warp roles (18 warps per CTA, the pair striding over the tile list):
 //   MMA        warp 0 of the even CTA, one thread: up to 6 x tcgen05.mma per
@@ -58,9 +58,9 @@
 //              part of each class half of the accumulator (tcgen05.ld) to
 //              shared memory as 16-bit counts and hand it back, then bound
 //              every SNP pair per row pair (one chi^2 bound covers a row
-//              pair's five tests, for either objective) and queue the few
-//              that may pass; the warp then runs the per-test bounds and the
-//              out-of-line refinement over its queue densely
+//              pair's five tests, for either objective; lane = B SNP, one A
+//              SNP per round); the rare lane whose bound passes runs the
+//              per-test bounds and the out-of-line refinement
 // mbarriers: pfull[j] (copy transaction bytes) / pempty[j] (8 producer warps)
 // per ring slot of each CTA; full[s] (even CTA: 16 producer warps of the pair)
 // / empty[s] (commit, both CTAs) per stage; dfull[c] (commit, both CTAs) /
@@ -119,9 +119,7 @@ constexpr uint32_t kTcIdesc = (1u << 7) | (1u << 10)           // A, B = E2M1
                               | ((uint32_t)(256 >> 4) << 24);  // M (the pair)
 constexpr size_t kTcPOff = kTcStages * (size_t)kTcBStageBytes;               // packed ring
 constexpr size_t kTcXOff = kTcPOff + kTcPStages * (size_t)kTcPStageBytes;    // exchange rows
-constexpr int kTcQueueCap = 3 * 32;                // pairs a warp can queue per group of 8 B SNPs
-constexpr size_t kTcQOff = kTcXOff + (size_t)kTcEpiWarps * 32 * kTcXPitch * 2;  // pair queues
-constexpr size_t kTcSmem = kTcQOff + (size_t)kTcEpiWarps * kTcQueueCap * 4;
+constexpr size_t kTcSmem = kTcXOff + (size_t)kTcEpiWarps * 32 * kTcXPitch * 2;
 static_assert(kTcSfCol + 32 <= kTcCols, "tensor memory budget");
 static_assert(kTcBWarps * 32 == 2 * kTcBRows && kTcBWarps <= kTcProducerWarps, "B pieces");
 static_assert(kTcHalfWords == 4 || kTcHalfWords == 6,
@@ -679,19 +677,22 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
         const int eh = ew >> 2;                   // B SNPs 32 eh .. 32 eh + 31
         // this warp's accumulator region as 16-bit counts: row = TMEM lane,
         // [group 0: class 0 (24), class 1 (24) | group 1: ...] (odd word pitch)
+        // this warp's accumulator region as 16-bit counts: row = TMEM lane (plane
+        // p of A SNP i at row 3i + p), laid out [class][B plane qq][B SNP jl] so
+        // that the 32 lanes reading one plane pair of 32 B SNPs hit 16
+        // consecutive words (odd word pitch: the copy-out is conflict-free too)
         uint16_t *xh = reinterpret_cast<uint16_t *>(tc_smem + kTcXOff) + (size_t)ew * 32 * kTcXPitch;
-        uint32_t *qu = reinterpret_cast<uint32_t *>(tc_smem + kTcQOff) + (size_t)ew * kTcQueueCap;
-        const int i = lane / 3, p = lane % 3;
         const float theta = DUMP ? 0.f : ctx.st->theta;
         const float lp_thr = DUMP ? 0.f : ctx.st->lp_thr;
         const int aoff = kTcASnps * (int)rank + 10 * q;  // this warp's first A SNP in the tile
+        constexpr int kB = 8 * kTcEpiGroups;             // B SNPs of the warp: 32
         uint32_t lt = 0;
         bool live = true;
         for (int t = pair; t < ntiles && live; t += npairs, ++lt) {
             const int2 tl = tiles[t];
-            const int sA = a0 + tl.x * kTcPairASnps + aoff + i;
-            const int sB0 = b0 + tl.y * kTcBSnps + 8 * kTcEpiGroups * eh;
-            const uint32_t tq = tbase + ((uint32_t)(32 * q) << 16) + 24 * kTcEpiGroups * eh;
+            const int sAq = a0 + tl.x * kTcPairASnps + aoff;  // A SNP 0 of the lane quarter
+            const int sB0 = b0 + tl.y * kTcBSnps + kB * eh;
+            const uint32_t tq = tbase + ((uint32_t)(32 * q) << 16) + 3 * kB * eh;
             // copy each class half out as soon as its MMAs are done and hand it
             // back: the tensor pipe goes on with the other half, then the next tile
             for (int cls = 0; cls < 2; ++cls) {
@@ -700,93 +701,76 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
                     break;
                 }
                 tc_fence_after();
+                uint32_t *rw = reinterpret_cast<uint32_t *>(xh + lane * kTcXPitch) + cls * (3 * kB / 2);
 #pragma unroll
                 for (int gl = 0; gl < kTcEpiGroups; ++gl) {
-                    uint32_t v[24];
+                    uint32_t v[24];  // column 3 jl' + qq of B SNPs 8 gl + jl'
                     tmem_ld16(tq + cls * kTcN + 24 * gl, *reinterpret_cast<uint32_t(*)[16]>(v));
                     tmem_ld8(tq + cls * kTcN + 24 * gl + 16, *reinterpret_cast<uint32_t(*)[8]>(v + 16));
                     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                    uint32_t *row = reinterpret_cast<uint32_t *>(xh + lane * kTcXPitch + 48 * gl + 24 * cls);
 #pragma unroll
-                    for (int k = 0; k < 12; ++k)
-                        row[k] = __float2uint_rn(__uint_as_float(v[2 * k])) |
-                                 (__float2uint_rn(__uint_as_float(v[2 * k + 1])) << 16);
+                    for (int qq = 0; qq < 3; ++qq)
+#pragma unroll
+                        for (int m = 0; m < 4; ++m)
+                            rw[qq * (kB / 2) + 4 * gl + m] =
+                                __float2uint_rn(__uint_as_float(v[6 * m + qq])) |
+                                (__float2uint_rn(__uint_as_float(v[6 * m + 3 + qq])) << 16);
                 }
                 tc_fence_before();
                 __syncwarp();
                 mbar_arrive_warp_cl(cluster_addr(&dempty_bar[cls], 0));
             }
             if (!live) break;
+            __syncwarp();
             if constexpr (DUMP) {
+                const int i = lane / 3, p = lane % 3, sA = sAq + i;
                 if (lane < 30 && sA < a1) {
                     const uint16_t *xr = xh + lane * kTcXPitch;
-                    for (int jb = 0; jb < 8 * kTcEpiGroups; ++jb) {
+                    for (int jb = 0; jb < kB; ++jb) {
                         const int sBt = sB0 + jb;
                         if (sBt >= b1) continue;
-                        const int gl = jb >> 3, jl = jb & 7;
                         uint32_t *o = dump + ((size_t)(sA - a0) * (b1 - b0) + (sBt - b0)) * 18;
 #pragma unroll
                         for (int qq = 0; qq < 3; ++qq) {
-                            o[p * 3 + qq] = xr[48 * gl + 3 * jl + qq];
-                            o[9 + p * 3 + qq] = xr[48 * gl + 24 + 3 * jl + qq];
+                            o[p * 3 + qq] = xr[qq * kB + jb];
+                            o[9 + p * 3 + qq] = xr[3 * kB + qq * kB + jb];
                         }
                     }
                 }
                 __syncwarp();
+                continue;
             }
-            for (int gl = 0; gl < kTcEpiGroups && !DUMP; ++gl) {
-                const uint16_t *xg = xh + 48 * gl;
-                // Phase 1: every lane bounds its SNP pairs (i, jl), jl = p + 3r, and
-                // queues those with a row pair that may pass.  Phase 2: the warp
-                // runs stage 1 and the refinement over the queue, densely.
-                int qn = 0;
+            // Round r bounds the pairs (A SNP r of the quarter, B SNP lane) per row
+            // pair; the rare lane whose bound passes runs the per-test bounds and
+            // the out-of-line refinement on the counts it holds.
+            const int sBt = sB0 + lane;
+            for (int r = 0; r < 10; ++r) {
+                const int sA = sAq + r;
+                if (!(sA < a1 && sBt < b1 && sBt <= sA)) continue;
+                const uint16_t *xr = xh + 3 * r * kTcXPitch + lane;
+                float G[18];
 #pragma unroll
-                for (int r = 0; r < 3; ++r) {
-                    const int jl = p + 3 * r;
-                    const int sBt = sB0 + 8 * gl + jl;
-                    uint32_t rp = 0;
-                    if (lane < 30 && sA < a1 && jl < 8 && sBt < b1 && sBt <= sA) {
-                        float G[18];
+                for (int pp = 0; pp < 3; ++pp)
 #pragma unroll
-                        for (int pp = 0; pp < 3; ++pp)
-#pragma unroll
-                            for (int qq = 0; qq < 3; ++qq) {
-                                G[pp * 3 + qq] = u16f(xg[(3 * i + pp) * kTcXPitch + 3 * jl + qq]);
-                                G[9 + pp * 3 + qq] = u16f(xg[(3 * i + pp) * kTcXPitch + 24 + 3 * jl + qq]);
-                            }
-                        rp = rowpair_bounds(G, G + 9, sA == sBt, OBJ, theta, lp_thr);
+                    for (int qq = 0; qq < 3; ++qq) {
+                        G[pp * 3 + qq] = u16f(xr[pp * kTcXPitch + qq * kB]);
+                        G[9 + pp * 3 + qq] = u16f(xr[pp * kTcXPitch + 3 * kB + qq * kB]);
                     }
-                    const uint32_t bal = __ballot_sync(0xffffffffu, rp != 0);
-                    if (rp) qu[qn + __popc(bal & ((1u << lane) - 1u))] = ((uint32_t)lane << 8) | ((uint32_t)jl << 4) | rp;
-                    qn += __popc(bal);
+                const uint32_t rp = rowpair_bounds(G, G + 9, sA == sBt, OBJ, theta, lp_thr);
+                if (!rp) continue;
+                uint32_t mask = tc_stage1<OBJ>(ctx, G, G + 9, rp, theta, lp_thr);
+                const int y = (int)G[8], z = (int)G[17];
+                while (mask) {
+                    const int bit = __ffs(mask) - 1;
+                    mask &= mask - 1;
+                    const int rpi = bit / 5, f = bit - 5 * rpi, ri = rpi >> 1, rj = rpi & 1;
+                    const int w = fun_count((int)G[ri * 3 + rj], (int)G[ri * 3 + 2], (int)G[6 + rj], y, f);
+                    const int x = fun_count((int)G[9 + ri * 3 + rj], (int)G[9 + ri * 3 + 2],
+                                            (int)G[15 + rj], z, f);
+                    tc_refine<OBJ>(ctx, 2 * sA + ri, 2 * sBt + rj, f, w, x, y, z);
                 }
-                __syncwarp();
-                for (int e = lane; e < qn; e += 32) {
-                    const uint32_t ent = qu[e];
-                    const int il = (int)(ent >> 8) / 3, jl = (int)(ent >> 4) & 15;
-                    const int sAe = a0 + tl.x * kTcPairASnps + aoff + il, sBt = sB0 + 8 * gl + jl;
-                    float G[18];
-#pragma unroll
-                    for (int pp = 0; pp < 3; ++pp)
-#pragma unroll
-                        for (int qq = 0; qq < 3; ++qq) {
-                            G[pp * 3 + qq] = u16f(xg[(3 * il + pp) * kTcXPitch + 3 * jl + qq]);
-                            G[9 + pp * 3 + qq] = u16f(xg[(3 * il + pp) * kTcXPitch + 24 + 3 * jl + qq]);
-                        }
-                    uint32_t mask = tc_stage1<OBJ>(ctx, G, G + 9, ent & 15u, theta, lp_thr);
-                    const int y = (int)G[8], z = (int)G[17];
-                    while (mask) {
-                        const int bit = __ffs(mask) - 1;
-                        mask &= mask - 1;
-                        const int rp = bit / 5, f = bit - 5 * rp, ri = rp >> 1, rj = rp & 1;
-                        const int w = fun_count((int)G[ri * 3 + rj], (int)G[ri * 3 + 2], (int)G[6 + rj], y, f);
-                        const int x = fun_count((int)G[9 + ri * 3 + rj], (int)G[9 + ri * 3 + 2],
-                                                (int)G[15 + rj], z, f);
-                        tc_refine<OBJ>(ctx, 2 * sAe + ri, 2 * sBt + rj, f, w, x, y, z);
-                    }
-                }
-                __syncwarp();
             }
+            __syncwarp();
         }
     }
 

@@ -529,8 +529,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
         const bool arow = lane < 30;
         const int arow_off = (30 * q + (arow ? lane : 29)) * (kTcChunkWords * 4);
         const uint32_t ta0 = tbase + ((uint32_t)(32 * q) << 16) + kTcACol + 4 * HW * h;
-        // B piece of warps 0-5: row u = t % 96, words HW hb .. HW hb + HW - 1
-        // (consecutive lanes on consecutive rows: conflict-free 16-byte stores)
+        // B piece of the first six producer warps: row u = t % 96, words HW hb ..
+        // HW hb + HW - 1 (consecutive lanes on consecutive rows: conflict-free
+        // 16-byte stores)
         const bool has_b = warp - kTcProdWarp0 < kTcBWarps;
         const int t8 = 32 * (warp - kTcProdWarp0) + lane;
         const int u = t8 % kTcBRows, hb = t8 / kTcBRows;

@@ -267,9 +267,11 @@ gepi_status ensure_marginal(gepi_planes *pl) {
 constexpr int kHotSnps = 16;
 constexpr size_t kHotMinTiles = 4096;  // smaller scans keep the band order
 
-// The triangle scan's tile list in that order, generated directly (counted
-// and reserved first: no sort, no partition).  Empty hot sets give the plain
-// band order of build_tiles.
+// The triangle scan's tile list in that order, generated directly: counted,
+// sized once and written through a pointer (no sort, no partition).  Empty hot
+// sets give the plain band order of build_tiles.  One thread: the fill is
+// bound by the stores, and a thread team would keep spinning beside the
+// scan's host loop.
 void scan_tile_order(int a0, int a1, int b0, int b1, int TA, int TB, int band,
                      const std::vector<int> &hot_a, const std::vector<int> &hot_b,
                      std::vector<int2> &out) {
@@ -286,28 +288,36 @@ void scan_tile_order(int a0, int a1, int b0, int b1, int TA, int TB, int band,
         jend[(size_t)i] = std::min(nbt, e);
         total += (size_t)jend[(size_t)i];
     }
-    out.reserve(total);
+    out.resize(total);
+    int2 *w = out.data();
     std::vector<char> isa((size_t)nat, 0), isb((size_t)nbt, 0);
     for (int i : hot_a) isa[(size_t)i] = 1;
     for (int j : hot_b) isb[(size_t)j] = 1;
     for (int j = 0; j < nbt; ++j)
         for (int i : hot_a)
-            if (j < jend[(size_t)i]) out.push_back(make_int2(i, j));
+            if (j < jend[(size_t)i]) *w++ = make_int2(i, j);
     for (int i = 0; i < nat; ++i)
         if (!isa[(size_t)i])
             for (int j : hot_b)
-                if (j < jend[(size_t)i]) out.push_back(make_int2(i, j));
-    // the remaining tiles, band by band (one thread: the fill is bound by the
-    // stores, and a thread team would keep spinning beside the scan's host loop)
+                if (j < jend[(size_t)i]) *w++ = make_int2(i, j);
     for (int i0 = 0; i0 < nat; i0 += band) {
         const int i1 = std::min(nat, i0 + band);
-        const int jmax = jend[(size_t)(i1 - 1)];  // the band's last A tile reaches furthest
-        for (int j = 0; j < jmax; ++j) {
+        bool any_hot = false;
+        for (int i = i0; i < i1; ++i) any_hot |= isa[(size_t)i] != 0;
+        // jend grows with i: below the band's first A tile's end, every A tile of
+        // a band without hot rows pairs with B tile j
+        const int jmin = any_hot ? 0 : jend[(size_t)i0], jmax = jend[(size_t)(i1 - 1)];
+        for (int j = 0; j < jmin; ++j) {
+            if (isb[(size_t)j]) continue;
+            for (int i = i0; i < i1; ++i) *w++ = make_int2(i, j);
+        }
+        for (int j = jmin; j < jmax; ++j) {
             if (isb[(size_t)j]) continue;
             for (int i = i0; i < i1; ++i)
-                if (!isa[(size_t)i] && j < jend[(size_t)i]) out.push_back(make_int2(i, j));
+                if (!isa[(size_t)i] && j < jend[(size_t)i]) *w++ = make_int2(i, j);
         }
     }
+    out.resize((size_t)(w - out.data()));
 }
 
 // The A and B tiles of the kHotSnps strongest marginal SNPs (ascending).

@@ -150,6 +150,7 @@ def lib():
                                      _PROGRESS_FN, P, i32, i32]
     L.gepi_process_gpu_1.argtypes = [P, P, i32, i32, P, P, P, ctypes.POINTER(_Params)]
     L.gepi_last_scan_stats.argtypes = [P, ctypes.POINTER(_ScanStats)]
+    L.gepi_last_scan_values.argtypes = [P, P, i32]
     L.gepi_planes_autotune.argtypes = [P, ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_float),
                                        ctypes.POINTER(ctypes.c_float)]
     L.gepi_tensor_peak_tflops.argtypes = [i32, ctypes.POINTER(ctypes.c_double)]
@@ -175,7 +176,7 @@ def lib():
     for f in ("gepi_plink_open", "gepi_plink_row_info", "gepi_plink_decode_rows",
               "gepi_planes_from_bed", "gepi_planes_from_rows", "gepi_planes_class_sizes",
               "gepi_scan", "gepi_scan_range", "gepi_pair_counts", "gepi_process_gpu_1",
-              "gepi_last_scan_stats", "gepi_process_gpu_1_noalloc", "gepi_planes_autotune",
+              "gepi_last_scan_stats", "gepi_last_scan_values", "gepi_process_gpu_1_noalloc", "gepi_planes_autotune",
               "gepi_tensor_peak_tflops", "gepi_scan_batch", "gepi_scan_progress", "gepi_shard_range", "gepi_merge_results", "gepi_server_create",
               "gepi_server_submit", "gepi_server_wait",
               "gepi_synth_bed", "gepi_synth_write"):
@@ -416,6 +417,13 @@ class Planes:
         st = _ScanStats()
         _check(lib().gepi_last_scan_stats(self._h, ctypes.byref(st)))
         return {f: getattr(st, f) for f, _ in _ScanStats._fields_}
+
+    def last_values(self, k: int) -> np.ndarray:
+        """The FP64 objective each `ent` of the last ranked list was rounded
+        from (entropy -I bits, Fisher log10 p; 0 for zero-filled slots)."""
+        out = np.zeros(k, dtype=np.float64)
+        _check(lib().gepi_last_scan_values(self._h, out.ctypes.data, k))
+        return out
 
     def close(self):
         if self._h:

@@ -128,6 +128,7 @@ struct gepi_planes {
     size_t tiles_cap = 0;
     std::vector<cudaEvent_t> ev;  // timing events, reused across scans
     gepi_scan_stats stats{};
+    std::vector<double> last_values;  // FP64 objective of the last ranked list (gepi_last_scan_values)
 };
 
 

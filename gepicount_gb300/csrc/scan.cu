@@ -468,11 +468,14 @@ bool cand_better(const Cand &a, const Cand &b) {
 }
 
 // Top-k of `count` candidates (ranked by the deterministic tie-break) into
-// tops[0, k), zero-filling the rest.
-void rank_candidates(std::vector<Cand> &host, gepi_result *tops, int k) {
+// tops[0, k), zero-filling the rest.  `values` (optional) receives the double
+// each `ent` is rounded from (0 for zero-filled slots).
+void rank_candidates(std::vector<Cand> &host, gepi_result *tops, int k,
+                     std::vector<double> *values = nullptr) {
     std::memset(tops, 0, sizeof(gepi_result) * (size_t)k);
     const size_t keep = std::min<size_t>(host.size(), (size_t)k);
     std::partial_sort(host.begin(), host.begin() + keep, host.end(), cand_better);
+    if (values) values->assign((size_t)k, 0.0);
     for (size_t i = 0; i < keep; ++i) {
         const Cand &c = host[i];
         gepi_result &r = tops[i];
@@ -480,7 +483,9 @@ void rank_candidates(std::vector<Cand> &host, gepi_result *tops, int k) {
         r.sB = c.rBfun >> 3;
         r.fun = (char)(c.rBfun & 7);
         for (int j = 0; j < 4; ++j) r.n[j] = c.n[j];
-        r.ent = (float)(-value_of_key(c.key));
+        const double v = -value_of_key(c.key);
+        r.ent = (float)v;
+        if (values) (*values)[i] = v;
     }
 }
 
@@ -546,6 +551,7 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
     GEPI_TRY(ensure_tables(pl));
     GEPI_TRY(ensure_scan_buffers(pl, k));
     std::memset(tops, 0, sizeof(gepi_result) * (size_t)k);
+    pl->last_values.clear();
 
     int method = 0;
     GEPI_TRY(resolve_method(pl, par->method, &method));
@@ -732,7 +738,7 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
         S.scan_ms = ms;
         S.candidates = count;
     }
-    rank_candidates(host, tops, k);
+    rank_candidates(host, tops, k, &pl->last_values);
     if (prog && prog->next_end <= ntiles) {  // the last band end: the scan is complete
         gepi_progress pr{};
         pr.elapsed_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - prog->t0).count();
@@ -1114,6 +1120,14 @@ gepi_status gepi_tensor_peak_tflops(int device, double *tflops) {
 gepi_status gepi_last_scan_stats(const gepi_planes *pl, gepi_scan_stats *out) {
     if (!pl || !out) return set_error(GEPI_ERR_ARG, "gepi_last_scan_stats: bad argument");
     *out = pl->stats;
+    return GEPI_OK;
+}
+
+gepi_status gepi_last_scan_values(const gepi_planes *pl, double *out, int32_t k) {
+    if (!pl || !out || k <= 0) return set_error(GEPI_ERR_ARG, "gepi_last_scan_values: bad argument");
+    if ((size_t)k > pl->last_values.size())
+        return set_error(GEPI_ERR_ARG, "gepi_last_scan_values: k exceeds the last scan's list");
+    std::memcpy(out, pl->last_values.data(), sizeof(double) * (size_t)k);
     return GEPI_OK;
 }
 

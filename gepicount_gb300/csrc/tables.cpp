@@ -88,11 +88,16 @@ double fisher_lnp_host(int n11, int n12, int n21, int n22) {
         if (l[(size_t)(x - lo)] > lmax) lmax = l[(size_t)(x - lo)];
     }
     double num = 0.0, den = 0.0;
+    bool all = true;
     for (int x = lo; x <= hi; ++x) {
         const double v = l[(size_t)(x - lo)];
         den += std::exp(v - lmax);
         if (v <= lim) num += std::exp(v - lpo);
+        else all = false;
     }
+    // every term of the support qualifies: p = 1 exactly (the reference's
+    // linear-space ratio of two equal sums prints 0 there)
+    if (all) return 0.0;
     double r = lpo + std::log(num) - (lmax + std::log(den));
     return r > 0.0 ? 0.0 : r;
 }

@@ -7,7 +7,7 @@
  * project):
  *
  *   process_gpu_1(PlinkReader<ui8>*, InteractionResult*, const _paramP1&)
- *       src/proc_gpu.h:271, src/kernels/kernel1.cu:508-511
+ *       src/proc_gpu.h:134, src/kernels/kernel1.cu:508-511
  *       -> gepi_process_gpu_1()  (same inputs as plain arrays, same output)
  *   InteractionResult                 inc/gEpiCount.h:75-82  -> gepi_result
  *   struct _paramP1                   inc/gEpiCount.h:116-132 -> gepi_params
@@ -229,6 +229,15 @@ typedef struct gepi_scan_stats {
 } gepi_scan_stats;
 gepi_status gepi_last_scan_stats(const gepi_planes *pl, gepi_scan_stats *out);
 
+/* The FP64 objective each `ent` of the last ranked list on `pl` (gepi_scan,
+ * gepi_scan_range, gepi_scan_progress) was rounded from, before the float
+ * rounding of the InteractionResult field: entropy -I(F;C) in bits from the
+ * exact fixed-point key, Fisher log10 p from the device's log-space tail sums
+ * (src/kernels/fisher_d.cu:249-311 computes the same p in FP64 and returns it
+ * as float).  out[i] pairs with tops[i]; zero-filled slots give 0.  k may not
+ * exceed the last list's length. */
+gepi_status gepi_last_scan_values(const gepi_planes *pl, double *out, int32_t k);
+
 /* Counting-method autotuner (replaces the reference's --block-sizes /
  * --max-grid-area tuning, gEpiCount.cpp:135-141 and misc1.cu:35-89, which
  * size its batch grid).  GEPI_METHOD_AUTO requests on `pl` use the method this
@@ -323,11 +332,15 @@ gepi_status gepi_process_gpu_1(const uint64_t *bits, const uint64_t *valid, int 
  * device memory (held by every GPU that loads the library until exit).
  * Requests whose rows, planes, tables and tile list do not fit next to the
  * 2 x 65,536-record candidate buffers, or with topmost > 16,384, return
- * GEPI_ERR_LIMIT before any device work.  The first call on a device looks up
- * the array's device address; make it before any stream capture.  Calls share
- * the array: overlapping calls on one GPU race and must be serialised.
- * Popcount counting only.  This entry point has no counterpart in the
- * reference. */
+ * GEPI_ERR_LIMIT before any device work.  Each call looks up the array's
+ * device address on the device it runs on (cudaGetSymbolAddress, checked).
+ * Calls share the array and find the previous call's contents there (each
+ * call initialises what it reads): overlapping calls on one GPU race and must
+ * be serialised.  The log-factorial tables are the same host std::lgamma
+ * values gepi_process_gpu_1 uses, so both entry points return the same bits
+ * for either objective.  Only the success path is free of host heap
+ * allocation (an error message is a std::string).  Popcount counting only.
+ * This entry point has no counterpart in the reference. */
 gepi_status gepi_process_gpu_1_noalloc(const uint64_t *bits, const uint64_t *valid, int n_rows,
                                        int n_words, const uint64_t *mask1, const uint64_t *mask2,
                                        gepi_result *tops, const gepi_params *par);

@@ -1,15 +1,17 @@
 """Generate golden fixtures from the UNMODIFIED reference gEpiCount gold path.
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    GEPI_REFERENCE_ROOT=<reference tree> python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --ref <reference tree>
 
 Builds the reference with oracle/Makefile.ref into oracle/_ref/ (x86 build
 here; never shipped), writes seeded synthetic PLINK filesets with this
 package's generator, runs ``gEpiCount -g -i BASE -N k`` on each and stores
 the ranked rows it prints (src/misc/print_misc.h:59-78) plus the sha256 of the
 input files, so a test can regenerate the same input on any host and check it
-is byte-identical before comparing.  Cases that read the reference's own demo
-files (data/test, data/thinhap1) keep only the reference output; their tests
-skip when the reference tree is absent.
+is byte-identical before comparing.  The reference's own demo filesets
+(data/test: 2 SNPs x 6 samples, the known answer of README.txt; data/thinhap1:
+1,020 SNPs x 89 samples) are copied byte for byte into tests/golden/data/, so
+the tests run them on hosts without the reference tree (the GPU host).
 """
 from __future__ import annotations
 
@@ -18,6 +20,7 @@ import hashlib
 import json
 import os
 import re
+import shutil
 import subprocess
 import sys
 import tempfile
@@ -46,6 +49,7 @@ SYNTH_CASES = {
     "miss50": (dict(n_snps=33, n_cases=9, n_controls=11, missing=0.5, seed=50), 150),
 }
 REF_CASES = {"test": ("data/test", 10), "thinhap1": ("data/thinhap1", 200)}
+DATA_DIR = os.path.join(HERE, "data")
 
 
 def sha(path: str) -> str:
@@ -70,8 +74,11 @@ def run_gold(gold: str, base: str, k: int):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("GEPI_REFERENCE_ROOT"),
+                    help="root of the reference tree (default: $GEPI_REFERENCE_ROOT)")
     args = ap.parse_args()
+    if not args.ref or not os.path.isdir(args.ref):
+        ap.error("give the reference tree with --ref or GEPI_REFERENCE_ROOT")
     out_ref = os.path.join(ROOT, "oracle", "_ref")
     gold = os.path.join(out_ref, "gEpiCount")
     if not os.path.exists(gold):
@@ -91,8 +98,11 @@ def main():
             with open(os.path.join(HERE, f"gold_{name}.json"), "w") as f:
                 json.dump(doc, f, indent=0)
             print(name, len(rows))
+    os.makedirs(DATA_DIR, exist_ok=True)
     for name, (rel, k) in REF_CASES.items():
         base = os.path.join(args.ref, rel)
+        for ext in ("bed", "bim", "fam"):
+            shutil.copyfile(base + "." + ext, os.path.join(DATA_DIR, name + "." + ext))
         rows, stdout, qc, limit = run_gold(gold, base, k)
         doc = dict(case=name, kind="reference-data", path=rel, k=k,
                    sha256={e: sha(base + "." + e) for e in ("bed", "bim", "fam")},

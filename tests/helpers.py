@@ -65,7 +65,7 @@ def oracle():
     lib.orc_scan_topk.restype = i64
     lib.orc_scan_topk_range.argtypes = [P, P, P, P, i32, i32, i32, i32, i32, i32, i32, P, P, i32]
     lib.orc_scan_topk_range.restype = i64
-    lib.orc_gold_loop.argtypes = [P, P, P, P, i32, i32, i32, i32, P]
+    lib.orc_gold_loop.argtypes = [P, P, P, P, i32, i32, i32, i32, i32, P]
     lib.orc_gold_loop.restype = i64
     _oracle = lib
     return lib
@@ -202,7 +202,9 @@ def cells_to_n(cells):
 
 # ---- golden fixtures -----------------------------------------------------
 GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-REFERENCE_ROOT = os.environ.get("GEPI_REFERENCE_ROOT", "/root/reference")
+# the reference's demo filesets (data/test, data/thinhap1), copied byte for byte
+# by make_golden.py
+GOLDEN_DATA_DIR = os.path.join(GOLDEN_DIR, "data")
 
 
 def load_golden(name: str) -> dict:
@@ -217,8 +219,8 @@ def golden_names():
 
 
 def golden_input(doc: dict, tmpdir: str):
-    """Fileset base path for a golden case (regenerated if synthetic), or None
-    when it needs the reference's own data files and they are absent."""
+    """Fileset base path for a golden case: regenerated if synthetic, else the
+    reference's demo fileset committed under tests/golden/data/."""
     import hashlib
 
     if doc["kind"] == "synthetic":
@@ -227,9 +229,7 @@ def golden_input(doc: dict, tmpdir: str):
         base = os.path.join(tmpdir, doc["case"])
         g.synth_write(g.SynthSpec(**doc["spec"]), base)
     else:
-        base = os.path.join(REFERENCE_ROOT, doc["path"])
-        if not os.path.exists(base + ".bed"):
-            return None
+        base = os.path.join(GOLDEN_DATA_DIR, doc["case"])
     for ext, h in doc["sha256"].items():
         got = hashlib.sha256(open(base + "." + ext, "rb").read()).hexdigest()
         assert got == h, f"{base}.{ext}: input differs from the one the golden was made from"

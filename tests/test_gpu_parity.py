@@ -112,7 +112,8 @@ def test_rows_path_matches_bed_path(gepi, tmp_path):
 
 
 @pytest.mark.parametrize("method", sorted(METHODS))
-@pytest.mark.parametrize("name", ["cfg1", "s63", "s64", "s65", "s129", "miss50", "cfg2_small"])
+@pytest.mark.parametrize("name", ["test", "thinhap1", "cfg1", "s63", "s64", "s65", "s129", "miss50",
+                                  "cfg2_small"])
 def test_scan_entropy_matches_oracle_and_gold(gepi, tmp_path, name, method):
     doc = H.load_golden(name)
     base = H.golden_input(doc, str(tmp_path))
@@ -243,6 +244,73 @@ def test_scan_fisher_matches_oracle(gepi, tmp_path, kw, method):
                              rtol=FISHER_RTOL * 10)
     assert not probs, probs[:5]
     pl.close()
+
+
+def _device_value_errors(gepi, rows, got, values, objective):
+    """Largest |d ln p| (Fisher) or relative error of I (entropy) of the
+    device's FP64 values against the oracle's FP64 restatements
+    (fisher_p.c:52-76 with R's tie rule; entropyDelta4, entropy_inline.h:30-80)."""
+    lib = H.oracle()
+    worst = 0.0
+    for t, v in zip(got, values):
+        w, x, y, z = (int(q) for q in t["n"])
+        if w * z == x * y:  # zero-filled slot
+            assert v == 0.0
+            continue
+        if objective == 1:
+            ref = lib.orc_fisher_log10p(w, y - w, x, z - x, 0)
+            assert math.isfinite(ref)
+            worst = max(worst, abs(v - ref) * math.log(10.0))
+        else:
+            ref = lib.orc_entropy_f64(w, x, y, z)  # entropyDelta4: -I bits, the sign of `ent`
+            worst = max(worst, abs(v - ref) / abs(ref))
+        assert np.float32(v) == np.float32(t["ent"])
+    return worst
+
+
+@pytest.mark.parametrize("method", sorted(METHODS))
+@pytest.mark.parametrize("kw", [
+    dict(n_snps=60, n_cases=70, n_controls=65, missing=0.02, seed=81),
+    dict(n_snps=40, n_cases=300, n_controls=420, missing=0.05, n_planted=2, seed=82),
+    dict(n_snps=120, n_cases=1500, n_controls=1700, missing=0.01, n_planted=2, seed=83),
+])
+def test_device_fp64_values_within_tolerance(gepi, tmp_path, kw, method):
+    """The device's FP64 objective of every returned test, before the float
+    rounding of the output field: Fisher p within 1e-9 relative
+    (|d ln p| <= 1e-9) of the oracle's FP64 Fisher, entropy within 1e-6
+    relative of the FP64 entropyDelta4 restatement."""
+    pl, rows, fs, _ = make_planes(gepi, kw, tmp_path)
+    k = 150
+    got = pl.scan(k, objective=gepi.FISHER, method=METHODS[method])
+    err_f = _device_value_errors(gepi, rows, got, pl.last_values(k), 1)
+    assert err_f <= FISHER_RTOL, err_f
+    got = pl.scan(k, objective=gepi.ENTROPY, method=METHODS[method])
+    err_e = _device_value_errors(gepi, rows, got, pl.last_values(k), 0)
+    assert err_e <= 1e-6, err_e
+    print(f"max device error: Fisher |d ln p| {err_f:.3e}, entropy rel {err_e:.3e}")
+    pl.close()
+
+
+def test_device_fisher_fp64_config2_full_size(gepi):
+    """Config 2 at full size (20,000 SNPs x 4,000 samples, 3 planted pairs),
+    Fisher top-1,000 through both counting kernels: the same list, and every
+    returned p within 1e-9 relative of the oracle's FP64 Fisher."""
+    spec = gepi.SynthSpec(n_snps=20000, n_cases=2000, n_controls=2000, maf_lo=0.01, maf_hi=0.5,
+                          missing=0.01, n_planted=3, odds_ratio=2.0, seed=1002)
+    bed, ph, _ = gepi.synth_bed(spec)
+    fs = H.Fileset(bed=bed, pheno=ph, n_lines=spec.n_snps, bim=[])
+    rows = H.decode_rows(fs)
+    k = 1000
+    worst = 0.0
+    with gepi.Planes.from_bed(bed, spec.n_snps, ph) as pl:
+        lists = []
+        for method in (2, 1):
+            got = pl.scan(k, objective=gepi.FISHER, method=method)
+            worst = max(worst, _device_value_errors(gepi, rows, got, pl.last_values(k), 1))
+            lists.append(got)
+    assert lists[0].tobytes() == lists[1].tobytes()
+    assert worst <= FISHER_RTOL, worst
+    print(f"config 2 Fisher top-{k}: max |d ln p| {worst:.3e}")
 
 
 def test_config2_scale_properties(gepi):

@@ -47,9 +47,10 @@ def test_result_layout_matches_interaction_result(gepi):
 @pytest.mark.parametrize("name", [n for n in H.golden_names()])
 def test_generator_reproduces_golden_inputs(name, gepi, tmp_path):
     doc = H.load_golden(name)
-    if doc["kind"] != "synthetic":
-        pytest.skip("reference data case")
-    H.golden_input(doc, str(tmp_path))  # asserts sha256 of .bed/.bim/.fam
+    # synthetic cases are regenerated, the reference's demo filesets read from
+    # tests/golden/data; either way the sha256 of .bed/.bim/.fam must be the
+    # one the golden output was made from
+    H.golden_input(doc, str(tmp_path))
 
 
 def test_synth_bed_matches_written_file(gepi, tmp_path):
@@ -79,9 +80,7 @@ def test_reader_matches_oracle_decode(gepi, tmp_path):
 
 
 def test_reader_on_reference_demo_data(gepi):
-    base = os.path.join(H.REFERENCE_ROOT, "data", "thinhap1")
-    if not os.path.exists(base + ".bed"):
-        pytest.skip("reference data files not present")
+    base = os.path.join(H.GOLDEN_DATA_DIR, "thinhap1")
     r = gepi.BinPlinkReader(base)
     assert r.checkConsistency() and r.readData()
     bits, valid, m1, m2 = H.decode_rows(H.read_fileset(base))

@@ -74,6 +74,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cstdint>
+#include <cstdlib>
 
 #include "device.cuh"
 
@@ -124,7 +125,18 @@ static_assert(kTcSfCol + 32 <= kTcCols, "tensor memory budget");
 static_assert(kTcBWarps * 32 == 2 * kTcBRows && kTcBWarps <= kTcProducerWarps, "B pieces");
 static_assert(kTcHalfWords == 4 || kTcHalfWords == 6,
               "a producer thread stores 16 or 24 tensor-memory columns");
-constexpr long long kTcWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
+// Clock budget of every wait on another role's progress (~2 s at 2 GHz).  The
+// kernel takes it as an argument: the library passes this value.  Waits for
+// this CTA's own copies and MMAs on the way out (mbar_drain) always use the
+// full budget, so nothing lands in a CTA's memory after it has exited.
+//
+// Timeout test (GEPI_DEBUG_STALL=<cycles>, tests only): the producers of both
+// CTAs withhold their arrivals on the first chunk's full barrier -- a flag
+// that nothing else sets -- and every wait gives up after <cycles>.  The MMA
+// thread's wait for that stage then runs out, the CTA pair takes the abort
+// path (drain, final cluster barrier, tensor-memory free) and the host reads
+// GEPI_ERR_TIMEOUT; nothing faults and the context stays usable.
+constexpr long long kTcWaitCycles = 4000000000ll;
 static_assert(kTcPStageBytes % 128 == 0 && kTcPABytes % 128 == 0 && kTcPOff % 128 == 0,
               "TMA destinations 128-byte aligned");
 static_assert(kTcSmem > 114 * 1024 && kTcSmem <= 227 * 1024,
@@ -174,12 +186,12 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t b
 
 // Bounded wait; false when the CTA aborts or the clock budget runs out.
 __device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity, volatile int *abort_flag,
-                                          int *err, int code) {
+                                          int *err, int code, long long budget) {
     if (mbar_try(b, parity)) return true;
     const long long t0 = clock64();
     while (!mbar_try(b, parity)) {
         if (*abort_flag) return false;
-        if (clock64() - t0 > kTcWaitCycles) {
+        if (clock64() - t0 > budget) {
             *abort_flag = 1;
             atomicCAS(err, 0, code);
             return false;
@@ -219,12 +231,18 @@ __device__ __forceinline__ void cluster_sync_all() {
                  "barrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
-// Warp-wide bounded wait: every lane polls the same barrier, so the warp
-// never diverges (a lane-0 poll plus a broadcast costs a reconvergence per
-// wait).
+// Warp-wide bounded wait: every lane polls the same barrier (a lane-0 poll
+// plus a broadcast costs a reconvergence per wait), then the warp votes.  The
+// lanes' own results can differ -- one lane's clock runs out or it sees the
+// abort flag in the same instant another lane's try_wait succeeds -- and a
+// warp whose lanes split there would reach the .sync.aligned tcgen05.st/ld
+// that follow with part of the warp gone.  With the vote the whole warp goes
+// on, or the whole warp gives up.
 __device__ __forceinline__ bool mbar_wait_warp(uint64_t *b, uint32_t parity,
-                                               volatile int *abort_flag, int *err, int code) {
-    return mbar_wait(b, parity, abort_flag, err, code);
+                                               volatile int *abort_flag, int *err, int code,
+                                               long long budget) {
+    const bool ok = mbar_wait(b, parity, abort_flag, err, code, budget);
+    return __all_sync(0xffffffffu, ok);
 }
 
 // One arrival per warp, by a lane elected in-line (predicated, no branch).
@@ -455,7 +473,8 @@ template <bool DUMP, int OBJ>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
     tc_tile_kernel(const uint32_t *__restrict__ blk, int rows_pad, int Wp, int W0,
                    const int2 *__restrict__ tiles, int ntiles, int a0, int a1, int b0, int b1,
-                   ScanCtx ctx, uint32_t *__restrict__ dump, int *err) {
+                   ScanCtx ctx, uint32_t *__restrict__ dump, int *err, long long wait_cycles,
+                   int stall) {
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     __shared__ uint64_t pfull_bar[kTcPStages], pempty_bar[kTcPStages], full_bar[kTcStages],
         empty_bar[kTcStages], dfull_bar[2], dempty_bar[2], fin_bar;
@@ -538,7 +557,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
         unsigned char *bst0 = tc_smem + (u >> 3) * kTcSbo + (HW * hb) * kTcLbo + (u & 7) * 16;
         for (int idx = 0; idx < total; ++idx) {
             const uint32_t j = (uint32_t)idx % kTcPStages, s = (uint32_t)idx % kTcStages;
-            if (!mbar_wait_warp(&pfull_bar[j], ((uint32_t)idx / kTcPStages) & 1, vabort, err, 5)) break;
+            if (!mbar_wait_warp(&pfull_bar[j], ((uint32_t)idx / kTcPStages) & 1, vabort, err, 5,
+                                wait_cycles))
+                break;
             const unsigned char *pk = tc_smem + kTcPOff + (size_t)j * kTcPStageBytes;
             // every lane loads (lanes 30, 31 re-read row 30q+29 and clear it): no divergence
             uint2 pa[HW / 2], pb[HW / 2];
@@ -574,7 +595,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
                     expand_word(pb[m].y, o + 8 * m + 4);
                 }
             }
-            if (!mbar_wait_warp(&empty_bar[s], (((uint32_t)idx / kTcStages) & 1) ^ 1, vabort, err, 1))
+            if (!mbar_wait_warp(&empty_bar[s], (((uint32_t)idx / kTcStages) & 1) ^ 1, vabort, err, 1,
+                                wait_cycles))
                 break;
             tc_fence_after();
             tmem_st16(ta0 + s * kTcAStageCols, r);
@@ -590,7 +612,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             tc_fence_before();
             __syncwarp();
-            mbar_arrive_warp_cl(cluster_addr(&full_bar[s], 0));
+            if (!(stall && idx == 0)) mbar_arrive_warp_cl(cluster_addr(&full_bar[s], 0));
         }
     } else if (warp == kTcTmaWarp) {
         // ---------------- bulk-copy issuer ----------------
@@ -607,7 +629,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
                     if (k + 1 < my_tiles) tl_next = tiles[pair + (k + 1) * npairs];
                 }
                 const uint32_t j = (uint32_t)idx % kTcPStages;
-                if (!mbar_wait(&pempty_bar[j], (((uint32_t)idx / kTcPStages) & 1) ^ 1, vabort, err, 6))
+                if (!mbar_wait(&pempty_bar[j], (((uint32_t)idx / kTcPStages) & 1) ^ 1, vabort, err, 6,
+                               wait_cycles))
                     break;
                 unsigned char *pk = tc_smem + kTcPOff + (size_t)j * kTcPStageBytes;
                 const uint32_t *base = blk + (size_t)c * rows_pad * kTcChunkWords;
@@ -640,7 +663,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
                         // both CTAs' epilogues have copied this class half of the
                         // previous tile's accumulator out (while the other half was
                         // being accumulated): the tensor pipe never drains between tiles
-                        if (!mbar_wait(&dempty_bar[cls], (lt & 1) ^ 1, vabort, err, 2)) {
+                        if (!mbar_wait(&dempty_bar[cls], (lt & 1) ^ 1, vabort, err, 2, wait_cycles)) {
                             ok = false;
                             break;
                         }
@@ -652,7 +675,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
                     const uint32_t acc0 = (c == 0 || c == cm.n0) ? 0u : 1u;
                     const uint32_t a = tbase + kTcACol + s * kTcAStageCols;
                     const uint64_t bd = bdesc0 + (uint64_t)((s * (uint32_t)kTcBStageBytes) >> 4);
-                    if (!mbar_wait(&full_bar[s], (gc / kTcStages) & 1, vabort, err, 3)) {
+                    if (!mbar_wait(&full_bar[s], (gc / kTcStages) & 1, vabort, err, 3, wait_cycles)) {
                         ok = false;
                         break;
                     }
@@ -697,7 +720,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
             // copy each class half out as soon as its MMAs are done and hand it
             // back: the tensor pipe goes on with the other half, then the next tile
             for (int cls = 0; cls < 2; ++cls) {
-                if (!mbar_wait_warp(&dfull_bar[cls], lt & 1, vabort, err, 4)) {
+                if (!mbar_wait_warp(&dfull_bar[cls], lt & 1, vabort, err, 4, wait_cycles)) {
                     live = false;
                     break;
                 }
@@ -857,8 +880,17 @@ static cudaError_t launch_tc_pairs(const uint32_t *blk, int rows_pad, int Wp, in
         if (dev < 64) resident[dev].store(pairs);
     }
     pairs = std::max(1, std::min(pairs, ntiles));
+    long long wait_cycles = kTcWaitCycles;
+    int stall = 0;
+    if (const char *w = std::getenv("GEPI_DEBUG_STALL")) {
+        const long long v = std::atoll(w);
+        if (v > 0) {
+            wait_cycles = std::min(v, kTcWaitCycles);
+            stall = 1;
+        }
+    }
     kern<<<2 * pairs, kTcThreads, kTcSmem, stream>>>(blk, rows_pad, Wp, W0, tiles, ntiles, a0, a1,
-                                                    b0, b1, ctx, dump, err);
+                                                    b0, b1, ctx, dump, err, wait_cycles, stall);
     return cudaGetLastError();
 }
 

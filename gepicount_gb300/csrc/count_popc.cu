@@ -157,25 +157,22 @@ cudaError_t launch_popc_tiles(const uint32_t *planes, int Wp, int W0, const int2
                               int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
                               uint32_t *dump, cudaStream_t stream) {
     if (ntiles <= 0) return cudaSuccess;
-    static bool attr_set[2] = {false, false};
+    // The shared-memory opt-in above 48 KB is a property of the current
+    // device's context, so it is set on every launch (a cheap host call) rather
+    // than cached once per process: a process that scans on several GPUs, or
+    // from several host threads, gets it on each device.
     if (dump) {
-        if (!attr_set[1]) {
-            cudaError_t e = cudaFuncSetAttribute(popc_tile_kernel<true>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)kPopcSmem);
-            if (e != cudaSuccess) return e;
-            attr_set[1] = true;
-        }
+        cudaError_t e = cudaFuncSetAttribute(popc_tile_kernel<true>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kPopcSmem);
+        if (e != cudaSuccess) return e;
         popc_tile_kernel<true><<<ntiles, kPopcThreads, kPopcSmem, stream>>>(
             planes, Wp, W0, tiles, a0, a1, b0, b1, ctx, dump);
     } else {
-        if (!attr_set[0]) {
-            cudaError_t e = cudaFuncSetAttribute(popc_tile_kernel<false>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)kPopcSmem);
-            if (e != cudaSuccess) return e;
-            attr_set[0] = true;
-        }
+        cudaError_t e = cudaFuncSetAttribute(popc_tile_kernel<false>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kPopcSmem);
+        if (e != cudaSuccess) return e;
         popc_tile_kernel<false><<<ntiles, kPopcThreads, kPopcSmem, stream>>>(
             planes, Wp, W0, tiles, a0, a1, b0, b1, ctx, nullptr);
     }

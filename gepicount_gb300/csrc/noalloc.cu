@@ -10,20 +10,27 @@
 // scoring tables, tile list, candidate buffers, scan state, output records --
 // is carved from ONE file-scope device array, g_noalloc_scratch, of
 // kNoAllocScratchBytes (32 MiB).  Every GPU that loads the library holds that
-// array until the process exits.  No cudaMalloc, cudaFree, cudaMallocHost,
-// stream or event creation and no host heap allocation happen on this path:
-// tables and the class permutation are built by kernels, the final ranking is
-// done on the device, and only the k result records are copied back.
+// array until the process exits.  On success no cudaMalloc, cudaFree,
+// cudaMallocHost, stream or event creation and no host heap allocation happen
+// on this path: the class permutation and tile list are built by kernels, the
+// log-factorial tables are computed on the host in fixed-size chunks on the
+// stack (the same std::lgamma values gepi_process_gpu_1 uses, so both entry
+// points give the same bits for either objective), the final ranking is done
+// on the device, and only the k result records are copied back.  Error returns
+// record their message in a std::string (heap); only the success path is
+// allocation-free.
 //
 // Limits: the inputs, planes and tables must fit the array next to the
 // candidate buffers (two buffers of kNoAllocCap = 65,536 records), and
 // k <= kNoAllocCap / 4; larger requests return GEPI_ERR_LIMIT before any
 // device work.
 //
-// Set-up: the first call on a device, with that device current, looks up the
-// array's device address with cudaGetSymbolAddress (the host-side symbol is
-// only a stand-in and must not be passed to a kernel).  Make that first call
-// before any stream capture.
+// Device address: the host-side symbol g_noalloc_scratch is only a stand-in
+// and must never be passed to a kernel.  Every call, with the caller's device
+// made current, looks the array's device address up with
+// cudaGetSymbolAddress (a cheap host call) and checks its return code, so a
+// context torn down and rebuilt between calls (cudaDeviceReset) never leaves a
+// stale address behind.
 //
 // Sharing: every call on a device uses the same array and finds the previous
 // call's contents there; the call initialises everything it reads (scan state,
@@ -36,8 +43,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
-#include <mutex>
 
 #include "common.h"
 #include "device.cuh"
@@ -65,21 +72,14 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 namespace {
 
-std::mutex g_setup_mu;
-unsigned char *g_scratch_ptr[kMaxDevices] = {};
-
-// Device address of the scratch array on `dev` (looked up once per device).
+// Device address of the scratch array on the current device `dev`.
 gepi_status scratch_address(int dev, unsigned char **out) {
     if (dev < 0 || dev >= kMaxDevices) return set_error(GEPI_ERR_ARG, "device ordinal out of range");
-    std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_ptr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess)
-            return set_error(GEPI_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        g_scratch_ptr[dev] = static_cast<unsigned char *>(p);
-    }
-    *out = g_scratch_ptr[dev];
+    void *p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+        return set_error(GEPI_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    *out = static_cast<unsigned char *>(p);
     return GEPI_OK;
 }
 
@@ -113,13 +113,31 @@ __device__ uint64_t na_log2_fixed(uint64_t n, int F) {
     return ((uint64_t)e << F) + r;
 }
 
-__global__ void na_tables_kernel(uint64_t *T, double *lf, float *lf32, int nmax, int F) {
-    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n <= nmax; n += gridDim.x * blockDim.x) {
+__global__ void na_tfix_kernel(uint64_t *T, int nmax, int F) {
+    for (int n = blockIdx.x * blockDim.x + threadIdx.x; n <= nmax; n += gridDim.x * blockDim.x)
         T[n] = (uint64_t)n * na_log2_fixed((uint64_t)n, F);
-        const double v = lgamma((double)n + 1.0);
-        lf[n] = v;
-        lf32[n] = (float)v;
+}
+
+// log(n!) for n in [0, nmax] as double and float, computed on the host with
+// std::lgamma (the values build_lfact gives the allocating scan) in chunks of
+// kLfChunk on the stack, each copied to the device synchronously.
+constexpr int kLfChunk = 2048;
+cudaError_t upload_lfact(double *lf, float *lf32, int nmax) {
+    double hd[kLfChunk];
+    float hf[kLfChunk];
+    for (int n0 = 0; n0 <= nmax; n0 += kLfChunk) {
+        const int cnt = std::min(kLfChunk, nmax + 1 - n0);
+        for (int i = 0; i < cnt; ++i) {
+            const double v = std::lgamma((double)(n0 + i) + 1.0);
+            hd[i] = v;
+            hf[i] = (float)v;
+        }
+        cudaError_t e = cudaMemcpy(lf + n0, hd, (size_t)cnt * sizeof(double), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess)
+            e = cudaMemcpy(lf32 + n0, hf, (size_t)cnt * sizeof(float), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return e;
     }
+    return cudaSuccess;
 }
 
 // Class-sorted permutation from the two class masks (one block): slot j of
@@ -187,7 +205,11 @@ __device__ __forceinline__ bool na_better(const Cand &a, const Cand &b) {
 
 // Final ranking on the device: the rank of each survivor is the number of
 // survivors that beat it under (key desc, sA, sB, fun); ranks < k are written
-// as result records, slots with no survivor are zeroed.
+// as result records, slots with no survivor are zeroed.  The survivors are the
+// compacted candidates: at most k plus the tests tied with the k-th key, so
+// the all-pairs count is about k^2 (2.7e8 comparisons at k = 16,384); only
+// massive ties at the k-th key (up to the 65,536-record buffer) make it
+// larger.
 __global__ void na_rank_kernel(const Cand *cand, const ScanState *st, int k, gepi_result *out) {
     const uint32_t n = min(st->count, kNoAllocCap);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < k; i += gridDim.x * blockDim.x)
@@ -313,8 +335,9 @@ extern "C" gepi_status gepi_process_gpu_1_noalloc(const uint64_t *bits, const ui
     GEPI_CUDA(cudaMemcpy(d_m1, mask1, (size_t)n_words * 8, cudaMemcpyHostToDevice));
     GEPI_CUDA(cudaMemcpy(d_m2, mask2, (size_t)n_words * 8, cudaMemcpyHostToDevice));
     const int F = tfix_bits(nmax);
-    na_tables_kernel<<<num_sms, 256, 0, stream>>>(d_T, d_lf, d_lf32, nmax, F);
+    na_tfix_kernel<<<num_sms, 256, 0, stream>>>(d_T, nmax, F);
     GEPI_CUDA(cudaGetLastError());
+    GEPI_CUDA(upload_lfact(d_lf, d_lf32, nmax));
     na_perm_kernel<<<1, 1024, 0, stream>>>(d_m1, d_m2, n_words, W0, Wp, d_perm);
     GEPI_CUDA(cudaGetLastError());
     GEPI_CUDA(launch_decode_rows(d_bits, d_valid, n_words, n_snps, d_perm, Wp, d_planes, stream,
@@ -364,6 +387,8 @@ extern "C" gepi_status gepi_process_gpu_1_noalloc(const uint64_t *bits, const ui
             GEPI_CUDA(cudaMemcpy(&st, d_state, sizeof st, cudaMemcpyDeviceToHost));
             count = st.count;
             batch = std::max<size_t>(1, nbt / 2);
+            if (par->verbose)
+                std::fprintf(stderr, "gepi: candidate overflow, batch -> %zu tiles\n", batch);
             continue;
         }
         const uint32_t appended = st.count - count;

@@ -15,9 +15,12 @@ HWE genotypes with MAF ~ U(0.01, 0.5), 1% missing, 10 planted pairs, top-10,000
           plane set each step (mean step time; the slowest step is reported).
 
 `--impl reference` times the reference's CPU gold loop (the oracle's
-restatement of proc_gold_1.h:98-134, all host threads) on a bounded leading
-sub-triangle of the same workload.  Under torchrun every rank scans its own
-cohort (weak scaling: seed + rank, no collective on the data path).
+restatement of proc_gold_1.h:68-178 with its lookup-table popcount and 2 x
+topmost result buffer, all host threads) on a bounded leading sub-triangle of
+the same workload.  That arm never loads the scan library: its input fileset
+is written by the stand-alone generator tool (gepi-synth) and read back from
+disk.  Under torchrun every rank scans its own cohort (weak scaling: seed +
+rank, no collective on the data path).
 """
 from __future__ import annotations
 
@@ -135,6 +138,35 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
+# DRAM bytes per 80 x 64 tile of tc_tile_kernel at 10,000 samples, from one ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum of a whole launch / its
+# tiles); the operand blocks are re-read from L2, so traffic grows with the tiles
+# a launch processes and roofline.traffic scales it to the average launch.
+TC_DRAM_BYTES_PER_TILE = None
+
+
+def synth_fileset(cfg: dict, seed: int) -> str:
+    """BASE of the workload's fileset, written once per host by the stand-alone
+    generator (no CUDA, no scan library) into the temp directory."""
+    import tempfile
+
+    tool = os.path.join(HERE, "gepicount_gb300", "_build", "gepi-synth")
+    if not os.path.exists(tool):
+        subprocess.run([sys.executable, "-m", "gepicount_gb300.build"], cwd=HERE, check=True,
+                       stdout=subprocess.DEVNULL)
+    d = os.path.join(tempfile.gettempdir(), "gepi_bench_inputs")
+    os.makedirs(d, exist_ok=True)
+    base = os.path.join(d, f"n{cfg['n_snps']}_s{cfg['n_cases']}_{cfg['n_controls']}_seed{seed}")
+    if not os.path.exists(base + ".fam"):
+        args = [str(v) for v in (cfg["n_snps"], cfg["n_cases"], cfg["n_controls"], cfg["maf_lo"],
+                                 cfg["maf_hi"], cfg["missing"], cfg["n_planted"],
+                                 cfg.get("odds_ratio", 2.0), seed)]
+        subprocess.run([tool, base + ".tmp", *args], check=True)
+        for ext in ("bed", "bim", "fam"):  # .fam last: its presence marks a complete set
+            os.replace(base + ".tmp." + ext, base + "." + ext)
+    return base
+
+
 def cpu_baseline(cfg: dict, bed, ph, target_s: float, threads: int):
     """Time the reference gold loop (oracle restatement) on a leading
     sub-triangle sized to about target_s seconds."""
@@ -152,22 +184,25 @@ def cpu_baseline(cfg: dict, bed, ph, target_s: float, threads: int):
     sub = H.Fileset(bed=bed[: 3 + n_lines * ((ph.size + 3) // 4)], pheno=ph, n_lines=n_lines, bim=[])
     bits, valid, m1, m2 = H.decode_rows(sub)
     chk = H.ctypes.c_double()
+    k = cfg["k"]
     t0 = time.perf_counter()
-    lib.orc_gold_loop(H.ptr(bits), H.ptr(valid), H.ptr(m1), H.ptr(m2), nw, 0, probe_rows, threads,
-                      H.ctypes.byref(chk))
+    lib.orc_gold_loop(H.ptr(bits), H.ptr(valid), H.ptr(m1), H.ptr(m2), nw, 0, probe_rows, k,
+                      threads, H.ctypes.byref(chk))
     dt = max(time.perf_counter() - t0, 1e-6)
     per_pair = dt / (probe_rows * (probe_rows + 1) / 2)
     want_pairs = target_s / per_pair
     r1 = int(min(2 * n_lines, max(probe_rows, (2 * want_pairs) ** 0.5)))
     t0 = time.perf_counter()
-    row_pairs = lib.orc_gold_loop(H.ptr(bits), H.ptr(valid), H.ptr(m1), H.ptr(m2), nw, 0, r1,
+    row_pairs = lib.orc_gold_loop(H.ptr(bits), H.ptr(valid), H.ptr(m1), H.ptr(m2), nw, 0, r1, k,
                                   threads, H.ctypes.byref(chk))
     dt = time.perf_counter() - t0
     snp_pairs = row_pairs / 4.0
     return dict(value=snp_pairs / dt, unit=UNIT, seconds=dt, rows=r1,
                 sample=(f"allele rows 0..{r1 - 1} against every row <= them (leading "
                         f"sub-triangle, {row_pairs:,} row pairs = {snp_pairs:,.0f} SNP-pair "
-                        f"equivalents) of the same workload, 5 functions, float entropy"))
+                        f"equivalents) of the same workload: 5 functions, popcount through "
+                        f"the reference's 64K lookup table, float entropy, 2 x {k:,} result "
+                        f"buffer sorted when full (C restatement of proc_gold_1.h:68-178)"))
 
 
 def run_reference(args, cfg):
@@ -176,11 +211,10 @@ def run_reference(args, cfg):
         return 0
     import numpy as np
 
-    import gepicount_gb300 as g
-
-    g.lib()
-    spec = g.SynthSpec(**{k: v for k, v in cfg.items() if k != "k"})
-    bed, ph, _ = g.synth_bed(spec)
+    base = synth_fileset(cfg, cfg["seed"])
+    bed = np.fromfile(base + ".bed", dtype=np.uint8)
+    ph = np.array([int(line.split()[5]) for line in open(base + ".fam") if len(line) >= 5],
+                  dtype=np.int32)
     threads = os.cpu_count() or 1
     vals = []
     for i in range(args.warmup + args.steps):
@@ -293,8 +327,11 @@ def run_ours(args, cfg):
         peak = float(peaks.get("bf16_tflops", 1900.0))
         peak_src = f"{peak_kind} dense bf16 (burst)"
     kname = "tc_tile_kernel" if tensor else "popc_tile_kernel"
+    tiles_per_launch = sum(s["tiles"] for s in stats) / max(1, nlaunch)
+    traffic = (TC_DRAM_BYTES_PER_TILE * tiles_per_launch
+               if tensor and TC_DRAM_BYTES_PER_TILE and n_samples == 10000 else None)
     roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-            "frac": achieved / peak, "traffic": None, "kernel": kname, "peak_source": peak_src,
+            "frac": achieved / peak, "traffic": traffic, "kernel": kname, "peak_source": peak_src,
             "bf16_measured_tflops": float(peaks.get("bf16_tflops", 1900.0)),
             "work": "2 x 9 x samples ops per SNP pair (0/1 Gram), per launch",
             "avg_launch_ms": avg_launch_s * 1e3, "launches": nlaunch}
@@ -311,7 +348,7 @@ def run_ours(args, cfg):
     planes.close()
     e2e_times = []
     d2h = k * 48
-    for i in range(max(1, min(args.steps, 3))):
+    for i in range(max(1, args.steps)):
         barrier()
         t1 = time.perf_counter()
         with g.Planes.from_bed(bed, spec.n_snps, ph, device=local) as pl:

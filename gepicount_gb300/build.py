@@ -1,6 +1,6 @@
 """Build recipe for the native library and the CLI (no cmake).
 
-    python -m gepicount_gb300.build          # -> gepicount_gb300/_build/libgepi.so, gepi
+    python -m gepicount_gb300.build          # -> gepicount_gb300/_build/libgepi.so, gepi, gepi-synth
 
 Every CUDA translation unit is compiled for sm_103a only
 (-gencode arch=compute_103a,code=sm_103a), host code with -ffp-contract=off so
@@ -22,12 +22,14 @@ OUT = os.path.join(PKG, "_build")
 OBJ = os.path.join(OUT, "obj")
 LIB = os.path.join(OUT, "libgepi.so")
 CLI = os.path.join(OUT, "gepi")
+SYNTH = os.path.join(OUT, "gepi-synth")  # the data generator alone (no CUDA)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["scan.cu", "decode.cu", "count_popc.cu", "select.cu", "noalloc.cu", "count_tc.cu",
               "engine.cu"]
 CPP_SOURCES = ["plink.cpp", "synth.cpp", "tables.cpp"]
 CLI_SOURCES = ["cli.cpp"]
+SYNTH_SOURCES = ["synth.cpp", "synth_main.cpp"]
 HOST_FLAGS = ["-O2", "-fPIC", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-Wall",
               "-Wno-unused-function"]
 
@@ -90,6 +92,9 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     if cli_srcs and _stale(CLI, cli_srcs + heads + [LIB]):
         _run(["g++", *HOST_FLAGS, *cli_srcs, "-o", CLI, f"-L{OUT}", "-lgepi",
               "-Wl,-rpath,$ORIGIN"], verbose)
+    synth_srcs = [os.path.join(CSRC, s) for s in SYNTH_SOURCES]
+    if _stale(SYNTH, synth_srcs + heads):
+        _run(["g++", *HOST_FLAGS, *synth_srcs, "-o", SYNTH], verbose)
     return LIB
 
 

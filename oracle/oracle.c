@@ -446,15 +446,55 @@ int64_t orc_scan_topk(const uint64_t *bits, const uint64_t *valid, const uint64_
 }
 
 /* ------------------------------------------------------------------------- */
-/* CPU baseline: the reference gold loop body (proc_gold_1.h:98-134).          */
+/* CPU baseline: the reference gold loop (proc_gold_1.h:68-178) with its own   */
+/* cost model: masks per row pair, 5 binFunc calls (proc_gold.h:38-71) whose   */
+/* popcounts go through the 64K-entry byte table of bitops.h:33-62 (four       */
+/* lookups per 64-bit word), float entropyDelta4, and the 2 x topmost result   */
+/* buffer: a test better than the current limit is stored, and a full buffer   */
+/* is sorted by score and cut back to topmost (proc_gold_1.h:114-137).  With   */
+/* threads > 1 every thread keeps its own buffer over its share of the rows.   */
 /* ------------------------------------------------------------------------- */
+static unsigned char orc_bits_in16[65536];
+static int orc_bits_ready = 0;
+
+static void orc_bits_init(void) {
+    if (orc_bits_ready) return;
+    for (int j = 0; j < 65536; ++j) {
+        int c = 0, v = j;
+        while (v) {
+            ++c;
+            v &= v - 1;
+        }
+        orc_bits_in16[j] = (unsigned char)c;
+    }
+    orc_bits_ready = 1;
+}
+
+static inline int orc_bits_lut(uint64_t a) {
+    return orc_bits_in16[a & 0xffff] + orc_bits_in16[(a >> 16) & 0xffff] +
+           orc_bits_in16[(a >> 32) & 0xffff] + orc_bits_in16[a >> 48];
+}
+
+typedef struct {
+    float ent;
+    int32_t sA, sB, fun;
+    int32_t n[4];
+} orc_gold_item;
+
+static int orc_gold_cmp(const void *a, const void *b) {
+    const float x = ((const orc_gold_item *)a)->ent, y = ((const orc_gold_item *)b)->ent;
+    return x < y ? -1 : (x > y ? 1 : 0);
+}
+
 int64_t orc_gold_loop(const uint64_t *bits, const uint64_t *valid, const uint64_t *mask1,
-                      const uint64_t *mask2, int n_words, int r0, int r1, int threads,
-                      double *checksum) {
+                      const uint64_t *mask2, int n_words, int r0, int r1, int topmost,
+                      int threads, double *checksum) {
     int nt = 1;
 #ifdef _OPENMP
     nt = threads > 0 ? threads : omp_get_max_threads();
 #endif
+    if (topmost < 1) topmost = 1;
+    orc_bits_init();
     int64_t pairs = 0;
     double acc = 0.0;
 #ifdef _OPENMP
@@ -463,7 +503,9 @@ int64_t orc_gold_loop(const uint64_t *bits, const uint64_t *valid, const uint64_
     {
         uint64_t *am0 = (uint64_t *)malloc((size_t)n_words * 8);
         uint64_t *am1 = (uint64_t *)malloc((size_t)n_words * 8);
+        orc_gold_item *buf = (orc_gold_item *)calloc((size_t)2 * topmost, sizeof(orc_gold_item));
         float worst = 3.0e38f;
+        int widx = -1;
 #ifdef _OPENMP
 #pragma omp for schedule(dynamic, 1)
 #endif
@@ -479,20 +521,35 @@ int64_t orc_gold_loop(const uint64_t *bits, const uint64_t *valid, const uint64_
                     int w = 0, x = 0, y = 0, z = 0;
                     for (int m = 0; m < n_words; ++m) {
                         uint64_t c = bfun(a[m], b[m], fun);
-                        w += __builtin_popcountll(c & am0[m]);
-                        x += __builtin_popcountll(c & am1[m]);
-                        y += __builtin_popcountll(am0[m]);
-                        z += __builtin_popcountll(am1[m]);
+                        w += orc_bits_lut(c & am0[m]);
+                        x += orc_bits_lut(c & am1[m]);
+                        y += orc_bits_lut(am0[m]);
+                        z += orc_bits_lut(am1[m]);
                     }
                     float ee = orc_entropy_ref_f32(w, x, y, z);
                     if (ee < worst) {
-                        acc += ee;
-                        if (ee < -0.05f) worst = ee;
+                        if (widx >= 2 * topmost - 1) {
+                            qsort(buf, (size_t)2 * topmost, sizeof(orc_gold_item), orc_gold_cmp);
+                            widx = topmost - 1;
+                            worst = buf[widx].ent;
+                            if (!(ee < worst)) continue;
+                        }
+                        orc_gold_item *it = &buf[++widx];
+                        it->ent = ee;
+                        it->sA = j;
+                        it->sB = k;
+                        it->fun = fun;
+                        it->n[0] = w;
+                        it->n[1] = x;
+                        it->n[2] = y;
+                        it->n[3] = z;
                     }
                 }
                 ++pairs;
             }
         }
+        for (int i = 0; i <= widx; ++i) acc += buf[i].ent;
+        free(buf);
         free(am0);
         free(am1);
     }

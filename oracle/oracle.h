@@ -80,12 +80,14 @@ int64_t orc_scan_topk_range(const uint64_t *bits, const uint64_t *valid,
                             int ra0, int ra1, int rb0, int rb1, int objective, int k,
                             orc_result *tops, double *keys, int threads);
 
-/* The reference's gold loop cost model for a CPU baseline: processes rows
- * [r0, r1) against all rB <= rA exactly as proc_gold_1.h:98-134 does (masks,
- * 5 binFunc calls, float entropyDelta4) and returns the number of row pairs. */
+/* The reference's gold loop for a CPU baseline: processes rows [r0, r1)
+ * against all rB <= rA as proc_gold_1.h:68-178 does (masks, 5 binFunc calls
+ * with the 64K-entry popcount table of bitops.h:33-62, float entropyDelta4,
+ * the 2 x topmost result buffer sorted when full) and returns the number of
+ * row pairs. */
 int64_t orc_gold_loop(const uint64_t *bits, const uint64_t *valid, const uint64_t *mask1,
-                      const uint64_t *mask2, int n_words, int r0, int r1, int threads,
-                      double *checksum);
+                      const uint64_t *mask2, int n_words, int r0, int r1, int topmost,
+                      int threads, double *checksum);
 
 #ifdef __cplusplus
 }

@@ -58,7 +58,8 @@ class GepiError(RuntimeError):
 class _Params(ctypes.Structure):
     _fields_ = [("gpu_num", ctypes.c_int32), ("topmost", ctypes.c_int32),
                 ("objective", ctypes.c_int32), ("method", ctypes.c_int32),
-                ("verbose", ctypes.c_int32), ("reserved", ctypes.c_int32 * 7)]
+                ("verbose", ctypes.c_int32), ("variant", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 6)]
 
 
 class _SynthSpec(ctypes.Structure):
@@ -76,14 +77,25 @@ class _ScanStats(ctypes.Structure):
                 ("overflows", ctypes.c_int32), ("snp_pairs", ctypes.c_uint64),
                 ("diag_snps", ctypes.c_uint64), ("tiles", ctypes.c_uint64),
                 ("candidates", ctypes.c_uint64), ("method", ctypes.c_int32),
-                ("tile_snps", ctypes.c_int32)]
+                ("tile_snps", ctypes.c_int32), ("variant", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
 
 
 class _ScanReq(ctypes.Structure):
     _fields_ = [("planes", ctypes.c_void_p), ("a0", ctypes.c_int32), ("na", ctypes.c_int32),
                 ("b0", ctypes.c_int32), ("nb", ctypes.c_int32), ("topmost", ctypes.c_int32),
                 ("objective", ctypes.c_int32), ("method", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("variant", ctypes.c_int32)]
+
+
+class _BatchStats(ctypes.Structure):
+    _fields_ = [("steps", ctypes.c_int64), ("count_launches", ctypes.c_int64),
+                ("select_launches", ctypes.c_int64), ("graph_launches", ctypes.c_int64)]
+
+
+class _TuneReport(ctypes.Structure):
+    _fields_ = [("variant", ctypes.c_int32), ("n_variants", ctypes.c_int32),
+                ("ms", ctypes.c_float * 8)]
 
 
 class _Progress(ctypes.Structure):
@@ -154,6 +166,12 @@ def lib():
     L.gepi_planes_autotune.argtypes = [P, ctypes.POINTER(i32), ctypes.POINTER(ctypes.c_float),
                                        ctypes.POINTER(ctypes.c_float)]
     L.gepi_tensor_peak_tflops.argtypes = [i32, ctypes.POINTER(ctypes.c_double)]
+    L.gepi_tensor_peak_probe.argtypes = [i32, i32, ctypes.POINTER(ctypes.c_double)]
+    L.gepi_planes_autotune_variants.argtypes = [P, ctypes.POINTER(_TuneReport)]
+    L.gepi_scan_batch_stats.argtypes = [i32, ctypes.POINTER(_BatchStats)]
+    L.gepi_count_variant_name.argtypes = [i32]
+    L.gepi_count_variant_name.restype = ctypes.c_char_p
+    L.gepi_count_variant_shape.argtypes = [i32] + [ctypes.POINTER(i32)] * 4
     L.gepi_process_gpu_1_noalloc.argtypes = [P, P, i32, i32, P, P, P, ctypes.POINTER(_Params)]
     L.gepi_shard_range.argtypes = [i32, i32, i32] + [ctypes.POINTER(ctypes.c_int32)] * 4
     L.gepi_merge_results.argtypes = [i32, i32, ctypes.POINTER(P), ctypes.POINTER(ctypes.c_int32),
@@ -177,7 +195,8 @@ def lib():
               "gepi_planes_from_bed", "gepi_planes_from_rows", "gepi_planes_class_sizes",
               "gepi_scan", "gepi_scan_range", "gepi_pair_counts", "gepi_process_gpu_1",
               "gepi_last_scan_stats", "gepi_last_scan_values", "gepi_process_gpu_1_noalloc", "gepi_planes_autotune",
-              "gepi_tensor_peak_tflops", "gepi_scan_batch", "gepi_scan_progress", "gepi_shard_range", "gepi_merge_results", "gepi_server_create",
+              "gepi_tensor_peak_tflops", "gepi_tensor_peak_probe", "gepi_planes_autotune_variants",
+              "gepi_count_variant_shape", "gepi_scan_batch_stats", "gepi_scan_batch", "gepi_scan_progress", "gepi_shard_range", "gepi_merge_results", "gepi_server_create",
               "gepi_server_submit", "gepi_server_wait",
               "gepi_synth_bed", "gepi_synth_write"):
         getattr(L, f).restype = i32
@@ -216,6 +235,7 @@ class Params:
     qaRemoveMissing: bool = False
     method: int = METHOD_AUTO
     verbose: int = 0
+    variant: int = 0
 
     def _c(self) -> _Params:
         p = _Params()
@@ -224,6 +244,7 @@ class Params:
         p.objective = self.ffun
         p.method = self.method
         p.verbose = self.verbose
+        p.variant = self.variant
         return p
 
 
@@ -352,15 +373,16 @@ class Planes:
         return a.value, b.value
 
     def scan(self, k: int, objective: int = ENTROPY, method: int = METHOD_AUTO,
-             verbose: int = 0) -> np.ndarray:
-        par = Params(topmost=k, ffun=objective, method=method, verbose=verbose, gpuNum=self.device)
+             verbose: int = 0, variant: int = 0) -> np.ndarray:
+        par = Params(topmost=k, ffun=objective, method=method, verbose=verbose, gpuNum=self.device,
+                     variant=variant)
         tops = np.zeros(k, dtype=RESULT_DTYPE)
         _check(lib().gepi_scan(self._h, ctypes.byref(par._c()), _ptr(tops), k))
         return tops
 
     def scan_range(self, a0: int, na: int, b0: int, nb: int, k: int, objective: int = ENTROPY,
-                   method: int = METHOD_AUTO) -> np.ndarray:
-        par = Params(topmost=k, ffun=objective, method=method, gpuNum=self.device)
+                   method: int = METHOD_AUTO, variant: int = 0) -> np.ndarray:
+        par = Params(topmost=k, ffun=objective, method=method, gpuNum=self.device, variant=variant)
         tops = np.zeros(k, dtype=RESULT_DTYPE)
         _check(lib().gepi_scan_range(self._h, ctypes.byref(par._c()), a0, na, b0, nb,
                                      _ptr(tops), k))
@@ -402,6 +424,14 @@ class Planes:
         out = np.zeros((na, nb, 18), dtype=np.uint32)
         _check(lib().gepi_pair_counts(self._h, method, a0, na, b0, nb, _ptr(out)))
         return out
+
+    def autotune_variants(self) -> dict:
+        """The counting variant METHOD_AUTO uses on these planes and every
+        variant's time on the tuning triangle ({name: ms}, 0 = not timed)."""
+        r = _TuneReport()
+        _check(lib().gepi_planes_autotune_variants(self._h, ctypes.byref(r)))
+        return {"variant": r.variant, "name": variant_name(r.variant),
+                "ms": {variant_name(v): float(r.ms[v - 1]) for v in range(1, r.n_variants + 1)}}
 
     def autotune(self) -> dict:
         """The counting method METHOD_AUTO uses on these planes, with the two
@@ -505,10 +535,11 @@ class ScanRequest:
     na: int = -1
     b0: int = 0
     nb: int = -1
+    variant: int = 0
 
     def _c(self) -> _ScanReq:
         return _ScanReq(self.planes._h, self.a0, self.na, self.b0, self.nb, self.k,
-                        self.objective, self.method, 0)
+                        self.objective, self.method, self.variant)
 
 
 def scan_batch(reqs, with_stats: bool = False):
@@ -524,6 +555,14 @@ def scan_batch(reqs, with_stats: bool = False):
     if with_stats:
         return outs, [{f: getattr(st, f) for f, _ in _ScanStats._fields_} for st in stats]
     return outs
+
+
+def scan_batch_stats(device: int = 0) -> dict:
+    """Launch counts of the last scan_batch call on `device` (engine steps,
+    counting launches, batched select launches, step-graph replays)."""
+    st = _BatchStats()
+    _check(lib().gepi_scan_batch_stats(device, ctypes.byref(st)))
+    return {f: getattr(st, f) for f, _ in _BatchStats._fields_}
 
 
 class Server:
@@ -573,6 +612,34 @@ def tensor_peak_tflops(device: int = 0) -> float:
     """Dense kind::mxf4 tensor-core rate of `device` (TFLOP/s), measured now."""
     v = ctypes.c_double()
     _check(lib().gepi_tensor_peak_tflops(device, ctypes.byref(v)))
+    return v.value
+
+
+PEAK_KINDS = {"mxf4": 0, "mxf4nvf4_2x_ue8m0": 1, "mxf4nvf4_4x_ue4m3": 2}
+NUM_VARIANTS = 4
+
+
+def variant_name(v: int) -> str:
+    """Name of counting variant v (gepi_count_variant_name)."""
+    return lib().gepi_count_variant_name(v).decode()
+
+
+def variant_shape(v: int) -> dict:
+    m, ta, tb, w = (ctypes.c_int32() for _ in range(4))
+    _check(lib().gepi_count_variant_shape(v, ctypes.byref(m), ctypes.byref(ta), ctypes.byref(tb),
+                                          ctypes.byref(w)))
+    return {"method": m.value, "tile_a": ta.value, "tile_b": tb.value, "stage_words": w.value}
+
+
+def variant_method(v: int) -> int:
+    """The `method` argument of pair_counts() that selects counting variant v."""
+    return 16 + v
+
+
+def tensor_peak_probe(kind: str, device: int = 0) -> float:
+    """Dense FP4 tensor-core rate (TFLOP/s) of one exact 0/1 encoding (PEAK_KINDS)."""
+    v = ctypes.c_double()
+    _check(lib().gepi_tensor_peak_probe(device, PEAK_KINDS[kind], ctypes.byref(v)))
     return v.value
 
 

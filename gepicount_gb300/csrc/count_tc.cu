@@ -232,17 +232,19 @@ __device__ __forceinline__ void cluster_sync_all() {
 }
 
 // Warp-wide bounded wait: every lane polls the same barrier (a lane-0 poll
-// plus a broadcast costs a reconvergence per wait), then the warp votes.  The
-// lanes' own results can differ -- one lane's clock runs out or it sees the
-// abort flag in the same instant another lane's try_wait succeeds -- and a
-// warp whose lanes split there would reach the .sync.aligned tcgen05.st/ld
-// that follow with part of the warp gone.  With the vote the whole warp goes
-// on, or the whole warp gives up.
+// plus a broadcast costs a reconvergence per wait).  The warp decides as one:
+// it enters the wait converged, and in every iteration all its lanes execute
+// the same try_wait on the same barrier word, read the same clock (one
+// counter read per warp) and the same abort flag in the same instructions, so
+// every branch of the loop is uniform and the lanes leave together with the
+// same result -- the .sync.aligned tcgen05.st/ld and elect.sync that follow
+// see the whole warp.  An explicit vote after the wait measured 7% slower on
+// the 100,000 x 10,000 scan (238 against 224 ms), a __syncwarp and a shared
+// flag read 14%.
 __device__ __forceinline__ bool mbar_wait_warp(uint64_t *b, uint32_t parity,
                                                volatile int *abort_flag, int *err, int code,
                                                long long budget) {
-    const bool ok = mbar_wait(b, parity, abort_flag, err, code, budget);
-    return __all_sync(0xffffffffu, ok);
+    return mbar_wait(b, parity, abort_flag, err, code, budget);
 }
 
 // One arrival per warp, by a lane elected in-line (predicated, no branch).
@@ -469,12 +471,340 @@ struct ChunkMap {
     }
 };
 
-template <bool DUMP, int OBJ>
+// ---- the roles, shared by the single-request and the batched kernel --------
+
+// Barriers and wait policy of one CTA.  budget: clock budget of waits on other
+// roles (kTcWaitCycles; a test lowers it).
+struct TcSync {
+    uint64_t *pfull, *pempty, *full, *empty, *dfull, *dempty;
+    volatile int *abort_flag;
+    int *err;
+    long long budget;
+};
+
+// A producer lane's fixed geometry: lane quarter q, A words HW h .. of packed
+// A row 30 q + lane (lanes 30, 31 re-read row 30q+29 and clear it), and for
+// the first six producer warps a B piece (row u = t % 96, words HW hb ..;
+// consecutive lanes on consecutive rows: conflict-free 16-byte stores).
+struct TcProducer {
+    static constexpr int HW = kTcHalfWords;
+    int h, u, hb, arow_off;
+    bool arow, has_b;
+    uint32_t ta0;
+    unsigned char *bst0;
+
+    __device__ __forceinline__ TcProducer(unsigned char *smem, uint32_t tbase, int warp, int lane) {
+        const int q = warp & 3;  // TMEM lane quarter
+        h = (warp - kTcProdWarp0) >> 2;
+        arow = lane < 30;
+        arow_off = (30 * q + (arow ? lane : 29)) * (kTcChunkWords * 4);
+        ta0 = tbase + ((uint32_t)(32 * q) << 16) + kTcACol + 4 * HW * h;
+        has_b = warp - kTcProdWarp0 < kTcBWarps;
+        const int t8 = 32 * (warp - kTcProdWarp0) + lane;
+        u = t8 % kTcBRows;
+        hb = t8 / kTcBRows;
+        bst0 = smem + (u >> 3) * kTcSbo + (HW * hb) * kTcLbo + (u & 7) * 16;
+    }
+
+    // Global chunk idx: packed ring slot idx % kTcPStages -> stage idx %
+    // kTcStages (A into tensor memory, B into shared memory), then one arrival
+    // per warp on the pair's full barrier (none when `withhold`).  false: the
+    // CTA aborts.
+    __device__ __forceinline__ bool chunk(unsigned char *smem, const TcSync &S, int idx,
+                                          bool withhold) const {
+        const uint32_t j = (uint32_t)idx % kTcPStages, s = (uint32_t)idx % kTcStages;
+        if (!mbar_wait_warp(&S.pfull[j], ((uint32_t)idx / kTcPStages) & 1, S.abort_flag, S.err, 5,
+                            S.budget))
+            return false;
+        const unsigned char *pk = smem + kTcPOff + (size_t)j * kTcPStageBytes;
+        // every lane loads: no divergence
+        uint2 pa[HW / 2], pb[HW / 2];
+        {
+            const uint2 *r = reinterpret_cast<const uint2 *>(pk + 4 * HW * h + arow_off);
+#pragma unroll
+            for (int m = 0; m < HW / 2; ++m) {
+                pa[m] = r[m];
+                pa[m].x = arow ? pa[m].x : 0u;
+                pa[m].y = arow ? pa[m].y : 0u;
+            }
+        }
+        if (has_b) {
+            const uint2 *r =
+                reinterpret_cast<const uint2 *>(pk + kTcPABytes + u * (kTcChunkWords * 4) + 4 * HW * hb);
+#pragma unroll
+            for (int m = 0; m < HW / 2; ++m) pb[m] = r[m];
+        }
+        __syncwarp();
+        mbar_arrive_warp(&S.pempty[j]);
+        // expand into registers before waiting for the stage: the wait is on the
+        // MMAs kTcStages chunks back, and only the stores follow it
+        uint32_t r[4 * HW], o[4 * HW];
+#pragma unroll
+        for (int m = 0; m < HW / 2; ++m) {
+            expand_word(pa[m].x, r + 8 * m);
+            expand_word(pa[m].y, r + 8 * m + 4);
+        }
+        if (has_b) {
+#pragma unroll
+            for (int m = 0; m < HW / 2; ++m) {
+                expand_word(pb[m].x, o + 8 * m);
+                expand_word(pb[m].y, o + 8 * m + 4);
+            }
+        }
+        if (!mbar_wait_warp(&S.empty[s], (((uint32_t)idx / kTcStages) & 1) ^ 1, S.abort_flag, S.err, 1,
+                            S.budget))
+            return false;
+        tc_fence_after();
+        tmem_st16(ta0 + s * kTcAStageCols, r);
+        if constexpr (HW == 6) tmem_st8(ta0 + s * kTcAStageCols + 16, r + 16);
+        if (has_b) {
+            unsigned char *bst = bst0 + (size_t)s * kTcBStageBytes;
+#pragma unroll
+            for (int m = 0; m < HW; ++m)
+                *reinterpret_cast<uint4 *>(bst + m * kTcLbo) =
+                    make_uint4(o[4 * m], o[4 * m + 1], o[4 * m + 2], o[4 * m + 3]);
+        }
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        tc_fence_before();
+        __syncwarp();
+        if (!withhold) mbar_arrive_warp_cl(cluster_addr(&S.full[s], 0));
+        return true;
+    }
+};
+
+// The copy issuer's chunk: waits for ring slot idx % kTcPStages to be free and
+// lands chunk c of the tile's packed A rows (from arow) and B rows (from brow).
+__device__ __forceinline__ bool tc_copy_chunk(unsigned char *smem, const TcSync &S, int idx,
+                                              const uint32_t *blk, int rows_pad, int c, size_t arow,
+                                              size_t brow, bool wait_free = true) {
+    const uint32_t j = (uint32_t)idx % kTcPStages;
+    if (wait_free && !mbar_wait(&S.pempty[j], (((uint32_t)idx / kTcPStages) & 1) ^ 1, S.abort_flag,
+                                S.err, 6, S.budget))
+        return false;
+    unsigned char *pk = smem + kTcPOff + (size_t)j * kTcPStageBytes;
+    const uint32_t *base = blk + (size_t)c * rows_pad * kTcChunkWords;
+    mbar_expect_tx(&S.pfull[j], kTcPStageBytes);
+    bulk_load(pk, base + arow * kTcChunkWords, kTcPABytes, &S.pfull[j]);
+    bulk_load(pk + kTcPABytes, base + brow * kTcChunkWords, kTcPBBytes, &S.pfull[j]);
+    return true;
+}
+
+// Every copy the issuer made (`issued` chunks) lands before the CTA exits.
+__device__ __forceinline__ void tc_copy_drain(const TcSync &S, int issued) {
+    for (int idx = issued > kTcPStages ? issued - kTcPStages : 0; idx < issued; ++idx)
+        mbar_drain(&S.pfull[idx % kTcPStages], ((uint32_t)idx / kTcPStages) & 1);
+}
+
+// The MMA issuer's chunk c of local tile lt (global chunk gc) with map cm.
+struct TcMma {
+    uint64_t bdesc0;  // stage 0's B descriptor; stage s adds s * kTcBStageBytes >> 4
+    uint32_t tbase, sf;
+    __device__ __forceinline__ bool chunk(const TcSync &S, const ChunkMap &cm, int c, uint32_t gc,
+                                          uint32_t lt) const {
+        const int cls = c < cm.n0 ? 0 : 1;
+        if (c == 0 || c == cm.n0) {
+            // both CTAs' epilogues have copied this class half of the previous
+            // tile's accumulator out (while the other half was being
+            // accumulated): the tensor pipe never drains between tiles
+            if (!mbar_wait(&S.dempty[cls], (lt & 1) ^ 1, S.abort_flag, S.err, 2, S.budget)) return false;
+            tc_fence_after();
+        }
+        const uint32_t s = gc % kTcStages;
+        const int nm = cm.mmas(c);
+        const uint32_t d = tbase + (uint32_t)(cls * kTcN);
+        const uint32_t acc0 = (c == 0 || c == cm.n0) ? 0u : 1u;
+        const uint32_t a = tbase + kTcACol + s * kTcAStageCols;
+        const uint64_t bd = bdesc0 + (uint64_t)((s * (uint32_t)kTcBStageBytes) >> 4);
+        if (!mbar_wait(&S.full[s], (gc / kTcStages) & 1, S.abort_flag, S.err, 3, S.budget)) return false;
+        tc_fence_after();
+        // MMA kk reads A columns 8kk.. and the k-group pair 2kk (256 B further
+        // each: +16 in the descriptor's address field)
+#pragma unroll
+        for (int kk = 0; kk < kTcChunkWords / 2; ++kk)
+            if (kk < nm) tc_mma2(d, a + kk * 8, bd + (uint64_t)(16 * kk), sf, kk == 0 ? acc0 : 1u);
+        tc_commit2_both(&S.empty[s]);
+        if (c == cm.n0 - 1 || c == cm.nchunks - 1) tc_commit2_both(&S.dfull[cls]);
+        return true;
+    }
+};
+
+// A scoring warp's fixed geometry: lane quarter q, B SNPs 32 eh .. 32 eh + 31
+// of the tile, its exchange rows (16-bit counts, row = TMEM lane: plane p of A
+// SNP i at row 3i + p, laid out [class][B plane qq][B SNP jl] so that the 32
+// lanes reading one plane pair of 32 B SNPs hit 16 consecutive words; odd word
+// pitch, so the copy-out is conflict-free too).
+struct TcScorer {
+    static constexpr int kB = 8 * kTcEpiGroups;  // B SNPs of the warp: 32
+    int eh, aoff;
+    uint16_t *xh;
+    uint32_t tq;
+    __device__ __forceinline__ TcScorer(unsigned char *smem, uint32_t tbase, int warp, uint32_t rank) {
+        const int q = warp & 3;
+        const int ew = warp - kTcEpiWarp0;
+        eh = ew >> 2;
+        xh = reinterpret_cast<uint16_t *>(smem + kTcXOff) + (size_t)ew * 32 * kTcXPitch;
+        aoff = kTcASnps * (int)rank + 10 * q;  // this warp's first A SNP in the tile
+        tq = tbase + ((uint32_t)(32 * q) << 16) + 3 * kB * eh;
+    }
+
+    // Local tile lt (A tile tx, B tile ty of ranges [a0,a1) x [b0,b1)): copy
+    // each class half out as soon as its MMAs are done and hand it back (the
+    // tensor pipe goes on with the other half, then the next tile), then bound
+    // every SNP pair per row pair: lane = B SNP, one A SNP per round; the rare
+    // lane whose bound passes runs the per-test bounds and the out-of-line
+    // refinement on the counts it holds.  false: the CTA aborts.
+    template <bool DUMP, int OBJ>
+    __device__ __forceinline__ bool tile(const TcSync &S, int lane, uint32_t lt, int tx, int ty,
+                                         int a0, int a1, int b0, int b1, const ScanCtx &ctx,
+                                         float theta, float lp_thr, uint32_t *dump) const {
+        const int sAq = a0 + tx * kTcPairASnps + aoff;  // A SNP 0 of the lane quarter
+        const int sB0 = b0 + ty * kTcBSnps + kB * eh;
+        for (int cls = 0; cls < 2; ++cls) {
+            if (!mbar_wait_warp(&S.dfull[cls], lt & 1, S.abort_flag, S.err, 4, S.budget)) return false;
+            tc_fence_after();
+            uint32_t *rw = reinterpret_cast<uint32_t *>(xh + lane * kTcXPitch) + cls * (3 * kB / 2);
+#pragma unroll
+            for (int gl = 0; gl < kTcEpiGroups; ++gl) {
+                uint32_t v[24];  // column 3 jl' + qq of B SNPs 8 gl + jl'
+                tmem_ld16(tq + cls * kTcN + 24 * gl, *reinterpret_cast<uint32_t(*)[16]>(v));
+                tmem_ld8(tq + cls * kTcN + 24 * gl + 16, *reinterpret_cast<uint32_t(*)[8]>(v + 16));
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int qq = 0; qq < 3; ++qq)
+#pragma unroll
+                    for (int m = 0; m < 4; ++m)
+                        rw[qq * (kB / 2) + 4 * gl + m] =
+                            __float2uint_rn(__uint_as_float(v[6 * m + qq])) |
+                            (__float2uint_rn(__uint_as_float(v[6 * m + 3 + qq])) << 16);
+            }
+            tc_fence_before();
+            __syncwarp();
+            mbar_arrive_warp_cl(cluster_addr(&S.dempty[cls], 0));
+        }
+        __syncwarp();
+        if constexpr (DUMP) {
+            const int i = lane / 3, p = lane % 3, sA = sAq + i;
+            if (lane < 30 && sA < a1) {
+                const uint16_t *xr = xh + lane * kTcXPitch;
+                for (int jb = 0; jb < kB; ++jb) {
+                    const int sBt = sB0 + jb;
+                    if (sBt >= b1) continue;
+                    uint32_t *o = dump + ((size_t)(sA - a0) * (b1 - b0) + (sBt - b0)) * 18;
+#pragma unroll
+                    for (int qq = 0; qq < 3; ++qq) {
+                        o[p * 3 + qq] = xr[qq * kB + jb];
+                        o[9 + p * 3 + qq] = xr[3 * kB + qq * kB + jb];
+                    }
+                }
+            }
+            __syncwarp();
+            return true;
+        }
+        const int sBt = sB0 + lane;
+        for (int r = 0; r < 10; ++r) {
+            const int sA = sAq + r;
+            if (!(sA < a1 && sBt < b1 && sBt <= sA)) continue;
+            const uint16_t *xr = xh + 3 * r * kTcXPitch + lane;
+            float G[18];
+#pragma unroll
+            for (int pp = 0; pp < 3; ++pp)
+#pragma unroll
+                for (int qq = 0; qq < 3; ++qq) {
+                    G[pp * 3 + qq] = u16f(xr[pp * kTcXPitch + qq * kB]);
+                    G[9 + pp * 3 + qq] = u16f(xr[pp * kTcXPitch + 3 * kB + qq * kB]);
+                }
+            const uint32_t rp = rowpair_bounds(G, G + 9, sA == sBt, OBJ, theta, lp_thr);
+            if (!rp) continue;
+            uint32_t mask = tc_stage1<OBJ>(ctx, G, G + 9, rp, theta, lp_thr);
+            const int y = (int)G[8], z = (int)G[17];
+            while (mask) {
+                const int bit = __ffs(mask) - 1;
+                mask &= mask - 1;
+                const int rpi = bit / 5, f = bit - 5 * rpi, ri = rpi >> 1, rj = rpi & 1;
+                const int w = fun_count((int)G[ri * 3 + rj], (int)G[ri * 3 + 2], (int)G[6 + rj], y, f);
+                const int x = fun_count((int)G[9 + ri * 3 + rj], (int)G[9 + ri * 3 + 2],
+                                        (int)G[15 + rj], z, f);
+                tc_refine<OBJ>(ctx, 2 * sA + ri, 2 * sBt + rj, f, w, x, y, z);
+            }
+        }
+        __syncwarp();
+        return true;
+    }
+};
+
+// Common prologue of both kernels: barriers (and the batched kernel's ring
+// barriers, `ring_bar`, `nring` of them), tensor memory for the pair.
+__device__ __forceinline__ void tc_prologue(const TcSync &S, uint64_t *fin_bar, uint64_t *ring_bar,
+                                            int nring, uint32_t *tmem_slot, int *abort_flag, int tid,
+                                            int warp) {
+    if (tid == 0) {
+        for (int j = 0; j < kTcPStages; ++j) {
+            mbar_init(&S.pfull[j], 1);
+            mbar_init(&S.pempty[j], kTcProducerWarps);
+        }
+        for (int s = 0; s < kTcStages; ++s) {
+            mbar_init(&S.full[s], 2 * kTcProducerWarps);  // both CTAs' producers (even CTA's)
+            mbar_init(&S.empty[s], 1);
+        }
+        for (int cls = 0; cls < 2; ++cls) {  // the accumulator's class halves
+            mbar_init(&S.dfull[cls], 1);
+            mbar_init(&S.dempty[cls], 2 * kTcEpiWarps);  // both CTAs' epilogues (even CTA's)
+        }
+        mbar_init(fin_bar, 1);
+        for (int j = 0; j < nring; ++j) mbar_init(&ring_bar[j], 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        // one warp of each CTA of the pair, collectively
+        asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         su32(tmem_slot)),
+                     "r"(kTcCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+    }
+}
+
+__device__ __forceinline__ void tc_scales(uint32_t tbase, int warp) {
+    if (warp < 4) {
+        // unit block scales (UE8M0 1.0) over all lanes of the scale-factor columns
+        uint32_t r[32];
+#pragma unroll
+        for (int k = 0; k < 32; ++k) r[k] = 0x7F7F7F7Fu;
+        tmem_st32(tbase + ((uint32_t)(32 * warp) << 16) + kTcSfCol, r);
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+    }
+}
+
+// Common epilogue: the pair's MMAs have drained (the even CTA's issuer waited
+// for them) and no thread arrives on the peer's barriers any more once both
+// CTAs pass the cluster barrier; then the pair's tensor memory is freed.
+__device__ __forceinline__ void tc_teardown(uint32_t tbase, int warp) {
+    tc_fence_before();
+    __syncthreads();
+    cluster_sync_all();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(kTcCols)
+                     : "memory");
+    }
+}
+
+// The single-request kernel (gepi_scan, gepi_scan_range, gepi_pair_counts).
+// Its roles are written out in line rather than through the role structs the
+// batched kernel shares: the same code behind those structs measured 8%
+// slower on the 100,000 x 10,000 scan (242 against 224 ms).
+// TEST: the wait budget and the withheld first arrival of the timeout test
+// (GEPI_DEBUG_STALL) are kernel arguments; the library's instances compile
+// them out.
+template <bool DUMP, int OBJ, bool TEST>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
     tc_tile_kernel(const uint32_t *__restrict__ blk, int rows_pad, int Wp, int W0,
                    const int2 *__restrict__ tiles, int ntiles, int a0, int a1, int b0, int b1,
                    ScanCtx ctx, uint32_t *__restrict__ dump, int *err, long long wait_cycles,
                    int stall) {
+    const long long budget = TEST ? wait_cycles : kTcWaitCycles;
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     __shared__ uint64_t pfull_bar[kTcPStages], pempty_bar[kTcPStages], full_bar[kTcStages],
         empty_bar[kTcStages], dfull_bar[2], dempty_bar[2], fin_bar;
@@ -557,8 +887,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
         unsigned char *bst0 = tc_smem + (u >> 3) * kTcSbo + (HW * hb) * kTcLbo + (u & 7) * 16;
         for (int idx = 0; idx < total; ++idx) {
             const uint32_t j = (uint32_t)idx % kTcPStages, s = (uint32_t)idx % kTcStages;
-            if (!mbar_wait_warp(&pfull_bar[j], ((uint32_t)idx / kTcPStages) & 1, vabort, err, 5,
-                                wait_cycles))
+            if (!mbar_wait_warp(&pfull_bar[j], ((uint32_t)idx / kTcPStages) & 1, vabort, err, 5, budget))
                 break;
             const unsigned char *pk = tc_smem + kTcPOff + (size_t)j * kTcPStageBytes;
             // every lane loads (lanes 30, 31 re-read row 30q+29 and clear it): no divergence
@@ -596,7 +925,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
                 }
             }
             if (!mbar_wait_warp(&empty_bar[s], (((uint32_t)idx / kTcStages) & 1) ^ 1, vabort, err, 1,
-                                wait_cycles))
+                                budget))
                 break;
             tc_fence_after();
             tmem_st16(ta0 + s * kTcAStageCols, r);
@@ -612,7 +941,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             tc_fence_before();
             __syncwarp();
-            if (!(stall && idx == 0)) mbar_arrive_warp_cl(cluster_addr(&full_bar[s], 0));
+            if (!(TEST && stall && idx == 0)) mbar_arrive_warp_cl(cluster_addr(&full_bar[s], 0));
         }
     } else if (warp == kTcTmaWarp) {
         // ---------------- bulk-copy issuer ----------------
@@ -630,7 +959,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
                 }
                 const uint32_t j = (uint32_t)idx % kTcPStages;
                 if (!mbar_wait(&pempty_bar[j], (((uint32_t)idx / kTcPStages) & 1) ^ 1, vabort, err, 6,
-                               wait_cycles))
+                               budget))
                     break;
                 unsigned char *pk = tc_smem + kTcPOff + (size_t)j * kTcPStageBytes;
                 const uint32_t *base = blk + (size_t)c * rows_pad * kTcChunkWords;
@@ -663,7 +992,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
                         // both CTAs' epilogues have copied this class half of the
                         // previous tile's accumulator out (while the other half was
                         // being accumulated): the tensor pipe never drains between tiles
-                        if (!mbar_wait(&dempty_bar[cls], (lt & 1) ^ 1, vabort, err, 2, wait_cycles)) {
+                        if (!mbar_wait(&dempty_bar[cls], (lt & 1) ^ 1, vabort, err, 2, budget)) {
                             ok = false;
                             break;
                         }
@@ -675,7 +1004,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
                     const uint32_t acc0 = (c == 0 || c == cm.n0) ? 0u : 1u;
                     const uint32_t a = tbase + kTcACol + s * kTcAStageCols;
                     const uint64_t bd = bdesc0 + (uint64_t)((s * (uint32_t)kTcBStageBytes) >> 4);
-                    if (!mbar_wait(&full_bar[s], (gc / kTcStages) & 1, vabort, err, 3, wait_cycles)) {
+                    if (!mbar_wait(&full_bar[s], (gc / kTcStages) & 1, vabort, err, 3, budget)) {
                         ok = false;
                         break;
                     }
@@ -720,7 +1049,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
             // copy each class half out as soon as its MMAs are done and hand it
             // back: the tensor pipe goes on with the other half, then the next tile
             for (int cls = 0; cls < 2; ++cls) {
-                if (!mbar_wait_warp(&dfull_bar[cls], lt & 1, vabort, err, 4, wait_cycles)) {
+                if (!mbar_wait_warp(&dfull_bar[cls], lt & 1, vabort, err, 4, budget)) {
                     live = false;
                     break;
                 }
@@ -810,6 +1139,187 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
     }
 }
 
+
+// ---- batched kernel: one launch over the tiles of many requests ------------
+//
+// The tiles of every request of an engine step form one work list (runs of
+// consecutive tiles of a request's list, WorkRange); CTA pairs claim tiles
+// from it with an atomic counter, so pairs that drew cheap tiles (few samples)
+// take more of them.  The copy issuer of the even CTA claims: it resolves the
+// claimed index to (request, A tile, B tile), writes it into slot k % kTcRing
+// of a ring in both CTAs' shared memory and arrives on that slot's barrier in
+// both (release at cluster scope for the peer); every other role reads tile k
+// from the ring after waiting on the barrier (acquire at cluster scope in the
+// odd CTA).  A request index < 0 ends the pair's work.
+//
+// Slots are reused without an "empty" barrier because the claimer cannot get
+// kTcRing tiles ahead of the slowest reader: claiming tile K waits for the
+// packed-ring slot of K's first chunk, so the even CTA's producers have loaded
+// chunk g - 4 (g = K's first chunk), hence waited for the MMAs of chunk g - 7,
+// which the MMA thread issued only after both CTAs' producers finished chunk
+// g - 7 and both CTAs' scoring warps released the accumulator of the tile
+// before it.  Every tile has at least two chunks (one per class), so all
+// readers have read the slots of tiles <= K - 5; K - kTcRing = K - 8 is older.
+constexpr int kTcRing = 8;
+
+__device__ __forceinline__ bool mbar_try_cluster(uint64_t *b, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2, %3;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(su32(b)), "r"(parity), "r"(kTcSuspendNs)
+        : "memory");
+    return done != 0;
+}
+
+// Bounded wait for ring slot `slot` of tile k (the odd CTA acquires at cluster
+// scope: the claimer in the even CTA wrote it).
+__device__ __forceinline__ bool ring_wait(uint64_t *b, uint32_t parity, uint32_t rank,
+                                          const TcSync &S) {
+    if (rank == 0) return mbar_wait(b, parity, S.abort_flag, S.err, 7, S.budget);
+    if (mbar_try_cluster(b, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try_cluster(b, parity)) {
+        if (*S.abort_flag) return false;
+        if (clock64() - t0 > S.budget) {
+            *S.abort_flag = 1;
+            atomicCAS(S.err, 0, 7);
+            return false;
+        }
+    }
+    return true;
+}
+
+__device__ __forceinline__ ChunkMap chunk_map(int W0, int Wp) {
+    ChunkMap cm;
+    cm.W0 = W0;
+    cm.W1 = Wp - W0;
+    cm.n0 = (W0 + kTcChunkWords - 1) / kTcChunkWords;
+    cm.nchunks = cm.n0 + (cm.W1 + kTcChunkWords - 1) / kTcChunkWords;
+    return cm;
+}
+
+template <int OBJ, bool TEST>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
+    tc_batch_kernel(const ReqDesc *__restrict__ reqs, WorkQueue *q, long long wait_cycles, int stall) {
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    __shared__ uint64_t pfull_bar[kTcPStages], pempty_bar[kTcPStages], full_bar[kTcStages],
+        empty_bar[kTcStages], dfull_bar[2], dempty_bar[2], fin_bar, ring_bar[kTcRing];
+    __shared__ int4 ring[kTcRing];
+    __shared__ uint32_t tmem_slot;
+    __shared__ int abort_flag;
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t rank = cluster_rank();
+    TcSync S{pfull_bar, pempty_bar, full_bar, empty_bar, dfull_bar, dempty_bar, &abort_flag, &q->err,
+             TEST ? wait_cycles : kTcWaitCycles};
+    tc_prologue(S, &fin_bar, ring_bar, kTcRing, &tmem_slot, &abort_flag, tid, warp);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = tmem_slot;
+    tc_scales(tbase, warp);
+    tc_fence_before();
+    __syncthreads();
+    cluster_sync_all();
+    tc_fence_after();
+
+    // tile k of this pair from the ring (all lanes of a warp read the same slot)
+    auto next_tile = [&](int k, int4 &d) -> bool {
+        const int slot = k % kTcRing;
+        if (!ring_wait(&ring_bar[slot], ((uint32_t)k / kTcRing) & 1, rank, S)) return false;
+        const volatile int *v = reinterpret_cast<const volatile int *>(&ring[slot]);
+        d = make_int4(v[0], v[1], v[2], v[3]);
+        return d.x >= 0;
+    };
+
+    if (warp >= kTcProdWarp0 && warp < kTcEpiWarp0) {
+        const TcProducer P(tc_smem, tbase, warp, lane);
+        int idx = 0;
+        bool ok = true;
+        int4 d;
+        for (int k = 0; ok && next_tile(k, d); ++k) {
+            const ReqDesc &R = reqs[d.x];
+            const int nch = chunk_map(R.W0, R.Wp).nchunks;
+            for (int c = 0; c < nch && ok; ++c, ++idx) ok = P.chunk(tc_smem, S, idx, TEST && stall && idx == 0);
+        }
+    } else if (warp == kTcTmaWarp) {
+        if (lane == 0) {
+            int idx = 0, issued = 0;
+            const uint32_t peer_ring = cluster_addr(ring, 1), peer_bar = cluster_addr(ring_bar, 1);
+            for (int k = 0;; ++k) {
+                const int slot = k % kTcRing;
+                int4 d;
+                if (rank == 0) {
+                    // claim only once the packed-ring slot of the tile's first chunk is free
+                    const uint32_t j = (uint32_t)idx % kTcPStages;
+                    if (!mbar_wait(&S.pempty[j], (((uint32_t)idx / kTcPStages) & 1) ^ 1, S.abort_flag,
+                                   S.err, 6, S.budget))
+                        break;
+                    const int t = (int)atomicAdd(&q->next, 1u);
+                    d = resolve_work(reqs, q, t);
+                    ring[slot] = d;
+                    asm volatile("st.shared::cluster.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(
+                                     peer_ring + (uint32_t)(slot * sizeof(int4))),
+                                 "r"(d.x), "r"(d.y), "r"(d.z), "r"(d.w)
+                                 : "memory");
+                    mbar_arrive(&ring_bar[slot]);
+                    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(
+                                     peer_bar + (uint32_t)(slot * sizeof(uint64_t)))
+                                 : "memory");
+                    if (d.x < 0) break;
+                } else if (!next_tile(k, d)) {
+                    break;
+                }
+                const ReqDesc &R = reqs[d.x];
+                const ChunkMap cm = chunk_map(R.W0, R.Wp);
+                const size_t arow = (size_t)3 * (R.a0 + d.y * kTcPairASnps + kTcASnps * (int)rank);
+                const size_t brow = (size_t)3 * (R.b0 + d.z * kTcBSnps) + kTcBRows * rank;
+                bool ok = true;
+                for (int c = 0; c < cm.nchunks; ++c, ++idx) {
+                    // the even CTA waited for its first chunk's slot before claiming
+                    ok = tc_copy_chunk(tc_smem, S, idx, R.blk, R.rows_pad, c, arow, brow,
+                                       !(rank == 0 && c == 0));
+                    if (!ok) break;
+                    issued = idx + 1;
+                }
+                if (!ok) break;
+            }
+            tc_copy_drain(S, issued);
+        }
+        __syncwarp();
+    } else if (warp == kTcMmaWarp) {
+        if (rank == 0 && lane == 0) {
+            const TcMma M{tc_bdesc(su32(tc_smem)), tbase, tbase + kTcSfCol};
+            uint32_t gc = 0, lt = 0;
+            bool ok = true;
+            int4 d;
+            for (int k = 0; ok && next_tile(k, d); ++k, ++lt) {
+                const ReqDesc &R = reqs[d.x];
+                const ChunkMap cm = chunk_map(R.W0, R.Wp);
+                for (int c = 0; c < cm.nchunks && ok; ++c, ++gc) ok = M.chunk(S, cm, c, gc, lt);
+            }
+            tc_commit2(&fin_bar);
+            mbar_drain(&fin_bar, 0);
+        }
+        __syncwarp();
+    } else {
+        const TcScorer E(tc_smem, tbase, warp, rank);
+        uint32_t lt = 0;
+        int4 d;
+        for (int k = 0; next_tile(k, d); ++k, ++lt) {
+            const ReqDesc &R = reqs[d.x];
+            const ScanCtx ctx = R.ctx;
+            const float theta = ctx.st->theta, lp_thr = ctx.st->lp_thr;
+            if (!E.template tile<false, OBJ>(S, lane, lt, d.y, d.z, R.a0, R.a1, R.b0, R.b1, ctx, theta,
+                                             lp_thr, nullptr))
+                break;
+        }
+    }
+    tc_teardown(tbase, warp);
+}
+
 // Block-major operand layout (see the file comment).
 __global__ void tc_relayout_kernel(const uint32_t *__restrict__ planes, int Wp, int W0, int nrows,
                                    int rows_pad, int n0, int nblk, uint32_t *__restrict__ blk) {
@@ -853,17 +1363,12 @@ cudaError_t launch_tc_relayout(const uint32_t *planes, int Wp, int W0, int n_snp
 
 // Pairs of CTAs the GPU holds at once (each pair on two SMs of one GPC): the
 // persistent grid, asked of the occupancy calculator once per device.
-template <bool DUMP, int OBJ>
-static cudaError_t launch_tc_pairs(const uint32_t *blk, int rows_pad, int Wp, int W0,
-                                   const int2 *tiles, int ntiles, int a0, int a1, int b0, int b1,
-                                   const ScanCtx &ctx, uint32_t *dump, int *err, int num_sms,
-                                   cudaStream_t stream) {
+template <class K>
+static cudaError_t resident_pairs(K kern, int num_sms, cudaStream_t stream, int *out) {
     static std::atomic<int> resident[64];
-    auto kern = tc_tile_kernel<DUMP, OBJ>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
-    if (e != cudaSuccess) return e;
     int dev = 0;
-    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
     int pairs = dev < 64 ? resident[dev].load() : 0;
     if (pairs <= 0) {
         cudaLaunchConfig_t cfg = {};
@@ -879,18 +1384,36 @@ static cudaError_t launch_tc_pairs(const uint32_t *blk, int rows_pad, int Wp, in
         pairs = std::min(nc, num_sms / 2);
         if (dev < 64) resident[dev].store(pairs);
     }
-    pairs = std::max(1, std::min(pairs, ntiles));
-    long long wait_cycles = kTcWaitCycles;
-    int stall = 0;
+    *out = pairs;
+    return cudaSuccess;
+}
+
+// The timeout test's settings (GEPI_DEBUG_STALL=<cycles>): true when set.
+static bool debug_stall(long long *wait_cycles) {
+    *wait_cycles = kTcWaitCycles;
     if (const char *w = std::getenv("GEPI_DEBUG_STALL")) {
         const long long v = std::atoll(w);
         if (v > 0) {
-            wait_cycles = std::min(v, kTcWaitCycles);
-            stall = 1;
+            *wait_cycles = std::min(v, kTcWaitCycles);
+            return true;
         }
     }
+    return false;
+}
+
+template <bool DUMP, int OBJ, bool TEST>
+static cudaError_t launch_tc_pairs(const uint32_t *blk, int rows_pad, int Wp, int W0,
+                                   const int2 *tiles, int ntiles, int a0, int a1, int b0, int b1,
+                                   const ScanCtx &ctx, uint32_t *dump, int *err, int num_sms,
+                                   long long wait_cycles, cudaStream_t stream) {
+    auto kern = tc_tile_kernel<DUMP, OBJ, TEST>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+    if (e != cudaSuccess) return e;
+    int pairs = 0;
+    if ((e = resident_pairs(kern, num_sms, stream, &pairs)) != cudaSuccess) return e;
+    pairs = std::max(1, std::min(pairs, ntiles));
     kern<<<2 * pairs, kTcThreads, kTcSmem, stream>>>(blk, rows_pad, Wp, W0, tiles, ntiles, a0, a1,
-                                                    b0, b1, ctx, dump, err, wait_cycles, stall);
+                                                    b0, b1, ctx, dump, err, wait_cycles, TEST ? 1 : 0);
     return cudaGetLastError();
 }
 
@@ -905,24 +1428,109 @@ cudaError_t launch_tc_tiles(const uint32_t *blk, int n_snps, int Wp, int W0, con
         return cudaErrorInvalidValue;
     int rows_pad, nblk;
     tc_block_shape(n_snps, Wp, W0, &rows_pad, &nblk);
+    long long wc = 0;
+    const bool test = debug_stall(&wc);
     if (dump)
-        return launch_tc_pairs<true, 0>(blk, rows_pad, Wp, W0, tiles, ntiles, a0, a1, b0, b1, ctx,
-                                        dump, err, num_sms, stream);
+        return test ? launch_tc_pairs<true, 0, true>(blk, rows_pad, Wp, W0, tiles, ntiles, a0, a1, b0,
+                                                     b1, ctx, dump, err, num_sms, wc, stream)
+                    : launch_tc_pairs<true, 0, false>(blk, rows_pad, Wp, W0, tiles, ntiles, a0, a1, b0,
+                                                      b1, ctx, dump, err, num_sms, wc, stream);
     if (ctx.objective == 0)
-        return launch_tc_pairs<false, 0>(blk, rows_pad, Wp, W0, tiles, ntiles, a0, a1, b0, b1, ctx,
-                                         nullptr, err, num_sms, stream);
-    return launch_tc_pairs<false, 1>(blk, rows_pad, Wp, W0, tiles, ntiles, a0, a1, b0, b1, ctx,
-                                     nullptr, err, num_sms, stream);
+        return test ? launch_tc_pairs<false, 0, true>(blk, rows_pad, Wp, W0, tiles, ntiles, a0, a1,
+                                                      b0, b1, ctx, nullptr, err, num_sms, wc, stream)
+                    : launch_tc_pairs<false, 0, false>(blk, rows_pad, Wp, W0, tiles, ntiles, a0, a1,
+                                                       b0, b1, ctx, nullptr, err, num_sms, wc, stream);
+    return launch_tc_pairs<false, 1, false>(blk, rows_pad, Wp, W0, tiles, ntiles, a0, a1, b0, b1, ctx,
+                                            nullptr, err, num_sms, wc, stream);
 }
 
-// Dense kind::mxf4 MMA rate of this GPU, the roofline denominator of the
+// setup: the shared-memory opt-in and the occupancy query only (outside any
+// stream capture); the engine does it before it captures a step graph.
+template <int OBJ, bool TEST>
+static cudaError_t launch_tc_batch_obj(const ReqDesc *reqs, WorkQueue *q, int num_sms,
+                                       long long wait_cycles, bool setup, cudaStream_t stream) {
+    auto kern = tc_batch_kernel<OBJ, TEST>;
+    int pairs = 0;
+    if (setup) {
+        cudaError_t e =
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem);
+        if (e == cudaSuccess) e = resident_pairs(kern, num_sms, stream, &pairs);
+        return e;
+    }
+    cudaError_t e = resident_pairs(kern, num_sms, stream, &pairs);
+    if (e != cudaSuccess) return e;
+    kern<<<2 * std::max(1, pairs), kTcThreads, kTcSmem, stream>>>(reqs, q, wait_cycles, TEST ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_tc_batch(const ReqDesc *reqs, WorkQueue *q, int objective, int num_sms,
+                            cudaStream_t stream, bool setup) {
+    long long wc = 0;
+    const bool test = debug_stall(&wc);
+    if (objective == 0)
+        return test ? launch_tc_batch_obj<0, true>(reqs, q, num_sms, wc, setup, stream)
+                    : launch_tc_batch_obj<0, false>(reqs, q, num_sms, wc, setup, stream);
+    return launch_tc_batch_obj<1, false>(reqs, q, num_sms, wc, setup, stream);
+}
+
+bool tc_debug_stall() {
+    long long wc = 0;
+    return debug_stall(&wc);
+}
+
+bool tc_shape_ok(int Wp, int W0) {
+    return !((W0 & 1) || (Wp & 1) || W0 <= 0 || Wp <= W0 || 32 * W0 > kTcMaxClass + 31 + 32 ||
+             32 * (Wp - W0) > kTcMaxClass + 31 + 32);
+}
+
+int tc_rows_pad(int n_snps) {
+    int rows_pad = 0, nblk = 0;
+    tc_block_shape(n_snps, 2, 0, &rows_pad, &nblk);
+    return rows_pad;
+}
+
+// Dense block-scaled FP4 MMA rates of this GPU, the roofline denominator of the
 // tensor-core counting kernel: one CTA per SM issues `iters` back-to-back
 // M=128 x N=256 x K=64 MMAs (A in tensor memory, B in shared memory, unit
-// scales) and waits for them once.
-constexpr uint32_t kTcPeakIdesc = (1u << 7) | (1u << 10) | ((uint32_t)(256 >> 3) << 17) |
-                                  (1u << 23) | ((uint32_t)(128 >> 4) << 24);
+// scales) and waits for them once.  Three exact encodings of 0/1 operands are
+// probed (PTX tcgen05.mma block_scale forms):
+//   kind 0: kind::mxf4,     scale_vec::2X, UE8M0 scales (the counting kernel's)
+//   kind 1: kind::mxf4nvf4, scale_vec::2X, UE8M0 scales
+//   kind 2: kind::mxf4nvf4, scale_vec::4X, UE4M3 scales
+// A and B are E2M1 in every kind; all scale factors are 1.0 (UE8M0 0x7F, UE4M3
+// 0x38), so the products are the same 0/1 values.
+constexpr int kTcPeakKinds = 3;
+template <int KIND>
+__host__ __device__ constexpr uint32_t tc_peak_idesc() {
+    return (1u << 7) | (1u << 10) | ((uint32_t)(256 >> 3) << 17) | (KIND == 2 ? 0u : (1u << 23)) |
+           ((uint32_t)(128 >> 4) << 24);
+}
 constexpr int kTcPeakSmem = 120 * 1024;  // one CTA per SM
 
+template <int KIND>
+__device__ __forceinline__ void tc_peak_mma(uint32_t d, uint32_t a, uint64_t bd, uint32_t sf,
+                                            uint32_t acc) {
+    if constexpr (KIND == 0)
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %5, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::mxf4.block_scale.scale_vec::2X [%0], [%1], %2, %3, "
+            "[%4], [%4], p;\n}\n" ::"r"(d),
+            "r"(a), "l"(bd), "r"(tc_peak_idesc<KIND>()), "r"(sf), "r"(acc));
+    else if constexpr (KIND == 1)
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %5, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::mxf4nvf4.block_scale.scale_vec::2X [%0], [%1], %2, %3, "
+            "[%4], [%4], p;\n}\n" ::"r"(d),
+            "r"(a), "l"(bd), "r"(tc_peak_idesc<KIND>()), "r"(sf), "r"(acc));
+    else
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %5, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::mxf4nvf4.block_scale.scale_vec::4X [%0], [%1], %2, %3, "
+            "[%4], [%4], p;\n}\n" ::"r"(d),
+            "r"(a), "l"(bd), "r"(tc_peak_idesc<KIND>()), "r"(sf), "r"(acc));
+}
+
+template <int KIND>
 __global__ void __launch_bounds__(128, 1) tc_peak_kernel(int iters, int *err) {
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     __shared__ uint64_t done_bar;
@@ -947,9 +1555,10 @@ __global__ void __launch_bounds__(128, 1) tc_peak_kernel(int iters, int *err) {
     tc_fence_after();
     const uint32_t tbase = tmem_slot;
     {
+        const uint32_t one = KIND == 2 ? 0x38383838u : 0x7F7F7F7Fu;  // unit scales
         uint32_t r[32];
 #pragma unroll
-        for (int k = 0; k < 32; ++k) r[k] = 0x7F7F7F7Fu;
+        for (int k = 0; k < 32; ++k) r[k] = one;
         tmem_st32(tbase + ((uint32_t)(32 * warp) << 16) + kTcSfCol, r);
 #pragma unroll
         for (int k = 0; k < 32; ++k) r[k] = 0x22222222u;
@@ -965,12 +1574,7 @@ __global__ void __launch_bounds__(128, 1) tc_peak_kernel(int iters, int *err) {
         const uint64_t bd = (uint64_t)((su32(tc_smem) & 0x3FFFF) >> 4) | ((uint64_t)(128 >> 4) << 16) |
                             ((uint64_t)(256 >> 4) << 32) | (1ull << 46);
         const uint32_t sf = tbase + kTcSfCol;
-        for (int i = 0; i < iters; ++i)
-            asm volatile(
-                "{\n .reg .pred p;\n setp.ne.b32 p, %5, 0;\n"
-                " tcgen05.mma.cta_group::1.kind::mxf4.block_scale.scale_vec::2X [%0], [%1], %2, %3, [%4], "
-                "[%4], p;\n}\n" ::"r"(tbase),
-                "r"(tbase + 256), "l"(bd), "r"(kTcPeakIdesc), "r"(sf), "r"(i > 0 ? 1u : 0u));
+        for (int i = 0; i < iters; ++i) tc_peak_mma<KIND>(tbase, tbase + 256, bd, sf, i > 0 ? 1u : 0u);
         tc_commit(&done_bar);
         const long long t0 = clock64();
         while (!mbar_try(&done_bar, 0)) {
@@ -989,9 +1593,13 @@ __global__ void __launch_bounds__(128, 1) tc_peak_kernel(int iters, int *err) {
     }
 }
 
-// Best of `reps` timed launches; TFLOP/s counting 2 per multiply-accumulate.
-cudaError_t tc_measure_peak(int num_sms, int reps, double *tflops, int *err, cudaStream_t stream) {
-    cudaError_t e = cudaFuncSetAttribute(tc_peak_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+// Best of `reps` timed launches of probe `kind`; TFLOP/s counting 2 per
+// multiply-accumulate.
+cudaError_t tc_measure_peak(int num_sms, int reps, int kind, double *tflops, int *err,
+                            cudaStream_t stream) {
+    if (kind < 0 || kind >= kTcPeakKinds) return cudaErrorInvalidValue;
+    auto kern = kind == 0 ? tc_peak_kernel<0> : kind == 1 ? tc_peak_kernel<1> : tc_peak_kernel<2>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          kTcPeakSmem);
     if (e != cudaSuccess) return e;
     cudaEvent_t e0, e1;
@@ -1004,7 +1612,7 @@ cudaError_t tc_measure_peak(int num_sms, int reps, double *tflops, int *err, cud
     double best = 0.0;
     for (int r = 0; r < reps + 1 && e == cudaSuccess; ++r) {
         cudaEventRecord(e0, stream);
-        tc_peak_kernel<<<num_sms, 128, kTcPeakSmem, stream>>>(iters, err);
+        kern<<<num_sms, 128, kTcPeakSmem, stream>>>(iters, err);
         cudaEventRecord(e1, stream);
         e = cudaEventSynchronize(e1);
         if (e == cudaSuccess) e = cudaGetLastError();
@@ -1020,8 +1628,6 @@ cudaError_t tc_measure_peak(int num_sms, int reps, double *tflops, int *err, cud
     return e;
 }
 
-int tc_tile_a_snps() { return kTcPairASnps; }
-int tc_tile_b_snps() { return kTcBSnps; }
 int tc_max_class() { return kTcMaxClass; }
 
 }  // namespace gepi

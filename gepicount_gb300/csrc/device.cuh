@@ -45,6 +45,25 @@ struct ScanState {
     float tau_f;                 // entropy: tau as mutual information in bits, rounded down
     int kerr;                    // non-zero: a counting kernel gave up a bounded wait
     double tau_val;              // tau as a value (I bits or -log10 p); -inf: none yet
+    uint32_t sel_mode;           // batched engine: select run after the last batch
+                                 // (0 none, 1 threshold select, 2 overflow retry)
+    uint32_t count_batch;        // batched engine: count after the last batch, before its select
+};
+
+struct SelState;
+
+// One request's select in a batched engine step (device memory; select.cu).
+struct SelJob {
+    Cand *in, *out;         // candidate buffer filled by the batch, and the other one
+    ScanState *st;
+    SelState *sel;          // radix-select scratch of the request
+    uint32_t cap, k;
+    uint32_t trigger;       // not the last batch: select when count > trigger
+    uint32_t count_before;  // candidates before the batch (overflow: compaction limit)
+    int32_t final_batch;    // the request's last batch: select when count > k
+    int32_t objective;
+    float lp_margin;
+    int32_t active;         // 0: no batch this step
 };
 
 struct ScanCtx {
@@ -57,6 +76,50 @@ struct ScanCtx {
     uint32_t cap;
     ScanState *st;
 };
+
+// ---- batched engine: one counting launch over the tiles of many requests ----
+
+// A request of an engine step (device memory).
+struct ReqDesc {
+    const uint32_t *planes;  // plane layout (popcount kernels)
+    const uint32_t *blk;     // block-major operand copy (tensor-core kernel)
+    const int2 *tiles;       // the request's tile list
+    int Wp, W0, rows_pad, n_snps;
+    int a0, a1, b0, b1;      // SNP ranges
+    ScanCtx ctx;             // tables, this step's candidate buffer, scan state
+};
+// A run of consecutive tiles of one request in a launch's work list.
+struct WorkRange {
+    int req;    // ReqDesc index
+    int first;  // first tile, as an index into the request's tile list
+    int start;  // position of the run's first tile in the work list
+    int count;
+};
+// One launch's work list; CTAs claim indices with `next` (zeroed every step).
+struct WorkQueue {
+    unsigned int next;
+    int ntiles;  // tiles in the list
+    int nranges;
+    int err;     // non-zero: the launch gave up a bounded wait
+    const WorkRange *ranges;
+};
+
+#ifdef __CUDACC__
+// Claimed work index t -> (request, A tile, B tile); (-1, 0, 0) past the end.
+__device__ __forceinline__ int4 resolve_work(const ReqDesc *reqs, const WorkQueue *q, int t) {
+    if (t >= q->ntiles) return make_int4(-1, 0, 0, 0);
+    const WorkRange *rg = q->ranges;
+    int lo = 0, hi = q->nranges - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (rg[mid].start <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    const WorkRange r = rg[lo];
+    const int2 tl = reqs[r.req].tiles[r.first + (t - r.start)];
+    return make_int4(r.req, tl.x, tl.y, 0);
+}
+#endif
 
 // Order-preserving map double -> u64 (larger double -> larger key).
 __host__ __device__ inline unsigned long long key_of(double v) {

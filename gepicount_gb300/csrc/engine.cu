@@ -4,17 +4,25 @@
 //
 // Replaces the reference's one-cohort-per-process batch loop
 // (launch_process_gpu_1, src/kernels/kernel1.cu:387-483).  Each request walks
-// its tile list in adaptive batches as a direct scan does, with the same
-// exact thresholds, so its results are bit-identical to gepi_scan_range's.
-// Requests progress independently and the host never waits on one request's
-// device work while others could be launched: every device operation of a
-// request (a counting batch, a threshold-raising radix select replayed from a
-// CUDA graph, an overflow retry's compaction) ends in a completion event that
-// the engine polls; when it fires, the request's next operation is issued at
-// once.  Batches can be capped to a device-time quantum, and requests with
-// little work left run on a high-priority stream, so short requests are not
-// held behind long ones.  Tile lists depend only on the SNP ranges and tile
-// shape and are cached on the device across requests.
+// its tile list in adaptive batches with the same exact thresholds as a direct
+// scan, so its results are bit-identical to gepi_scan_range's.  The engine
+// advances all requests in steps; one step is ONE CUDA graph replay:
+//   * an upload of the step's descriptors (per request: its tables, this
+//     step's candidate buffer and scan state, its slice of its tile list),
+//   * one persistent counting launch per kernel group -- the tensor-core
+//     kernel for every tensor-core request of an objective, the popcount
+//     kernel of a variant for every popcount request of that variant -- whose
+//     CTAs (pairs) claim tiles from the concatenated work list with an atomic
+//     counter,
+//   * one chain of 20 batched select launches over every request (gridDim.y =
+//     request), each request's select decided on the device from its scan
+//     state exactly as the direct scan decides it on the host,
+//   * a read-back of every request's scan state.
+// The graph is captured once per set of kernel groups and slot capacity and
+// replayed with new descriptors every step.  Between steps the host sizes
+// every request's next batch (append rate, select budget, optional
+// device-time quantum), retires finished requests and admits new ones
+// (serving), so requests arriving while others run join at the next step.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -26,6 +34,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <deque>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -62,18 +71,23 @@ double ms_between(Clock::time_point a, Clock::time_point b) {
     return std::chrono::duration<double, std::milli>(b - a).count();
 }
 
-// Requests whose remaining device work is estimated below this run on the
-// high-priority stream.
-constexpr double kShortMs = 50.0;
 // Device bytes of cached tile lists kept when no request uses them.
 constexpr size_t kTileCacheBytes = 1ull << 30;
+
+// Kernel groups of a step, in launch order: tensor cores (entropy, Fisher),
+// then one per popcount variant.
+constexpr int kGroups = 5;
+int group_of(const CountVariant &v, int objective) {
+    if (v.method == GEPI_METHOD_TENSOR) return objective == GEPI_ENTROPY ? 0 : 1;
+    return 1 + v.id;  // popcount variants 1..3 -> groups 2..4
+}
 
 }  // namespace
 
 struct ScanRequest {
     gepi_planes *pl = nullptr;
     int a0 = 0, na = 0, b0 = 0, nb = 0;
-    int k = 0, objective = 0, method = 0;
+    int k = 0, objective = 0, method = 0, variant = 0;
 };
 
 // Device tile list of one (SNP ranges, tile shape), shared by requests.
@@ -87,23 +101,11 @@ struct TileList {
 // strongest marginal SNPs first, so lists are kept per plane set
 using TileKey = std::array<int64_t, 7>;
 
-// Device resources of one request, pooled by candidate capacity.
+// Candidate buffers of one request, pooled by capacity.
 struct JobBuffers {
     Cand *cand[2] = {nullptr, nullptr};
     uint32_t cap = 0;
-    ScanState *state = nullptr;
-    ScanState *h_state = nullptr;  // pinned
-    void *sel = nullptr;           // radix-select scratch
-    cudaStream_t stream[2] = {nullptr, nullptr};  // normal, high priority
-    // scan start, scan done, batch launch start / end, operation complete
-    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-    cudaGraphExec_t sel_graph[2] = {nullptr, nullptr};  // select+compact cand[c] -> cand[c^1]
-    int sel_k = -1, sel_obj = -1;
-    float sel_margin = 0.f;
 };
-
-// The device operation a request has in flight.
-enum class Op { None, Batch, SelRetry, SelBudget, SelFinal };
 
 struct Job {
     ScanRequest rq;
@@ -112,68 +114,81 @@ struct Job {
     uint64_t ticket = 0;
     size_t footprint = 0;
     bool finished = false;  // serving: results ready for the waiter
-    bool tc = false;
+    const CountVariant *cv = nullptr;
+    int group = 0;
     int TA = 0, TB = 0;
+    double weight = 1.0;  // device cost of one tile relative to other requests'
     TileList *tl = nullptr;
-    size_t ntiles = 0, next = 0, batch = 1, inflight = 0, last_nbt = 0;
-    uint32_t last_appended = 0;
-    double ms_per_tile = 0.0;  // from the last batch (0: not measured yet)
+    size_t ntiles = 0, next = 0, batch = 1, inflight = 0;
     JobBuffers *buf = nullptr;
-    cudaStream_t s = nullptr;  // stream of the request's last operation
-    Op op = Op::None;
+    int slot = -1;
     int cur = 0;
-    uint32_t count = 0, budget = 0;
+    uint32_t count = 0, budget = 0, trigger = 0;
     int retries = 0;
     float lp_margin = 0.f;
-    bool started = false, done = false, final_selected = false;
-    bool oldest = false;  // the oldest unfinished request (Policy::Oldest)
+    bool done = false, final_selected = false;
     gepi_status status = GEPI_OK;
     std::string error;
     gepi_scan_stats S{};
     Clock::time_point t_submit, t_admit, t_done;
 };
 
-// Which requests' launches go on the high-priority stream: those with little
-// work left (shortest first), or the oldest unfinished request (first come,
-// first served, with the others filling the SMs it leaves).
+// Which requests' tiles go first in a step and get the quantum first: those
+// with little work left (shortest first), or the oldest.
 enum class Policy { ShortFirst, Oldest };
 
 class Engine {
    public:
-    // quantum_ms > 0 caps each batch at about that much device time.
+    // quantum_ms > 0 caps each step at about that much device time.
     Engine(int device, double quantum_ms, Policy policy = Policy::ShortFirst)
         : device_(device), quantum_ms_(quantum_ms), policy_(policy) {}
     ~Engine();
     gepi_status init();
-    // Method choice, plane-set tables and the device tile list: may run on
+    // Counting variant, plane-set tables and the device tile list: may run on
     // any thread (serialised internally).
     gepi_status prepare(Job &j);
-    // Candidate buffers and the initial scan state: the polling thread.
+    // Candidate buffers, a state slot and the initial scan state.
     gepi_status admit(Job &j);
-    // Issues the next operation of every idle request and completes those
-    // whose operation has finished; returns how many completed or finished.
-    int poll(std::vector<Job *> &active);
-    // Returns a request's buffers (after its streams drain) and tile list.
+    // One engine step over the active requests: finishes requests with no
+    // tiles left, runs one batch of every other one (one graph replay) and
+    // consumes the results.
+    void step(std::vector<Job *> &active);
+    // Returns a request's buffers, slot and tile list.
     void release(Job &j);
     std::mutex run_mu;  // serialises gepi_scan_batch calls on the device
+    gepi_batch_stats counters{};  // launches since the last reset
 
    private:
-    gepi_status advance(Job &j);
-    gepi_status complete(Job &j);
-    gepi_status launch(Job &j);
-    gepi_status select_async(Job &j, int n_override, uint32_t n_compact, Op op);
-    gepi_status finish(Job &j);
-    void size_next_batch(Job &j);
-    void fail(Job &j, gepi_status st);
+    gepi_status ensure_slots(int need);
+    // setup = true: only the kernels' shared-memory opt-ins and occupancy
+    // queries (outside any capture)
+    cudaError_t enqueue_step(unsigned mask, bool setup = false);
+    gepi_status launch_step(unsigned mask);
+    gepi_status finish(std::vector<Job *> &jobs);
+    void size_next_batch(Job &j, uint32_t appended, size_t nbt);
+    void plan(std::vector<Job *> &run);
 
     int device_ = 0, num_sms_ = 0;
     double quantum_ms_ = 0.0;
     Policy policy_ = Policy::ShortFirst;
-    int prio_lo_ = 0, prio_hi_ = 0;
+    cudaStream_t stream_ = nullptr, upload_ = nullptr;
+    cudaEvent_t ev_[3] = {nullptr, nullptr, nullptr};  // step start, counting done, step done
+    // per-slot device state: scan state, radix-select scratch
+    int nslots_ = 0;
+    ScanState *d_states_ = nullptr, *h_states_ = nullptr;
+    unsigned char *d_sel_ = nullptr;
+    std::vector<int> free_slots_;
+    // step descriptors: pinned host image and its device copy, same layout
+    // [WorkQueue x kGroups | ReqDesc x slots | SelJob x slots | WorkRange x slots x kGroups]
+    size_t step_bytes_ = 0, off_reqs_ = 0, off_jobs_ = 0, off_ranges_ = 0;
+    unsigned char *h_step_ = nullptr, *d_step_ = nullptr;
+    WorkQueue *h_queues_ = nullptr;  // pinned: the launches' error codes, read back each step
+    std::map<unsigned, cudaGraphExec_t> graphs_;
+    // estimated device ms per unit of tile weight, per kernel group
+    double ms_per_weight_[kGroups] = {0, 0, 0, 0, 0};
     std::vector<std::unique_ptr<JobBuffers>> pool_;
     std::vector<JobBuffers *> free_;
     std::mutex prep_mu_, cache_mu_;
-    cudaStream_t upload_ = nullptr;
     std::map<TileKey, TileList> tiles_;
     size_t tile_bytes_ = 0;
     uint64_t stamp_ = 0;
@@ -181,35 +196,158 @@ class Engine {
 
 Engine::~Engine() {
     DeviceGuard g(device_);
+    if (stream_) cudaStreamSynchronize(stream_);
+    for (auto &kv : graphs_) cudaGraphExecDestroy(kv.second);
     for (auto &b : pool_) {
-        for (cudaStream_t s : b->stream)
-            if (s) cudaStreamSynchronize(s);
         dfree(b->cand[0]);
         dfree(b->cand[1]);
-        dfree(b->state);
-        dfree(b->sel);
-        if (b->h_state) cudaFreeHost(b->h_state);
-        for (cudaEvent_t e : b->ev)
-            if (e) cudaEventDestroy(e);
-        for (cudaGraphExec_t x : b->sel_graph)
-            if (x) cudaGraphExecDestroy(x);
-        for (cudaStream_t s : b->stream)
-            if (s) cudaStreamDestroy(s);
     }
+    dfree(d_states_);
+    dfree(d_sel_);
+    dfree(d_step_);
+    if (h_states_) cudaFreeHost(h_states_);
+    if (h_step_) cudaFreeHost(h_step_);
+    if (h_queues_) cudaFreeHost(h_queues_);
+    for (cudaEvent_t e : ev_)
+        if (e) cudaEventDestroy(e);
     for (auto &kv : tiles_)
         if (kv.second.d) cudaFreeAsync(kv.second.d, upload_);
     if (upload_) {
         cudaStreamSynchronize(upload_);
         cudaStreamDestroy(upload_);
     }
+    if (stream_) cudaStreamDestroy(stream_);
 }
 
 gepi_status Engine::init() {
     DeviceGuard g(device_);
     if (!g.ok) return set_error(GEPI_ERR_CUDA, "cudaSetDevice failed");
     GEPI_CUDA(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, device_));
-    GEPI_CUDA(cudaDeviceGetStreamPriorityRange(&prio_lo_, &prio_hi_));
+    GEPI_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     GEPI_CUDA(cudaStreamCreateWithFlags(&upload_, cudaStreamNonBlocking));
+    for (cudaEvent_t &e : ev_) GEPI_CUDA(cudaEventCreate(&e));
+    GEPI_CUDA(cudaMallocHost(&h_queues_, sizeof(WorkQueue) * kGroups));
+    return ensure_slots(16);
+}
+
+// Slot capacity (a power of two): per-slot scan states and select scratch, and
+// the step descriptor buffers sized for that many requests.  Growing drops
+// the captured graphs (their launch shapes depend on the capacity).
+gepi_status Engine::ensure_slots(int need) {
+    if (need <= nslots_) return GEPI_OK;
+    int n = std::max(16, nslots_);
+    while (n < need) n *= 2;
+    GEPI_CUDA(cudaStreamSynchronize(stream_));
+    for (auto &kv : graphs_) cudaGraphExecDestroy(kv.second);
+    graphs_.clear();
+    ScanState *ds = nullptr, *hs = nullptr;
+    unsigned char *dsel = nullptr, *hstep = nullptr, *dstep = nullptr;
+    const size_t off_reqs = ((sizeof(WorkQueue) * kGroups + 255) / 256) * 256;
+    const size_t off_jobs = off_reqs + ((sizeof(ReqDesc) * n + 255) / 256) * 256;
+    const size_t off_ranges = off_jobs + ((sizeof(SelJob) * n + 255) / 256) * 256;
+    const size_t bytes = off_ranges + sizeof(WorkRange) * (size_t)n * kGroups;
+    cudaError_t e = cudaMalloc(&ds, sizeof(ScanState) * n);
+    if (e == cudaSuccess) e = cudaMallocHost(&hs, sizeof(ScanState) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&dsel, sel_state_bytes() * n);
+    if (e == cudaSuccess) e = cudaMallocHost(&hstep, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&dstep, bytes);
+    if (e == cudaSuccess && nslots_)  // keep the states of admitted requests
+        e = cudaMemcpy(ds, d_states_, sizeof(ScanState) * nslots_, cudaMemcpyDeviceToDevice);
+    if (e != cudaSuccess) {
+        dfree(ds);
+        dfree(dsel);
+        dfree(dstep);
+        if (hs) cudaFreeHost(hs);
+        if (hstep) cudaFreeHost(hstep);
+        return set_error(GEPI_ERR_CUDA, std::string("engine slots: ") + cudaGetErrorString(e));
+    }
+    std::memset(hstep, 0, bytes);
+    std::memset(hs, 0, sizeof(ScanState) * n);
+    if (nslots_) std::memcpy(hs, h_states_, sizeof(ScanState) * nslots_);
+    dfree(d_states_);
+    dfree(d_sel_);
+    dfree(d_step_);
+    if (h_states_) cudaFreeHost(h_states_);
+    if (h_step_) cudaFreeHost(h_step_);
+    d_states_ = ds;
+    h_states_ = hs;
+    d_sel_ = dsel;
+    h_step_ = hstep;
+    d_step_ = dstep;
+    step_bytes_ = bytes;
+    off_reqs_ = off_reqs;
+    off_jobs_ = off_jobs;
+    off_ranges_ = off_ranges;
+    for (int s = n - 1; s >= nslots_; --s) free_slots_.push_back(s);
+    std::sort(free_slots_.begin(), free_slots_.end(), std::greater<int>());
+    nslots_ = n;
+    return GEPI_OK;
+}
+
+// The device work of one step on the engine's stream: upload, the counting
+// launches of the kernel groups in `mask` (bit g), the batched selects, the
+// read-back.
+cudaError_t Engine::enqueue_step(unsigned mask, bool setup) {
+    WorkQueue *dq = reinterpret_cast<WorkQueue *>(d_step_);
+    const ReqDesc *dreqs = reinterpret_cast<const ReqDesc *>(d_step_ + off_reqs_);
+    SelJob *djobs = reinterpret_cast<SelJob *>(d_step_ + off_jobs_);
+    // the timing events are recorded as graph nodes when captured (external
+    // records), so the host can wait for and time every replay
+    auto record = [&](cudaEvent_t ev) {
+        return cudaEventRecordWithFlags(ev, stream_, cudaEventRecordExternal);
+    };
+    cudaError_t e = cudaSuccess;
+    if (!setup) e = cudaMemcpyAsync(d_step_, h_step_, step_bytes_, cudaMemcpyHostToDevice, stream_);
+    if (e == cudaSuccess && !setup) e = record(ev_[0]);
+    for (int g = 0; g < kGroups && e == cudaSuccess; ++g) {
+        if (!(mask & (1u << g))) continue;
+        if (g < 2) {
+            e = launch_tc_batch(dreqs, dq + g, g, num_sms_, stream_, setup);
+        } else {
+            const CountVariant *v = count_variant(g - 1);
+            e = launch_popc_batch(v->ta, v->words, dreqs, dq + g, num_sms_, stream_, setup);
+        }
+    }
+    if (setup) return e;
+    if (e == cudaSuccess) e = record(ev_[1]);
+    if (e == cudaSuccess) e = run_select_batch(djobs, nslots_, num_sms_, stream_);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h_states_, d_states_, sizeof(ScanState) * nslots_, cudaMemcpyDeviceToHost,
+                            stream_);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h_queues_, d_step_, sizeof(WorkQueue) * kGroups, cudaMemcpyDeviceToHost,
+                            stream_);
+    if (e == cudaSuccess) e = record(ev_[2]);
+    return e;
+}
+
+// Replays the step graph of `mask` (captured on first use; the timeout test's
+// kernels are a graph of their own), or enqueues the same work directly if a
+// capture is refused.
+gepi_status Engine::launch_step(unsigned mask) {
+    const unsigned key = mask | (tc_debug_stall() ? 1u << 16 : 0u);
+    auto it = graphs_.find(key);
+    if (it == graphs_.end()) {
+        GEPI_CUDA(enqueue_step(mask, true));
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t x = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            const cudaError_t e1 = enqueue_step(mask);
+            const cudaError_t e2 = cudaStreamEndCapture(stream_, &graph);
+            e = e1 != cudaSuccess ? e1 : e2;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&x, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            (void)cudaGetLastError();
+            GEPI_CUDA(enqueue_step(mask));
+            return GEPI_OK;
+        }
+        it = graphs_.emplace(key, x).first;
+    }
+    GEPI_CUDA(cudaGraphLaunch(it->second, stream_));
+    counters.graph_launches += 1;
     return GEPI_OK;
 }
 
@@ -219,13 +357,15 @@ gepi_status Engine::prepare(Job &j) {
     const ScanRequest &rq = j.rq;
     gepi_planes *pl = rq.pl;
     GEPI_TRY(pl_ensure_tables(pl));
-    int method = 0;
-    GEPI_TRY(pl_resolve_method(pl, rq.method, &method));
-    j.tc = method == GEPI_METHOD_TENSOR;
-    if (j.tc) GEPI_TRY(pl_ensure_tc_blocks(pl));
+    GEPI_TRY(pl_resolve_variant(pl, rq.method, rq.variant, &j.cv));
+    if (j.cv->method == GEPI_METHOD_TENSOR) GEPI_TRY(pl_ensure_tc_blocks(pl));
     GEPI_CUDA(cudaStreamSynchronize(pl->stream));  // decode, relayout, tables done
-    j.TA = j.tc ? tc_tile_a_snps() : popc_tile_snps();
-    j.TB = j.tc ? tc_tile_b_snps() : popc_tile_snps();
+    j.TA = j.cv->ta;
+    j.TB = j.cv->tb;
+    j.group = group_of(*j.cv, rq.objective);
+    // device cost of a tile: its pipeline stages (samples) times its SNP pairs
+    const double w = (double)j.cv->words;
+    j.weight = (std::ceil(pl->W0 / w) + std::ceil(pl->W1 / w)) * (double)j.TA * j.TB / 1024.0;
 
     const TileKey key{rq.a0, (int64_t)rq.a0 + rq.na, rq.b0, (int64_t)rq.b0 + rq.nb, j.TA, j.TB,
                       (int64_t)pl->serial};
@@ -273,8 +413,9 @@ gepi_status Engine::prepare(Job &j) {
     }
     j.ntiles = j.tl->n;
     j.S = gepi_scan_stats{};
-    j.S.method = method;
+    j.S.method = j.cv->method;
     j.S.tile_snps = j.TA;
+    j.S.variant = j.cv->id;
     j.S.tiles = j.ntiles;
     {
         // pairs (s, t), t < s, s in A, t in B; and SNPs in both ranges
@@ -296,6 +437,7 @@ gepi_status Engine::admit(Job &j) {
     DeviceGuard g(device_);
     const uint64_t cap = cand_cap(j.rq.k);
     if (cap > (1ull << 31)) return set_error(GEPI_ERR_LIMIT, "topmost too large");
+    if (free_slots_.empty()) GEPI_TRY(ensure_slots(nslots_ + 1));
     JobBuffers *b = nullptr;
     for (size_t i = 0; i < free_.size(); ++i)
         if (free_[i]->cap == cap) {
@@ -312,38 +454,32 @@ gepi_status Engine::admit(Job &j) {
         pool_.push_back(std::move(nb));
         GEPI_CUDA(cudaMalloc(&b->cand[0], cap * sizeof(Cand)));
         GEPI_CUDA(cudaMalloc(&b->cand[1], cap * sizeof(Cand)));
-        GEPI_CUDA(cudaMalloc(&b->state, sizeof(ScanState)));
-        GEPI_CUDA(cudaMalloc(&b->sel, sel_state_bytes()));
-        GEPI_CUDA(cudaMallocHost(&b->h_state, sizeof(ScanState)));
-        GEPI_CUDA(cudaStreamCreateWithPriority(&b->stream[0], cudaStreamNonBlocking, prio_lo_));
-        GEPI_CUDA(cudaStreamCreateWithPriority(&b->stream[1], cudaStreamNonBlocking, prio_hi_));
-        for (cudaEvent_t &e : b->ev) GEPI_CUDA(cudaEventCreate(&e));
     }
     j.buf = b;
-    // the first batch goes on the high-priority stream (no rate measured yet),
-    // so the state upload is ordered before it on that stream
-    j.s = b->stream[1];
+    j.slot = free_slots_.back();
+    free_slots_.pop_back();
     ScanState init{};
     init.tau_key = 0ull;
     init.theta = 0.f;
     init.lp_thr = INFINITY;
     init.tau_f = -INFINITY;
     init.tau_val = -INFINITY;
-    *b->h_state = init;  // the previous user's copies have drained (release)
-    GEPI_CUDA(cudaMemcpyAsync(b->state, b->h_state, sizeof(ScanState), cudaMemcpyHostToDevice, j.s));
+    h_states_[j.slot] = init;  // no step in flight: the read-back buffer is free
+    GEPI_CUDA(cudaMemcpyAsync(d_states_ + j.slot, h_states_ + j.slot, sizeof(ScanState),
+                              cudaMemcpyHostToDevice, stream_));
+    GEPI_CUDA(cudaStreamSynchronize(stream_));
 
-    // as in the direct scan: the same select budget and first batch
+    // as in the direct scan: the same select budget, trigger and first batch
     const double tests_per_tile = 20.0 * j.TA * j.TB;
     j.budget = select_budget(b->cap, j.rq.k);
+    j.trigger = select_trigger(j.budget, j.rq.k);
     j.batch = (size_t)std::max(1.0, std::floor(pilot_tests(j.rq.objective, j.budget) / tests_per_tile));
     j.lp_margin = 2e-6f * j.rq.pl->lf_max + 1e-3f;
     j.cur = 0;
     j.next = 0;
     j.count = 0;
     j.retries = 0;
-    j.ms_per_tile = 0.0;
-    j.op = Op::None;
-    j.started = j.done = j.final_selected = false;
+    j.done = j.final_selected = false;
     j.t_admit = Clock::now();
     return GEPI_OK;
 }
@@ -351,9 +487,12 @@ gepi_status Engine::admit(Job &j) {
 void Engine::release(Job &j) {
     DeviceGuard g(device_);
     if (j.buf) {
-        for (cudaStream_t s : j.buf->stream) cudaStreamSynchronize(s);  // nothing in flight on reuse
         free_.push_back(j.buf);
         j.buf = nullptr;
+    }
+    if (j.slot >= 0) {
+        free_slots_.push_back(j.slot);
+        j.slot = -1;
     }
     if (j.tl) {
         std::lock_guard<std::mutex> ck(cache_mu_);
@@ -362,251 +501,254 @@ void Engine::release(Job &j) {
     }
 }
 
-void Engine::fail(Job &j, gepi_status st) {
-    j.status = st;
-    j.error = gepi_last_error();
-    j.done = true;
-    j.op = Op::None;
-    j.t_done = Clock::now();
-}
-
-// Queues the next batch of `j`: counting launch, state read-back, completion
-// event.  The policy picks the stream (high priority: a request with little
-// work left, or the oldest request); every earlier operation of the request
-// has completed, so changing streams between operations keeps its order.
-gepi_status Engine::launch(Job &j) {
-    JobBuffers *b = j.buf;
-    gepi_planes *pl = j.rq.pl;
-    const ScanRequest &r = j.rq;
-    j.inflight = std::min(j.batch, j.ntiles - j.next);
-    const bool high =
-        policy_ == Policy::Oldest
-            ? j.oldest
-            : (j.ms_per_tile <= 0.0 || (double)(j.ntiles - j.next) * j.ms_per_tile < kShortMs);
-    j.s = b->stream[high ? 1 : 0];
-    ScanCtx ctx;
-    ctx.T = pl->d_T;
-    ctx.F = pl->F;
-    ctx.lf = pl->d_lf;
-    ctx.lf32 = pl->d_lf32;
-    ctx.objective = r.objective;
-    ctx.cap = b->cap;
-    ctx.st = b->state;
-    ctx.cand = b->cand[j.cur];
-    if (!j.started) {
-        GEPI_CUDA(cudaEventRecord(b->ev[0], j.s));
-        j.started = true;
+// Reads the surviving candidates of finished requests back and writes their
+// ranked top-k.
+gepi_status Engine::finish(std::vector<Job *> &jobs) {
+    if (jobs.empty()) return GEPI_OK;
+    std::vector<std::vector<Cand>> host(jobs.size());
+    for (size_t i = 0; i < jobs.size(); ++i) {
+        Job &j = *jobs[i];
+        host[i].resize(j.count);
+        if (j.count)  // pageable destination: ordered on the stream
+            GEPI_CUDA(cudaMemcpyAsync(host[i].data(), j.buf->cand[j.cur], (size_t)j.count * sizeof(Cand),
+                                      cudaMemcpyDeviceToHost, stream_));
     }
-    GEPI_CUDA(cudaEventRecord(b->ev[2], j.s));
-    if (j.tc)
-        GEPI_CUDA(launch_tc_tiles(pl->d_tc_blocks, pl->n_snps, pl->Wp, pl->W0, j.tl->d + j.next,
-                                  (int)j.inflight, r.a0, r.a0 + r.na, r.b0, r.b0 + r.nb, ctx,
-                                  nullptr, &b->state->kerr, num_sms_, j.s));
-    else
-        GEPI_CUDA(launch_popc_tiles(pl->d_planes, pl->Wp, pl->W0, j.tl->d + j.next,
-                                    (int)j.inflight, r.a0, r.a0 + r.na, r.b0, r.b0 + r.nb, ctx,
-                                    nullptr, j.s));
-    GEPI_CUDA(cudaEventRecord(b->ev[3], j.s));
-    GEPI_CUDA(cudaMemcpyAsync(b->h_state, b->state, sizeof(ScanState), cudaMemcpyDeviceToHost, j.s));
-    GEPI_CUDA(cudaEventRecord(b->ev[4], j.s));
-    j.op = Op::Batch;
-    return GEPI_OK;
-}
-
-// Device radix select of the k-th best key, then compaction into the other
-// buffer, state read-back and completion event.  The common form (all
-// entries) replays a CUDA graph captured once per buffer orientation.
-gepi_status Engine::select_async(Job &j, int n_override, uint32_t n_compact, Op op) {
-    JobBuffers *b = j.buf;
-    const int k = j.rq.k, obj = j.rq.objective;
-    Cand *in = b->cand[j.cur], *out = b->cand[j.cur ^ 1];
-    j.S.other_launches += kSelectLaunches;
-    bool done = false;
-    if (n_override < 0 && n_compact == 0xFFFFFFFFu) {
-        if (b->sel_k != k || b->sel_obj != obj || b->sel_margin != j.lp_margin) {
-            for (cudaGraphExec_t &x : b->sel_graph)
-                if (x) {
-                    cudaGraphExecDestroy(x);
-                    x = nullptr;
-                }
-            b->sel_k = k;
-            b->sel_obj = obj;
-            b->sel_margin = j.lp_margin;
+    GEPI_CUDA(cudaStreamSynchronize(stream_));
+    for (size_t i = 0; i < jobs.size(); ++i) {
+        Job &j = *jobs[i];
+        const int k = j.rq.k;
+        std::memset(j.tops, 0, sizeof(gepi_result) * (size_t)k);
+        const size_t keep = std::min<size_t>(host[i].size(), (size_t)k);
+        std::partial_sort(host[i].begin(), host[i].begin() + keep, host[i].end(), cand_better);
+        for (size_t q = 0; q < keep; ++q) {
+            const Cand &c = host[i][q];
+            gepi_result &r = j.tops[q];
+            r.sA = c.rA;
+            r.sB = c.rBfun >> 3;
+            r.fun = (char)(c.rBfun & 7);
+            for (int t = 0; t < 4; ++t) r.n[t] = c.n[t];
+            r.ent = (float)(-value_of_key(c.key));
         }
-        cudaGraphExec_t &x = b->sel_graph[j.cur];
-        if (!x) {
-            cudaGraph_t graph = nullptr;
-            if (cudaStreamBeginCapture(j.s, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-                cudaError_t e = run_select_compact(in, out, b->state, b->sel, b->cap, (uint32_t)k,
-                                                   -1, 0xFFFFFFFFu, obj, j.lp_margin, num_sms_, j.s);
-                cudaError_t e2 = cudaStreamEndCapture(j.s, &graph);
-                if (e == cudaSuccess && e2 == cudaSuccess && graph &&
-                    cudaGraphInstantiate(&x, graph, 0) != cudaSuccess)
-                    x = nullptr;
-                if (graph) cudaGraphDestroy(graph);
-                cudaGetLastError();  // a failed capture leaves the plain launches below
-            }
-        }
-        if (x) {
-            GEPI_CUDA(cudaGraphLaunch(x, j.s));
-            done = true;
-        }
+        j.S.candidates = j.count;
+        j.done = true;
+        j.t_done = Clock::now();
     }
-    if (!done)
-        GEPI_CUDA(run_select_compact(in, out, b->state, b->sel, b->cap, (uint32_t)k, n_override,
-                                     n_compact, obj, j.lp_margin, num_sms_, j.s));
-    j.cur ^= 1;
-    GEPI_CUDA(cudaMemcpyAsync(b->h_state, b->state, sizeof(ScanState), cudaMemcpyDeviceToHost, j.s));
-    GEPI_CUDA(cudaEventRecord(b->ev[4], j.s));
-    j.op = op;
-    return GEPI_OK;
-}
-
-// Reads the surviving candidates back and writes the ranked top-k.
-gepi_status Engine::finish(Job &j) {
-    JobBuffers *b = j.buf;
-    const uint32_t count = j.count;
-    std::vector<Cand> host(count);
-    GEPI_CUDA(cudaEventRecord(b->ev[1], j.s));
-    if (count)  // pageable destination: returns when the copy is done
-        GEPI_CUDA(cudaMemcpyAsync(host.data(), b->cand[j.cur], (size_t)count * sizeof(Cand),
-                                  cudaMemcpyDeviceToHost, j.s));
-    GEPI_CUDA(cudaEventSynchronize(b->ev[1]));
-    float ms = 0.f;
-    if (j.started) GEPI_CUDA(cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]));
-    j.S.scan_ms = ms;
-    j.S.candidates = count;
-    const int k = j.rq.k;
-    std::memset(j.tops, 0, sizeof(gepi_result) * (size_t)k);
-    const size_t keep = std::min<size_t>(host.size(), (size_t)k);
-    std::partial_sort(host.begin(), host.begin() + keep, host.end(), cand_better);
-    for (size_t i = 0; i < keep; ++i) {
-        const Cand &c = host[i];
-        gepi_result &r = j.tops[i];
-        r.sA = c.rA;
-        r.sB = c.rBfun >> 3;
-        r.fun = (char)(c.rBfun & 7);
-        for (int q = 0; q < 4; ++q) r.n[q] = c.n[q];
-        r.ent = (float)(-value_of_key(c.key));
-    }
-    j.done = true;
-    j.t_done = Clock::now();
     return GEPI_OK;
 }
 
 // Next batch: as many tiles as the remaining budget allows at the append
-// rate just observed, growing at most 8x per step, and within the device-time
-// quantum at the rate just measured (an over-estimate when other requests
-// shared the SMs).
-void Engine::size_next_batch(Job &j) {
-    const double nbt = (double)std::max<size_t>(1, j.last_nbt);
-    const double rate = std::max(1.0, (double)j.last_appended) / nbt;
+// rate just observed, growing at most 8x per step (the direct scan's rule).
+void Engine::size_next_batch(Job &j, uint32_t appended, size_t nbt) {
+    const double rate = std::max(1.0, (double)appended) / (double)std::max<size_t>(1, nbt);
     const double room = (double)j.budget - (double)j.count;
     double nb_next = room > 0 ? room / rate : 1.0;
-    nb_next = std::min(nb_next, 8.0 * nbt);
-    if (quantum_ms_ > 0.0 && j.ms_per_tile > 0.0)
-        nb_next = std::min(nb_next, quantum_ms_ / j.ms_per_tile);
+    nb_next = std::min(nb_next, 8.0 * (double)std::max<size_t>(1, nbt));
     j.batch = (size_t)std::max(1.0, nb_next);
 }
 
-// Issues the request's next operation (no operation in flight).
-gepi_status Engine::advance(Job &j) {
-    if (j.next >= j.ntiles) {
-        if (j.count > (uint32_t)j.rq.k && !j.final_selected)
-            return select_async(j, -1, 0xFFFFFFFFu, Op::SelFinal);
-        return finish(j);
-    }
-    return launch(j);
-}
-
-// Consumes the result of the operation that just completed, then advances.
-gepi_status Engine::complete(Job &j) {
-    JobBuffers *b = j.buf;
-    const Op op = j.op;
-    j.op = Op::None;
-    const ScanState st = *b->h_state;
-    switch (op) {
-    case Op::Batch: {
-        float ms = 0.f;
-        GEPI_CUDA(cudaEventElapsedTime(&ms, b->ev[2], b->ev[3]));
-        j.S.count_ms += ms;
-        j.S.max_count_ms = std::max<double>(j.S.max_count_ms, ms);
-        j.S.count_launches += 1;
-        if (st.kerr)
-            return set_error(GEPI_ERR_TIMEOUT, "counting kernel gave up a bounded wait (code " +
-                                                   std::to_string(st.kerr) + ")");
-        const size_t nbt = j.inflight;
-        if (nbt > 0 && ms > 0.f) j.ms_per_tile = (double)ms / (double)nbt;
-        j.last_nbt = nbt;
-        if (st.overflow) {
-            // Tighten with everything captured (a valid lower bound), drop
-            // this batch's partial appends, retry it in halves.  Only more
-            // than `cap` exactly tied candidates keep overflowing 1 tile.
-            if (++j.retries > 64)
-                return set_error(GEPI_ERR_LIMIT, "candidate buffer keeps overflowing (massive ties)");
-            j.S.overflows += 1;
-            return select_async(j, (int)b->cap, j.count, Op::SelRetry);
+// This step's batch of every running request: its natural batch; under a
+// device-time quantum the requests, in policy order (least work left first,
+// or oldest first), fill the quantum, each getting at least one tile.  The
+// order is also the order of their tiles in the work lists, so the CTAs claim
+// the first requests' tiles first.
+void Engine::plan(std::vector<Job *> &run) {
+    auto left = [&](const Job *j) {
+        return (double)(j->ntiles - j->next) * j->weight * ms_per_weight_[j->group];
+    };
+    if (policy_ == Policy::Oldest)
+        std::stable_sort(run.begin(), run.end(),
+                         [](const Job *a, const Job *b) { return a->t_admit < b->t_admit; });
+    else
+        std::stable_sort(run.begin(), run.end(),
+                         [&](const Job *a, const Job *b) { return left(a) < left(b); });
+    double room = quantum_ms_;
+    for (Job *j : run) {
+        size_t nbt = std::min(j->batch, j->ntiles - j->next);
+        const double per_tile = j->weight * ms_per_weight_[j->group];
+        if (quantum_ms_ > 0.0 && per_tile > 0.0 && nbt > 0) {
+            const double fit = std::floor(std::max(0.0, room) / per_tile);
+            nbt = std::max<size_t>(1, (size_t)std::min<double>((double)nbt, fit));
+            room -= (double)nbt * per_tile;
         }
-        j.last_appended = st.count - j.count;
-        j.count = st.count;
-        j.next += nbt;
-        j.retries = 0;
-        j.S.batches += 1;
-        if (j.next < j.ntiles && j.count > select_trigger(j.budget, j.rq.k))
-            return select_async(j, -1, 0xFFFFFFFFu, Op::SelBudget);
-        if (j.next < j.ntiles) size_next_batch(j);
-        return advance(j);
+        j->inflight = nbt;
     }
-    case Op::SelRetry:
-        j.count = st.count;
-        j.batch = std::max<size_t>(1, j.last_nbt / 2);
-        return advance(j);
-    case Op::SelBudget:
-        j.count = st.count;
-        size_next_batch(j);
-        return advance(j);
-    case Op::SelFinal:
-        j.count = st.count;
-        j.final_selected = true;
-        return advance(j);
-    case Op::None:
-        break;
-    }
-    return advance(j);
 }
 
-int Engine::poll(std::vector<Job *> &active) {
+void Engine::step(std::vector<Job *> &active) {
     DeviceGuard g(device_);
-    int progressed = 0;
-    if (policy_ == Policy::Oldest) {
-        Job *old = nullptr;
-        for (Job *j : active) {
-            j->oldest = false;
-            if (!j->done && (!old || j->t_admit < old->t_admit)) old = j;
+    // requests with every tile counted and no select pending finish; the rest
+    // run a batch (possibly empty: only the final select is left)
+    std::vector<Job *> fin, run;
+    for (Job *j : active) {
+        if (j->done) continue;
+        if (j->next >= j->ntiles && (j->count <= (uint32_t)j->rq.k || j->final_selected))
+            fin.push_back(j);
+        else
+            run.push_back(j);
+    }
+    auto fail_all = [&](std::vector<Job *> &js, gepi_status st) {
+        for (Job *j : js) {
+            j->status = st;
+            j->error = gepi_last_error();
+            j->done = true;
+            j->t_done = Clock::now();
         }
-        if (old) old->oldest = true;
+    };
+    if (!fin.empty()) {
+        const gepi_status st = finish(fin);
+        if (st != GEPI_OK) fail_all(fin, st);
     }
-    for (Job *j : active) {
-        if (j->done || j->op != Op::None) continue;
-        gepi_status st = advance(*j);  // newly admitted, or an empty range
-        if (st != GEPI_OK) fail(*j, st);
-        if (j->done) ++progressed;
+    if (run.empty()) return;
+    plan(run);
+
+    // the step's descriptors
+    WorkQueue *hq = reinterpret_cast<WorkQueue *>(h_step_);
+    ReqDesc *hreqs = reinterpret_cast<ReqDesc *>(h_step_ + off_reqs_);
+    SelJob *hjobs = reinterpret_cast<SelJob *>(h_step_ + off_jobs_);
+    WorkRange *hranges = reinterpret_cast<WorkRange *>(h_step_ + off_ranges_);
+    const WorkRange *dranges = reinterpret_cast<const WorkRange *>(d_step_ + off_ranges_);
+    for (int q = 0; q < kGroups; ++q) {
+        hq[q] = WorkQueue{};
+        hq[q].ranges = dranges + (size_t)q * nslots_;
     }
-    for (Job *j : active) {
-        if (j->done || j->op == Op::None) continue;
-        const cudaError_t q = cudaEventQuery(j->buf->ev[4]);
-        if (q == cudaErrorNotReady) continue;
-        gepi_status st = GEPI_OK;
-        if (q != cudaSuccess) {
-            cudaGetLastError();
-            st = set_error(GEPI_ERR_CUDA, std::string("scan operation: ") + cudaGetErrorString(q));
+    for (int s = 0; s < nslots_; ++s) hjobs[s] = SelJob{};
+    unsigned mask = 0;
+    for (Job *j : run) {
+        gepi_planes *pl = j->rq.pl;
+        const int s = j->slot;
+        ReqDesc &R = hreqs[s];
+        R.planes = pl->d_planes;
+        R.blk = pl->d_tc_blocks;
+        R.tiles = j->tl->d;
+        R.Wp = pl->Wp;
+        R.W0 = pl->W0;
+        R.rows_pad = j->cv->method == GEPI_METHOD_TENSOR ? tc_rows_pad(pl->n_snps) : 0;
+        R.n_snps = pl->n_snps;
+        R.a0 = j->rq.a0;
+        R.a1 = j->rq.a0 + j->rq.na;
+        R.b0 = j->rq.b0;
+        R.b1 = j->rq.b0 + j->rq.nb;
+        R.ctx.T = pl->d_T;
+        R.ctx.F = pl->F;
+        R.ctx.lf = pl->d_lf;
+        R.ctx.lf32 = pl->d_lf32;
+        R.ctx.objective = j->rq.objective;
+        R.ctx.cand = j->buf->cand[j->cur];
+        R.ctx.cap = j->buf->cap;
+        R.ctx.st = d_states_ + s;
+        const size_t nbt = j->inflight;
+        if (nbt > 0) {
+            WorkQueue &q = hq[j->group];
+            WorkRange &r = hranges[(size_t)j->group * nslots_ + q.nranges];
+            r.req = s;
+            r.first = (int)j->next;
+            r.start = q.ntiles;
+            r.count = (int)nbt;
+            q.ntiles += (int)nbt;
+            q.nranges += 1;
+            mask |= 1u << j->group;
+        }
+        SelJob &sj = hjobs[s];
+        sj.in = j->buf->cand[j->cur];
+        sj.out = j->buf->cand[j->cur ^ 1];
+        sj.st = d_states_ + s;
+        sj.sel = reinterpret_cast<SelState *>(d_sel_ + sel_state_bytes() * (size_t)s);
+        sj.cap = j->buf->cap;
+        sj.k = (uint32_t)j->rq.k;
+        sj.trigger = j->trigger;
+        sj.count_before = j->count;
+        sj.final_batch = j->next + nbt >= j->ntiles ? 1 : 0;
+        sj.objective = j->rq.objective;
+        sj.lp_margin = j->lp_margin;
+        sj.active = 1;
+    }
+    gepi_status st = launch_step(mask);
+    counters.steps += 1;
+    // on any failure below, the step's device work finishes before the
+    // requests -- and their buffers -- are released
+    auto drain = [&]() {
+        cudaStreamSynchronize(stream_);
+        (void)cudaGetLastError();
+    };
+    counters.select_launches += kSelectLaunches;
+    for (int q = 0; q < kGroups; ++q) counters.count_launches += (mask >> q) & 1u;
+    if (st == GEPI_OK) {
+        const cudaError_t e = cudaEventSynchronize(ev_[2]);
+        if (e != cudaSuccess) {
+            (void)cudaGetLastError();
+            st = set_error(GEPI_ERR_CUDA, std::string("engine step: ") + cudaGetErrorString(e));
+        }
+    }
+    float count_ms = 0.f, step_ms = 0.f;
+    if (st == GEPI_OK) {
+        cudaEventElapsedTime(&count_ms, ev_[0], ev_[1]);
+        cudaEventElapsedTime(&step_ms, ev_[0], ev_[2]);
+        for (int q = 0; q < kGroups; ++q)
+            if ((mask & (1u << q)) && h_queues_[q].err) {
+                st = set_error(GEPI_ERR_TIMEOUT, "counting kernel gave up a bounded wait (code " +
+                                                     std::to_string(h_queues_[q].err) + ")");
+                break;
+            }
+    }
+    if (st != GEPI_OK) {
+        drain();
+        fail_all(run, st);
+        return;
+    }
+    // device cost per unit of tile weight, per group (for the quantum)
+    {
+        double w[kGroups] = {0, 0, 0, 0, 0};
+        for (Job *j : run) w[j->group] += (double)j->inflight * j->weight;
+        double wsum = 0.0;
+        for (double v : w) wsum += v;
+        if (wsum > 0.0 && count_ms > 0.f) {
+            const double per = (double)count_ms / wsum;
+            for (int q = 0; q < kGroups; ++q)
+                if (w[q] > 0.0)
+                    ms_per_weight_[q] = ms_per_weight_[q] > 0.0 ? 0.5 * (ms_per_weight_[q] + per) : per;
+        }
+    }
+    for (Job *j : run) {
+        const ScanState &ss = h_states_[j->slot];
+        const size_t nbt = j->inflight;
+        j->S.scan_ms += step_ms;
+        j->S.other_launches += kSelectLaunches;
+        if (nbt > 0) {
+            j->S.count_ms += count_ms;
+            j->S.max_count_ms = std::max<double>(j->S.max_count_ms, count_ms);
+            j->S.count_launches += 1;
+        }
+        const uint32_t mode = ss.sel_mode;
+        if (mode == 2) {
+            // overflow: the select tightened with everything captured and kept
+            // only the candidates from before the batch; retry it in halves
+            j->cur ^= 1;
+            j->count = ss.count;
+            j->S.overflows += 1;
+            if (++j->retries > 64) {
+                j->status = set_error(GEPI_ERR_LIMIT, "candidate buffer keeps overflowing (massive ties)");
+                j->error = gepi_last_error();
+                j->done = true;
+                j->t_done = Clock::now();
+                continue;
+            }
+            j->batch = std::max<size_t>(1, nbt / 2);
+            continue;
+        }
+        const uint32_t appended = ss.count_batch - j->count;
+        if (mode == 1) j->cur ^= 1;
+        j->count = ss.count;
+        j->retries = 0;
+        if (nbt > 0) {
+            j->next += nbt;
+            j->S.batches += 1;
+        }
+        if (j->next >= j->ntiles) {
+            if (mode == 1) j->final_selected = true;
         } else {
-            st = complete(*j);
+            size_next_batch(*j, appended, nbt);
         }
-        if (st != GEPI_OK) fail(*j, st);
-        ++progressed;
     }
-    return progressed;
 }
 
 // ---- the device engines used by gepi_scan_batch -----------------------------
@@ -635,6 +777,8 @@ gepi_status check_request(const gepi_scan_req &r, ScanRequest *out) {
         return set_error(GEPI_ERR_ARG, "scan request: unknown objective");
     if (r.method < GEPI_METHOD_AUTO || r.method > GEPI_METHOD_TENSOR)
         return set_error(GEPI_ERR_ARG, "scan request: unknown method");
+    if (r.variant != 0 && !count_variant(r.variant))
+        return set_error(GEPI_ERR_ARG, "scan request: unknown counting variant");
     const int n = r.planes->n_snps;
     ScanRequest q;
     q.pl = r.planes;
@@ -654,14 +798,13 @@ gepi_status check_request(const gepi_scan_req &r, ScanRequest *out) {
     q.k = r.topmost;
     q.objective = r.objective;
     q.method = r.method;
+    q.variant = r.variant;
     *out = q;
     return GEPI_OK;
 }
 
 // Device memory a request holds while admitted: two candidate buffers.
 size_t request_footprint(int k) { return 2 * cand_cap(k) * sizeof(Cand) + sizeof(ScanState); }
-
-void idle_wait() { std::this_thread::sleep_for(std::chrono::microseconds(20)); }
 
 Policy env_policy(Policy dflt) {
     if (const char *e = std::getenv("GEPI_SERVE_POLICY")) {
@@ -702,6 +845,7 @@ gepi_status gepi_scan_batch(const gepi_scan_req *reqs, int32_t n, gepi_result *c
     Engine *eng = nullptr;
     GEPI_TRY(device_engine(reqs[0].planes->device, &eng));
     std::lock_guard<std::mutex> run_lock(eng->run_mu);
+    eng->counters = gepi_batch_stats{};
     std::vector<Job *> active;
     gepi_status st = GEPI_OK;
     for (Job &j : jobs) {
@@ -714,7 +858,7 @@ gepi_status gepi_scan_batch(const gepi_scan_req *reqs, int32_t n, gepi_result *c
         bool any = false;
         for (Job *j : active) any |= !j->done;
         if (!any) break;
-        if (eng->poll(active) == 0) idle_wait();
+        eng->step(active);
         for (Job *j : active)
             if (j->status != GEPI_OK) {
                 st = set_error(j->status, j->error);
@@ -726,6 +870,16 @@ gepi_status gepi_scan_batch(const gepi_scan_req *reqs, int32_t n, gepi_result *c
         eng->release(jobs[i]);
     }
     return st;
+}
+
+gepi_status gepi_scan_batch_stats(int32_t device, gepi_batch_stats *out) {
+    clear_error();
+    if (!out) return set_error(GEPI_ERR_ARG, "gepi_scan_batch_stats: null output");
+    Engine *eng = nullptr;
+    GEPI_TRY(device_engine(device, &eng));
+    std::lock_guard<std::mutex> run_lock(eng->run_mu);
+    *out = eng->counters;
+    return GEPI_OK;
 }
 
 }  // extern "C"
@@ -746,16 +900,17 @@ struct gepi_server {
     void run();
 };
 
+// Continuous batching: between two engine steps the loop admits queued
+// requests (first in, first out, while their footprint fits the budget; the
+// oldest always when nothing runs) and retires finished ones, so a request
+// arriving while others run joins at the next step.
 void gepi_server::run() {
     cudaSetDevice(device);
     std::vector<Job *> active, admitting;
-    bool idle = false;
     for (;;) {
         {
             std::unique_lock<std::mutex> lk(mu);
             for (;;) {
-                // admission: FIFO while the footprint fits; the head always
-                // gets in when nothing runs, so no request starves
                 while (!pending.empty()) {
                     Job *j = pending.front();
                     if (!active.empty() && used + j->footprint > budget) break;
@@ -767,8 +922,6 @@ void gepi_server::run() {
                 if (stop) return;
                 cv_work.wait(lk);
             }
-            // nothing completed last time round: sleep briefly, waking on a submit
-            if (idle && admitting.empty()) cv_work.wait_for(lk, std::chrono::microseconds(20));
         }
         for (Job *j : admitting) {
             gepi_status st = engine->admit(*j);
@@ -781,7 +934,7 @@ void gepi_server::run() {
             active.push_back(j);
         }
         admitting.clear();
-        idle = engine->poll(active) == 0;
+        engine->step(active);
         bool any = false;
         for (Job *j : active)
             if (j->done) {
@@ -797,7 +950,6 @@ void gepi_server::run() {
             }
         active.erase(std::remove_if(active.begin(), active.end(), [](Job *j) { return j->done; }),
                      active.end());
-        idle = false;
         cv_done.notify_all();
     }
 }
@@ -833,7 +985,7 @@ gepi_status gepi_server_submit(gepi_server *srv, const gepi_scan_req *req, uint6
     j->own_tops.assign((size_t)rq.k, gepi_result{});
     j->tops = j->own_tops.data();
     j->footprint = request_footprint(rq.k);
-    // method, tables and tile list on the caller's thread, off the loop
+    // variant, tables and tile list on the caller's thread, off the loop
     gepi_status st = srv->engine->prepare(*j);
     if (st != GEPI_OK) {
         srv->engine->release(*j);

@@ -21,25 +21,61 @@ cudaError_t launch_marginal(const uint32_t *planes, int n_snps, int Wp, int W0, 
 cudaError_t launch_decode_rows(const uint64_t *bits, const uint64_t *valid, int nw, int n_snps,
                                const int32_t *perm, int Wp, uint32_t *planes,
                                cudaStream_t stream, int num_sms);
-cudaError_t launch_popc_tiles(const uint32_t *planes, int Wp, int W0, const int2 *tiles,
-                              int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
-                              uint32_t *dump, cudaStream_t stream);
+// Popcount kernel of tile height ta (32 or 64 A SNPs; B tiles hold 32) and kc
+// plane words per pipeline stage (16 or 32).
+cudaError_t launch_popc_tiles(int ta, int kc, const uint32_t *planes, int Wp, int W0,
+                              const int2 *tiles, int ntiles, int a0, int a1, int b0, int b1,
+                              const ScanCtx &ctx, uint32_t *dump, cudaStream_t stream);
 cudaError_t launch_tc_tiles(const uint32_t *blk, int n_snps, int Wp, int W0, const int2 *tiles,
                             int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
                             uint32_t *dump, int *err, int num_sms, cudaStream_t stream);
 cudaError_t launch_tc_relayout(const uint32_t *planes, int Wp, int W0, int n_snps, uint32_t *blk,
                                int num_sms, cudaStream_t stream);
+// Batched engine: one persistent launch over the work list `q` of many
+// requests (reqs), tiles claimed with an atomic counter.  Tensor cores: every
+// request of one objective; popcount: every request of one (ta, kc) variant.
+// setup = true: only the kernel's shared-memory opt-in and occupancy query,
+// done once outside any stream capture before a launch is captured.
+cudaError_t launch_tc_batch(const ReqDesc *reqs, WorkQueue *q, int objective, int num_sms,
+                            cudaStream_t stream, bool setup = false);
+cudaError_t launch_popc_batch(int ta, int kc, const ReqDesc *reqs, WorkQueue *q, int num_sms,
+                              cudaStream_t stream, bool setup = false);
+bool tc_shape_ok(int Wp, int W0);  // class widths the tensor-core kernel takes
+bool tc_debug_stall();             // the timeout test's setting (GEPI_DEBUG_STALL) is on
+int tc_rows_pad(int n_snps);       // rows of the block-major operand copy
 size_t tc_block_words(int n_snps, int Wp, int W0);
-cudaError_t tc_measure_peak(int num_sms, int reps, double *tflops, int *err, cudaStream_t stream);
-int tc_tile_a_snps();
-int tc_tile_b_snps();
+cudaError_t tc_measure_peak(int num_sms, int reps, int kind, double *tflops, int *err,
+                            cudaStream_t stream);
 int tc_max_class();  // samples per class the tensor-core kernel takes
 cudaError_t run_select_compact(Cand *in, Cand *out, ScanState *st, void *sel, uint32_t cap,
                                uint32_t k, int n_override, uint32_t n_compact, int objective,
                                float lp_margin, int num_sms, cudaStream_t stream);
 size_t sel_state_bytes();
-int popc_tile_snps();
 constexpr int kSelectLaunches = 20;  // init + 8 x (histogram, pick) + apply + compact + count
+// The selects of every request of an engine step, decided on the device
+// (gridDim.y = request; 20 launches whatever the number of requests).
+cudaError_t run_select_batch(SelJob *jobs, int njobs, int num_sms, cudaStream_t stream);
+
+// Counting variants: a counting kernel with its tile shape and plane words per
+// pipeline stage.  Every variant gives the same results bit for bit; the
+// autotuner times them per plane-set shape (replacing the reference's
+// --block-sizes / --max-grid-area, gEpiCount.cpp:135-141, misc1.cu:35-89).
+// Ids are 1-based and stable (gepi_count_variant_name).
+struct CountVariant {
+    int id;
+    int method;  // GEPI_METHOD_POPC or GEPI_METHOD_TENSOR
+    int ta, tb;  // SNPs per tile, A x B
+    int words;   // plane words (32 samples each) per pipeline stage
+    const char *name;
+};
+constexpr int kNumVariants = 4;
+constexpr int kVariantPopcDefault = 1;  // GEPI_METHOD_POPC
+constexpr int kVariantTensor = 4;       // GEPI_METHOD_TENSOR
+const CountVariant *count_variant(int id);  // nullptr outside [1, kNumVariants]
+// One counting launch of variant v over tiles[0, ntiles).
+cudaError_t launch_count(const CountVariant &v, const gepi_planes *pl, const int2 *tiles,
+                         int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
+                         uint32_t *dump, int *err, cudaStream_t stream);
 
 // Candidates a scan lets accumulate before a device select raises its
 // threshold: 16 k (at least 64 Ki), at most half the buffer.  Raising the
@@ -107,8 +143,8 @@ gepi_status pl_check_mem(size_t bytes, const char *what);
 struct gepi_planes {
     uint64_t serial = 0;  // unique per plane set in the process (keys cached tile orders)
     int device = 0, num_sms = 0;
-    int auto_method = 0;  // AUTO's choice for this plane set (0 = not tuned yet)
-    float tune_ms[2] = {0.f, 0.f};  // autotuner timings: popcount, tensor core
+    int auto_variant = 0;  // AUTO's counting variant for this plane set (0 = not tuned yet)
+    float tune_ms[gepi::kNumVariants + 1] = {};  // autotuner timing of variant v (0: untimed)
     int n_snps = 0, S0 = 0, S1 = 0, W0 = 0, W1 = 0, Wp = 0;
     uint32_t *d_planes = nullptr;
     uint32_t *d_tc_blocks = nullptr;  // block-major copy for the tensor-core kernel (lazy)
@@ -136,7 +172,8 @@ namespace gepi {
 
 gepi_status pl_ensure_tables(gepi_planes *pl);
 gepi_status pl_ensure_tc_blocks(gepi_planes *pl);
-gepi_status pl_resolve_method(gepi_planes *pl, int m, int *out);
+// Counting variant of a request (method, optional variant id; AUTO tunes once per plane set).
+gepi_status pl_resolve_variant(gepi_planes *pl, int m, int variant, const CountVariant **out);
 // The tile list of a triangle scan: bands of about 320 A SNPs, and with `hot`
 // the tiles of the strongest marginal SNPs first (large lists only).
 gepi_status pl_scan_tiles(gepi_planes *pl, int a0, int a1, int b0, int b1, int TA, int TB, bool hot,

@@ -55,14 +55,17 @@ namespace gepi {
 cudaError_t launch_decode_rows(const uint64_t *bits, const uint64_t *valid, int nw, int n_snps,
                                const int32_t *perm, int Wp, uint32_t *planes,
                                cudaStream_t stream, int num_sms);
-cudaError_t launch_popc_tiles(const uint32_t *planes, int Wp, int W0, const int2 *tiles,
-                              int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
-                              uint32_t *dump, cudaStream_t stream);
+cudaError_t launch_popc_tiles(int ta, int kc, const uint32_t *planes, int Wp, int W0,
+                              const int2 *tiles, int ntiles, int a0, int a1, int b0, int b1,
+                              const ScanCtx &ctx, uint32_t *dump, cudaStream_t stream);
 cudaError_t run_select_compact(Cand *in, Cand *out, ScanState *st, void *sel, uint32_t cap,
                                uint32_t k, int n_override, uint32_t n_compact, int objective,
                                float lp_margin, int num_sms, cudaStream_t stream);
 size_t sel_state_bytes();
-int popc_tile_snps();
+// The popcount variant this entry point runs: 32 x 32 SNP tiles, 32 plane
+// words per stage (the library's default popcount variant).
+constexpr int kNoAllocTile = 32;
+constexpr int kNoAllocStageWords = 32;
 
 constexpr size_t kNoAllocScratchBytes = 32ull << 20;
 constexpr uint32_t kNoAllocCap = 65536;
@@ -270,7 +273,7 @@ extern "C" gepi_status gepi_process_gpu_1_noalloc(const uint64_t *bits, const ui
     const int W1 = ((S1 + kClassPadSamples - 1) / kClassPadSamples) * (kClassPadSamples / 32);
     const int Wp = W0 + W1;
     const int nmax = S0 + S1;
-    const int T = popc_tile_snps();
+    const int T = kNoAllocTile;
     const int nt = (n_snps + T - 1) / T;
     const long long ntiles = (long long)nt * (nt + 1) / 2;
 
@@ -374,7 +377,8 @@ extern "C" gepi_status gepi_process_gpu_1_noalloc(const uint64_t *bits, const ui
     while (t < (size_t)ntiles) {
         const size_t nbt = std::min(batch, (size_t)ntiles - t);
         ctx.cand = d_cand[cur];
-        GEPI_CUDA(launch_popc_tiles(d_planes, Wp, W0, d_tiles + t, (int)nbt, 0, n_snps, 0, n_snps,
+        GEPI_CUDA(launch_popc_tiles(kNoAllocTile, kNoAllocStageWords, d_planes, Wp, W0, d_tiles + t,
+                                    (int)nbt, 0, n_snps, 0, n_snps,
                                     ctx, nullptr, stream));
         GEPI_CUDA(cudaMemcpy(&st, d_state, sizeof st, cudaMemcpyDeviceToHost));
         if (st.overflow) {

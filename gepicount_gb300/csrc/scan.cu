@@ -355,16 +355,13 @@ gepi_status ensure_events(gepi_planes *pl, size_t n) {
     return GEPI_OK;
 }
 
-// GEPI_METHOD_AUTO picks the counting form.
-// Device time of one counting-kernel launch over the triangle of SNPs [0, n)
-// with a threshold nothing passes (the steady state of a long scan, where the
-// fused bounds reject almost every test).  The first launch warms up.
-gepi_status time_count_kernel(gepi_planes *pl, bool tc, int n, float *ms) {
-    if (tc) GEPI_TRY(ensure_tc_blocks(pl));
+// Device time of one launch of counting variant `v` over the triangle of SNPs
+// [0, n) with a threshold nothing passes (the steady state of a long scan,
+// where the fused bounds reject almost every test).  The first launch warms up.
+gepi_status time_count_kernel(gepi_planes *pl, const CountVariant &v, int n, float *ms) {
+    if (v.method == GEPI_METHOD_TENSOR) GEPI_TRY(ensure_tc_blocks(pl));
     std::vector<int2> tiles;
-    const int T0 = tc ? tc_tile_a_snps() : popc_tile_snps();
-    const int T1 = tc ? tc_tile_b_snps() : popc_tile_snps();
-    build_tiles(0, n, 0, n, T0, T1, true, tile_band(T0), tiles);
+    build_tiles(0, n, 0, n, v.ta, v.tb, true, tile_band(v.ta), tiles);
     GEPI_TRY(upload_tiles(pl, tiles));
     GEPI_TRY(ensure_events(pl, 4));
     ScanState st{};
@@ -387,13 +384,8 @@ gepi_status time_count_kernel(gepi_planes *pl, bool tc, int n, float *ms) {
     ctx.cand = pl->d_cand[0];
     for (int rep = 0; rep < 2; ++rep) {
         GEPI_CUDA(cudaEventRecord(pl->ev[2], pl->stream));
-        if (tc)
-            GEPI_CUDA(launch_tc_tiles(pl->d_tc_blocks, pl->n_snps, pl->Wp, pl->W0, pl->d_tiles,
-                                      (int)tiles.size(), 0, n, 0, n, ctx, nullptr,
-                                      &pl->d_state->kerr, pl->num_sms, pl->stream));
-        else
-            GEPI_CUDA(launch_popc_tiles(pl->d_planes, pl->Wp, pl->W0, pl->d_tiles, (int)tiles.size(),
-                                        0, n, 0, n, ctx, nullptr, pl->stream));
+        GEPI_CUDA(launch_count(v, pl, pl->d_tiles, (int)tiles.size(), 0, n, 0, n, ctx, nullptr,
+                               &pl->d_state->kerr, pl->stream));
         GEPI_CUDA(cudaEventRecord(pl->ev[3], pl->stream));
     }
     GEPI_CUDA(cudaMemcpyAsync(pl->h_state, pl->d_state, sizeof(ScanState), cudaMemcpyDeviceToHost,
@@ -406,58 +398,75 @@ gepi_status time_count_kernel(gepi_planes *pl, bool tc, int n, float *ms) {
     return GEPI_OK;
 }
 
-// Counting method for a request.  AUTO is tuned once per plane set: both
-// counting kernels are timed on the leading triangle of up to 4,096 SNPs at
-// the set's full sample width (sample count is what moves the crossover: the
-// tensor-core kernel's fixed per-tile epilogue is amortised over the samples),
-// and the faster one is kept.  Plane sets of fewer than 256 SNPs use the
-// popcount kernel without timing.
-gepi_status resolve_method(gepi_planes *pl, int m, int *out) {
+// Counting variant of a request: `variant` > 0 names one (gepi_params.variant),
+// else GEPI_METHOD_POPC and _TENSOR take their default variant and AUTO the
+// tuned one.  AUTO is tuned once per plane set: every variant is timed on the
+// leading triangle of up to 4,096 SNPs at the set's full sample width (sample
+// count moves the crossover: the tensor-core kernel's fixed per-tile epilogue
+// is amortised over the samples; tile height trades B-tile reuse against the
+// ragged edge of small triangles) and the fastest is kept.  Plane sets of
+// fewer than 256 SNPs use the default popcount variant without timing.
+gepi_status resolve_variant(gepi_planes *pl, int m, int variant, const CountVariant **out) {
     // the tensor-core kernel hands counts to its scoring warps as 16-bit values
     const bool tc_ok = pl->S0 <= tc_max_class() && pl->S1 <= tc_max_class();
-    if (m == GEPI_METHOD_TENSOR && !tc_ok)
+    auto tc_refused = [&]() {
         return set_error(GEPI_ERR_ARG, "the tensor-core counting kernel takes at most " +
                                            std::to_string(tc_max_class()) +
                                            " samples per class; use the popcount method");
-    if (m == GEPI_METHOD_POPC || m == GEPI_METHOD_TENSOR) {
-        *out = m;
+    };
+    if (variant != 0) {
+        const CountVariant *v = count_variant(variant);
+        if (!v) return set_error(GEPI_ERR_ARG, "unknown counting variant " + std::to_string(variant));
+        if (v->method == GEPI_METHOD_TENSOR && !tc_ok) return tc_refused();
+        *out = v;
         return GEPI_OK;
     }
-    if (!pl->auto_method) {
-        if (pl->n_snps < 256 || !tc_ok) {
-            pl->auto_method = GEPI_METHOD_POPC;
+    if (m == GEPI_METHOD_TENSOR && !tc_ok) return tc_refused();
+    if (m == GEPI_METHOD_POPC || m == GEPI_METHOD_TENSOR) {
+        *out = count_variant(m == GEPI_METHOD_POPC ? kVariantPopcDefault : kVariantTensor);
+        return GEPI_OK;
+    }
+    if (!pl->auto_variant) {
+        if (pl->n_snps < 256) {
+            pl->auto_variant = kVariantPopcDefault;
         } else {
             // The timing depends only on the shape (class widths, tuning
             // triangle) and the device, so it is kept for the process: later
             // plane sets of the same shape reuse the first one's choice.
             static std::mutex mu;
-            static std::map<std::array<int, 4>, std::array<float, 3>> tuned;
+            static std::map<std::array<int, 4>, std::array<float, kNumVariants + 1>> tuned;
             const int n = std::min(pl->n_snps, 4096);
             const std::array<int, 4> key{pl->device, pl->W0, pl->Wp, n};
             {
                 std::lock_guard<std::mutex> lk(mu);
                 auto it = tuned.find(key);
                 if (it != tuned.end()) {
-                    pl->auto_method = (int)it->second[0];
-                    pl->tune_ms[0] = it->second[1];
-                    pl->tune_ms[1] = it->second[2];
+                    pl->auto_variant = (int)it->second[0];
+                    for (int v = 1; v <= kNumVariants; ++v) pl->tune_ms[v] = it->second[v];
                 }
             }
-            if (!pl->auto_method) {
+            if (!pl->auto_variant) {
                 GEPI_TRY(ensure_tables(pl));
                 GEPI_TRY(ensure_scan_buffers(pl, 1));
-                float t_popc = 0.f, t_tc = 0.f;
-                GEPI_TRY(time_count_kernel(pl, false, n, &t_popc));
-                GEPI_TRY(time_count_kernel(pl, true, n, &t_tc));
-                pl->auto_method = t_tc < t_popc ? GEPI_METHOD_TENSOR : GEPI_METHOD_POPC;
-                pl->tune_ms[0] = t_popc;
-                pl->tune_ms[1] = t_tc;
+                std::array<float, kNumVariants + 1> row{};
+                int best = 0;
+                for (int v = 1; v <= kNumVariants; ++v) {
+                    const CountVariant &cv = *count_variant(v);
+                    if (cv.method == GEPI_METHOD_TENSOR && !tc_ok) continue;
+                    float ms = 0.f;
+                    GEPI_TRY(time_count_kernel(pl, cv, n, &ms));
+                    row[v] = ms;
+                    if (!best || ms < row[best]) best = v;
+                }
+                row[0] = (float)best;
+                pl->auto_variant = best;
+                for (int v = 1; v <= kNumVariants; ++v) pl->tune_ms[v] = row[v];
                 std::lock_guard<std::mutex> lk(mu);
-                tuned[key] = {(float)pl->auto_method, t_popc, t_tc};
+                tuned[key] = row;
             }
         }
     }
-    *out = pl->auto_method;
+    *out = count_variant(pl->auto_variant);
     return GEPI_OK;
 }
 
@@ -553,12 +562,10 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
     std::memset(tops, 0, sizeof(gepi_result) * (size_t)k);
     pl->last_values.clear();
 
-    int method = 0;
-    GEPI_TRY(resolve_method(pl, par->method, &method));
-    const bool tc = method == GEPI_METHOD_TENSOR;
-    if (tc) GEPI_TRY(ensure_tc_blocks(pl));
-    const int TA = tc ? tc_tile_a_snps() : popc_tile_snps();
-    const int TB = tc ? tc_tile_b_snps() : popc_tile_snps();
+    const CountVariant *cv = nullptr;
+    GEPI_TRY(resolve_variant(pl, par->method, par->variant, &cv));
+    if (cv->method == GEPI_METHOD_TENSOR) GEPI_TRY(ensure_tc_blocks(pl));
+    const int TA = cv->ta, TB = cv->tb;
     std::vector<int2> tiles;
     // progress snapshots cover band prefixes, so they keep the band order
     GEPI_TRY(pl_scan_tiles(pl, a0, a0 + na, b0, b0 + nb, TA, TB, !(prog && prog->fn), tiles));
@@ -566,8 +573,9 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
     GEPI_TRY(ensure_events(pl, 4));
     gepi_scan_stats &S = pl->stats;
     S = gepi_scan_stats{};
-    S.method = method;
+    S.method = cv->method;
     S.tile_snps = TA;
+    S.variant = cv->id;
     S.tiles = tiles.size();
     {
         // pairs (s, t), t < s, s in A, t in B; and SNPs in both ranges
@@ -621,13 +629,8 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
         if (prog && prog->with_tops && t < prog->next_end) nbt = std::min(nbt, prog->next_end - t);
         ctx.cand = pl->d_cand[cur];
         GEPI_CUDA(cudaEventRecord(pl->ev[2], pl->stream));
-        if (tc)
-            GEPI_CUDA(launch_tc_tiles(pl->d_tc_blocks, pl->n_snps, pl->Wp, pl->W0,
-                                      pl->d_tiles + t, (int)nbt, a0, a0 + na, b0, b0 + nb, ctx,
-                                      nullptr, &pl->d_state->kerr, pl->num_sms, pl->stream));
-        else
-            GEPI_CUDA(launch_popc_tiles(pl->d_planes, pl->Wp, pl->W0, pl->d_tiles + t, (int)nbt,
-                                        a0, a0 + na, b0, b0 + nb, ctx, nullptr, pl->stream));
+        GEPI_CUDA(launch_count(*cv, pl, pl->d_tiles + t, (int)nbt, a0, a0 + na, b0, b0 + nb, ctx,
+                               nullptr, &pl->d_state->kerr, pl->stream));
         GEPI_CUDA(cudaEventRecord(pl->ev[3], pl->stream));
         GEPI_CUDA(cudaMemcpyAsync(pl->h_state, pl->d_state, sizeof(ScanState),
                                   cudaMemcpyDeviceToHost, pl->stream));
@@ -766,7 +769,31 @@ cudaError_t pool_alloc(int device, void **ptr, size_t bytes, cudaStream_t s) {
 gepi_status pl_check_mem(size_t bytes, const char *what) { return check_mem(bytes, what); }
 gepi_status pl_ensure_tables(gepi_planes *pl) { return ensure_tables(pl); }
 gepi_status pl_ensure_tc_blocks(gepi_planes *pl) { return ensure_tc_blocks(pl); }
-gepi_status pl_resolve_method(gepi_planes *pl, int m, int *out) { return resolve_method(pl, m, out); }
+gepi_status pl_resolve_variant(gepi_planes *pl, int m, int variant, const CountVariant **out) {
+    return resolve_variant(pl, m, variant, out);
+}
+
+// The counting variants (ids 1..kNumVariants, stable).
+static const CountVariant kVariants[kNumVariants] = {
+    {1, GEPI_METHOD_POPC, 32, 32, 32, "popc_32x32_w32"},
+    {2, GEPI_METHOD_POPC, 32, 32, 16, "popc_32x32_w16"},
+    {3, GEPI_METHOD_POPC, 64, 32, 32, "popc_64x32_w32"},
+    {4, GEPI_METHOD_TENSOR, 80, 64, 12, "tensor_80x64_w12"},
+};
+
+const CountVariant *count_variant(int id) {
+    return id >= 1 && id <= kNumVariants ? &kVariants[id - 1] : nullptr;
+}
+
+cudaError_t launch_count(const CountVariant &v, const gepi_planes *pl, const int2 *tiles,
+                         int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
+                         uint32_t *dump, int *err, cudaStream_t stream) {
+    if (v.method == GEPI_METHOD_TENSOR)
+        return launch_tc_tiles(pl->d_tc_blocks, pl->n_snps, pl->Wp, pl->W0, tiles, ntiles, a0, a1,
+                               b0, b1, ctx, dump, err, pl->num_sms, stream);
+    return launch_popc_tiles(v.ta, v.words, pl->d_planes, pl->Wp, pl->W0, tiles, ntiles, a0, a1, b0,
+                             b1, ctx, dump, stream);
+}
 gepi_status pl_scan_tiles(gepi_planes *pl, int a0, int a1, int b0, int b1, int TA, int TB, bool hot,
                           std::vector<int2> &out) {
     std::vector<int> hot_a, hot_b;
@@ -1045,17 +1072,20 @@ gepi_status gepi_pair_counts(gepi_planes *pl, int method, int a0, int na, int b0
     if (!pl || !out || na <= 0 || nb <= 0 || a0 < 0 || b0 < 0 || a0 + na > pl->n_snps ||
         b0 + nb > pl->n_snps)
         return set_error(GEPI_ERR_ARG, "gepi_pair_counts: bad argument");
+    int variant = 0;
+    if (method >= GEPI_VARIANT(1)) {
+        variant = method - GEPI_VARIANT(0);
+        method = GEPI_METHOD_AUTO;
+    }
     if (method < GEPI_METHOD_AUTO || method > GEPI_METHOD_TENSOR)
         return set_error(GEPI_ERR_ARG, "gepi_pair_counts: unknown method");
     DeviceGuard g(pl->device);
     if (!g.ok) return set_error(GEPI_ERR_CUDA, "cudaSetDevice failed");
-    int resolved = 0;
-    GEPI_TRY(resolve_method(pl, method, &resolved));
-    const bool tc = resolved == GEPI_METHOD_TENSOR;
-    if (tc) GEPI_TRY(ensure_tc_blocks(pl));
+    const CountVariant *cv = nullptr;
+    GEPI_TRY(resolve_variant(pl, method, variant, &cv));
+    if (cv->method == GEPI_METHOD_TENSOR) GEPI_TRY(ensure_tc_blocks(pl));
     std::vector<int2> tiles;
-    build_tiles(a0, a0 + na, b0, b0 + nb, tc ? tc_tile_a_snps() : popc_tile_snps(),
-                tc ? tc_tile_b_snps() : popc_tile_snps(), false, 8, tiles);
+    build_tiles(a0, a0 + na, b0, b0 + nb, cv->ta, cv->tb, false, 8, tiles);
     GEPI_TRY(upload_tiles(pl, tiles));
     const size_t bytes = (size_t)na * nb * 18 * 4;
     GEPI_TRY(check_mem(bytes, "pair counts"));
@@ -1067,11 +1097,8 @@ gepi_status gepi_pair_counts(gepi_planes *pl, int method, int a0, int na, int b0
     int herr = 0;
     cudaError_t e = cudaMemsetAsync(d_err, 0, sizeof(int), pl->stream);
     if (e == cudaSuccess)
-        e = tc ? launch_tc_tiles(pl->d_tc_blocks, pl->n_snps, pl->Wp, pl->W0, pl->d_tiles,
-                                 (int)tiles.size(), a0, a0 + na, b0, b0 + nb, ctx, d_out, d_err,
-                                 pl->num_sms, pl->stream)
-               : launch_popc_tiles(pl->d_planes, pl->Wp, pl->W0, pl->d_tiles, (int)tiles.size(),
-                                   a0, a0 + na, b0, b0 + nb, ctx, d_out, pl->stream);
+        e = launch_count(*cv, pl, pl->d_tiles, (int)tiles.size(), a0, a0 + na, b0, b0 + nb, ctx, d_out,
+                         d_err, pl->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, bytes, cudaMemcpyDeviceToHost, pl->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, pl->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(pl->stream);
@@ -1090,17 +1117,60 @@ gepi_status gepi_planes_autotune(gepi_planes *pl, int32_t *method, float *popc_m
     if (!pl) return set_error(GEPI_ERR_ARG, "gepi_planes_autotune: null planes");
     DeviceGuard g(pl->device);
     if (!g.ok) return set_error(GEPI_ERR_CUDA, "cudaSetDevice failed");
-    int m = 0;
-    GEPI_TRY(resolve_method(pl, GEPI_METHOD_AUTO, &m));
-    if (method) *method = m;
-    if (popc_ms) *popc_ms = pl->tune_ms[0];
-    if (tensor_ms) *tensor_ms = pl->tune_ms[1];
+    const CountVariant *cv = nullptr;
+    GEPI_TRY(resolve_variant(pl, GEPI_METHOD_AUTO, 0, &cv));
+    if (method) *method = cv->method;
+    // the fastest timed variant of each kernel (0: not timed)
+    float best[3] = {0.f, 0.f, 0.f};
+    for (int v = 1; v <= kNumVariants; ++v) {
+        const float ms = pl->tune_ms[v];
+        const int m = count_variant(v)->method;
+        if (ms > 0.f && (best[m] == 0.f || ms < best[m])) best[m] = ms;
+    }
+    if (popc_ms) *popc_ms = best[GEPI_METHOD_POPC];
+    if (tensor_ms) *tensor_ms = best[GEPI_METHOD_TENSOR];
+    return GEPI_OK;
+}
+
+gepi_status gepi_planes_autotune_variants(gepi_planes *pl, gepi_tune_report *out) {
+    clear_error();
+    if (!pl || !out) return set_error(GEPI_ERR_ARG, "gepi_planes_autotune_variants: bad argument");
+    DeviceGuard g(pl->device);
+    if (!g.ok) return set_error(GEPI_ERR_CUDA, "cudaSetDevice failed");
+    const CountVariant *cv = nullptr;
+    GEPI_TRY(resolve_variant(pl, GEPI_METHOD_AUTO, 0, &cv));
+    std::memset(out, 0, sizeof *out);
+    out->variant = cv->id;
+    out->n_variants = kNumVariants;
+    for (int v = 1; v <= kNumVariants; ++v) out->ms[v - 1] = pl->tune_ms[v];
+    return GEPI_OK;
+}
+
+const char *gepi_count_variant_name(int32_t variant) {
+    const CountVariant *cv = count_variant(variant);
+    return cv ? cv->name : "";
+}
+
+gepi_status gepi_count_variant_shape(int32_t variant, int32_t *method, int32_t *tile_a,
+                                     int32_t *tile_b, int32_t *stage_words) {
+    const CountVariant *cv = count_variant(variant);
+    if (!cv) return set_error(GEPI_ERR_ARG, "unknown counting variant");
+    if (method) *method = cv->method;
+    if (tile_a) *tile_a = cv->ta;
+    if (tile_b) *tile_b = cv->tb;
+    if (stage_words) *stage_words = cv->words;
     return GEPI_OK;
 }
 
 gepi_status gepi_tensor_peak_tflops(int device, double *tflops) {
+    return gepi_tensor_peak_probe(device, GEPI_PEAK_MXF4, tflops);
+}
+
+gepi_status gepi_tensor_peak_probe(int32_t device, int32_t kind, double *tflops) {
     clear_error();
-    if (!tflops) return set_error(GEPI_ERR_ARG, "gepi_tensor_peak_tflops: null output");
+    if (!tflops) return set_error(GEPI_ERR_ARG, "gepi_tensor_peak_probe: null output");
+    if (kind < GEPI_PEAK_MXF4 || kind > GEPI_PEAK_MXF4NVF4_4X)
+        return set_error(GEPI_ERR_ARG, "gepi_tensor_peak_probe: unknown kind");
     DeviceGuard g(device);
     if (!g.ok) return set_error(GEPI_ERR_CUDA, "cudaSetDevice failed");
     int sms = 0;
@@ -1108,7 +1178,7 @@ gepi_status gepi_tensor_peak_tflops(int device, double *tflops) {
     int *d_err = nullptr;
     GEPI_CUDA(cudaMalloc(&d_err, sizeof(int)));
     cudaError_t e = cudaMemset(d_err, 0, sizeof(int));
-    if (e == cudaSuccess) e = tc_measure_peak(sms, 3, tflops, d_err, 0);
+    if (e == cudaSuccess) e = tc_measure_peak(sms, 3, kind, tflops, d_err, 0);
     int herr = 0;
     if (e == cudaSuccess) e = cudaMemcpy(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost);
     cudaFree(d_err);

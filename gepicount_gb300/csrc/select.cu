@@ -10,6 +10,7 @@
 // end, and the host sorts the survivors by (key desc, rA, rB, fun).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 
@@ -22,7 +23,7 @@ struct SelState {
     uint32_t krem;     // rank still to locate inside the current bucket (0 = no select)
     uint32_t n;        // entries examined
     uint32_t ncompact; // entries kept by compaction
-    uint32_t pad;
+    uint32_t pad;      // batched selects: the mode taken (0 none, 1 select, 2 overflow retry)
     uint32_t hist[256];
 };
 
@@ -58,7 +59,7 @@ __global__ void sel_hist_kernel(const Cand *__restrict__ cand, SelState *sel, in
 
 // One warp: walk buckets from the largest digit down to find the one holding
 // the krem-th largest key, fix that digit, clear the histogram.
-__global__ void sel_pick_kernel(SelState *sel, int shift) {
+__device__ __forceinline__ void sel_pick(SelState *sel, int shift) {
     if (sel->krem == 0) return;
     const int lane = threadIdx.x;
     // lane L owns buckets 255-8L .. 248-8L (descending)
@@ -99,11 +100,13 @@ __global__ void sel_pick_kernel(SelState *sel, int shift) {
     for (int i = lane; i < 256; i += 32) sel->hist[i] = 0u;
 }
 
+__global__ void sel_pick_kernel(SelState *sel, int shift) { sel_pick(sel, shift); }
+
 // Raise tau_key to the selected key and derive the float bounds.
 //   entropy: theta = (2^I - 1) * (1 - 2^-10), I the selected mutual information
 //   Fisher : lp_thr = ln(p) + margin, p = 10^-v for the selected v = -log10 p
-__global__ void sel_apply_kernel(ScanState *st, const SelState *sel, int objective,
-                                 float lp_margin) {
+__device__ __forceinline__ void sel_apply(ScanState *st, const SelState *sel, int objective,
+                                          float lp_margin) {
     if (sel->krem == 0) return;
     unsigned long long key = sel->prefix;
     if (key <= st->tau_key) return;
@@ -120,8 +123,14 @@ __global__ void sel_apply_kernel(ScanState *st, const SelState *sel, int objecti
     }
 }
 
-__global__ void compact_kernel(const Cand *__restrict__ in, Cand *__restrict__ out,
-                               const ScanState *st, SelState *sel, uint32_t n_limit) {
+__global__ void sel_apply_kernel(ScanState *st, const SelState *sel, int objective,
+                                 float lp_margin) {
+    sel_apply(st, sel, objective, lp_margin);
+}
+
+__device__ __forceinline__ void compact_range(const Cand *__restrict__ in, Cand *__restrict__ out,
+                                              const ScanState *st, SelState *sel,
+                                              uint32_t n_limit) {
     const unsigned long long tau = st->tau_key;
     uint32_t n = sel->n;
     if (n > n_limit) n = n_limit;
@@ -140,6 +149,11 @@ __global__ void compact_kernel(const Cand *__restrict__ in, Cand *__restrict__ o
         off = __shfl_sync(0xffffffffu, off, 0);
         if (keep) out[off + __popc(ball & ((1u << lane) - 1u))] = c;
     }
+}
+
+__global__ void compact_kernel(const Cand *__restrict__ in, Cand *__restrict__ out,
+                               const ScanState *st, SelState *sel, uint32_t n_limit) {
+    compact_range(in, out, st, sel, n_limit);
 }
 
 __global__ void set_count_kernel(ScanState *st, const SelState *sel) {
@@ -167,5 +181,104 @@ cudaError_t run_select_compact(Cand *in, Cand *out, ScanState *st, void *sel_raw
 }
 
 size_t sel_state_bytes() { return sizeof(SelState); }
+
+// ---- batched selects: one chain of launches for every request of an engine
+// step (gridDim.y = request), replayed from a CUDA graph.  Each request's
+// select is decided on the device from its scan state, exactly as the direct
+// scan decides it on the host (scan.cu):
+//   overflow in this batch             -> select over the first `cap` entries,
+//                                         compaction of the `count_before`
+//                                         entries captured before the batch
+//                                         (the batch is retried in halves)
+//   last batch and count > k, or
+//   not last and count > trigger       -> select over all entries, compaction
+//   otherwise                          -> nothing
+// The mode taken is left in ScanState::sel_mode for the host.
+
+// Slots without a request this step (active = 0) carry null state and
+// scratch pointers: every batched kernel returns before touching them.
+__global__ void bsel_init_kernel(SelJob *jobs) {
+    SelJob &j = jobs[blockIdx.y];
+    if (!j.active) return;
+    SelState *sel = j.sel;
+    if (threadIdx.x == 0) {
+        ScanState *st = j.st;
+        const uint32_t count = st->count;
+        int mode = 0;
+        if (st->overflow) mode = 2;
+        else if (j.final_batch ? count > j.k : count > j.trigger) mode = 1;
+        uint32_t n = count > j.cap ? j.cap : count;
+        sel->n = mode ? n : 0u;
+        sel->krem = (mode && n >= j.k && j.k > 0) ? j.k : 0u;
+        sel->prefix = 0ull;
+        sel->mask = 0ull;
+        sel->ncompact = 0u;
+        sel->pad = (uint32_t)mode;
+        st->sel_mode = (uint32_t)mode;
+        st->count_batch = count;
+    }
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) sel->hist[i] = 0u;
+}
+
+__global__ void bsel_hist_kernel(const SelJob *jobs, int shift) {
+    const SelJob &j = jobs[blockIdx.y];
+    if (!j.active) return;
+    SelState *sel = j.sel;
+    __shared__ uint32_t h[256];
+    if (sel->krem == 0) return;
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0u;
+    __syncthreads();
+    const uint32_t n = sel->n;
+    const unsigned long long prefix = sel->prefix, mask = sel->mask;
+    const Cand *__restrict__ cand = j.in;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        unsigned long long key = cand[i].key;
+        if ((key & mask) == prefix) atomicAdd(&h[(key >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 256; i += blockDim.x)
+        if (h[i]) atomicAdd(&sel->hist[i], h[i]);
+}
+
+__global__ void bsel_pick_kernel(const SelJob *jobs, int shift) {
+    const SelJob &j = jobs[blockIdx.y];
+    if (!j.active) return;
+    sel_pick(j.sel, shift);
+}
+
+__global__ void bsel_apply_kernel(const SelJob *jobs) {
+    const SelJob &j = jobs[blockIdx.y];
+    if (!j.active) return;
+    sel_apply(j.st, j.sel, j.objective, j.lp_margin);
+}
+
+__global__ void bcompact_kernel(const SelJob *jobs) {
+    const SelJob &j = jobs[blockIdx.y];
+    if (!j.active) return;
+    const int mode = (int)j.sel->pad;
+    if (!mode) return;
+    compact_range(j.in, j.out, j.st, j.sel, mode == 2 ? j.count_before : 0xFFFFFFFFu);
+}
+
+__global__ void bset_count_kernel(const SelJob *jobs) {
+    const SelJob &j = jobs[blockIdx.y];
+    if (!j.active || !j.sel->pad) return;
+    j.st->count = j.sel->ncompact;
+    j.st->overflow = 0u;
+}
+
+cudaError_t run_select_batch(SelJob *jobs, int njobs, int num_sms, cudaStream_t stream) {
+    if (njobs <= 0) return cudaSuccess;
+    const int gx = std::max(1, (num_sms * 4 + njobs - 1) / njobs);
+    bsel_init_kernel<<<dim3(1, njobs), 256, 0, stream>>>(jobs);
+    for (int shift = 56; shift >= 0; shift -= 8) {
+        bsel_hist_kernel<<<dim3(gx, njobs), 256, 0, stream>>>(jobs, shift);
+        bsel_pick_kernel<<<dim3(1, njobs), 32, 0, stream>>>(jobs, shift);
+    }
+    bsel_apply_kernel<<<dim3(1, njobs), 1, 0, stream>>>(jobs);
+    bcompact_kernel<<<dim3(gx, njobs), 256, 0, stream>>>(jobs);
+    bset_count_kernel<<<dim3(1, njobs), 1, 0, stream>>>(jobs);
+    return cudaGetLastError();
+}
 
 }  // namespace gepi

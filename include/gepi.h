@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define GEPI_ABI_VERSION 1
+#define GEPI_ABI_VERSION 2
 
 typedef enum gepi_status {
     GEPI_OK = 0,
@@ -53,6 +53,17 @@ enum { GEPI_AND = 0, GEPI_NAND = 1, GEPI_ANDN = 2, GEPI_NANDN = 3, GEPI_XOR = 4 
 enum { GEPI_ENTROPY = 0, GEPI_FISHER = 1 };
 /* Counting method. */
 enum { GEPI_METHOD_AUTO = 0, GEPI_METHOD_POPC = 1, GEPI_METHOD_TENSOR = 2 };
+/* Counting variants: a counting kernel with its tile shape and plane words per
+ * pipeline stage, ids 1..4 (gepi_count_variant_name / _shape):
+ *   1 popc_32x32_w32   popcount, 32 x 32 SNP tiles, 32 words per stage (GEPI_METHOD_POPC)
+ *   2 popc_32x32_w16   popcount, 32 x 32 SNP tiles, 16 words per stage
+ *   3 popc_64x32_w32   popcount, 64 x 32 SNP tiles, 32 words per stage
+ *   4 tensor_80x64_w12 tensor cores, 80 x 64 SNP tiles on a CTA pair, 12 words
+ *                      (384 samples) per stage (GEPI_METHOD_TENSOR)
+ * Every variant returns the same results bit for bit.  GEPI_VARIANT(v) passed
+ * as the `method` of gepi_pair_counts selects variant v. */
+#define GEPI_NUM_VARIANTS 4
+#define GEPI_VARIANT(v) (16 + (v))
 
 /* One ranked interaction.  Byte layout identical to InteractionResult
  * (inc/gEpiCount.h:75-82, sizeof 48, int4 aligned at offset 16):
@@ -81,7 +92,8 @@ typedef struct gepi_params {
     int32_t objective;      /* -f  : GEPI_ENTROPY / GEPI_FISHER                     */
     int32_t method;         /* GEPI_METHOD_*                                        */
     int32_t verbose;        /* 0 silent, 1 progress lines on stderr                 */
-    int32_t reserved[7];
+    int32_t variant;        /* 0: by `method`; 1..GEPI_NUM_VARIANTS: that variant   */
+    int32_t reserved[6];
 } gepi_params;
 
 /* Opaque device-resident genotype bit-planes (one cohort). */
@@ -225,7 +237,9 @@ typedef struct gepi_scan_stats {
     uint64_t tiles;           /* SNP tile pairs processed                               */
     uint64_t candidates;      /* candidates left for the final host sort                */
     int32_t method;           /* GEPI_METHOD_POPC or GEPI_METHOD_TENSOR actually used   */
-    int32_t tile_snps;        /* A SNPs per tile (80 tensor core, 32 popcount)          */
+    int32_t tile_snps;        /* A SNPs per tile of the variant used                    */
+    int32_t variant;          /* counting variant used (1..GEPI_NUM_VARIANTS)           */
+    int32_t reserved;
 } gepi_scan_stats;
 gepi_status gepi_last_scan_stats(const gepi_planes *pl, gepi_scan_stats *out);
 
@@ -250,12 +264,37 @@ gepi_status gepi_last_scan_values(const gepi_planes *pl, double *out, int32_t k)
 gepi_status gepi_planes_autotune(gepi_planes *pl, int32_t *method, float *popc_ms,
                                  float *tensor_ms);
 
+/* The autotuner's full report: GEPI_METHOD_AUTO times every counting variant
+ * (tile shape, words per stage, popcount or tensor cores) on the tuning
+ * triangle and uses the fastest; ms[v-1] is variant v's time (0: not timed --
+ * sets under 256 SNPs, or the tensor-core variant above its class-size limit).
+ * gepi_planes_autotune reports the fastest variant of each kernel. */
+typedef struct gepi_tune_report {
+    int32_t variant;     /* the variant AUTO uses on this plane set */
+    int32_t n_variants;  /* GEPI_NUM_VARIANTS                        */
+    float ms[8];
+} gepi_tune_report;
+gepi_status gepi_planes_autotune_variants(gepi_planes *pl, gepi_tune_report *out);
+/* Name ("" if unknown) and shape of counting variant v. */
+const char *gepi_count_variant_name(int32_t variant);
+gepi_status gepi_count_variant_shape(int32_t variant, int32_t *method, int32_t *tile_a,
+                                     int32_t *tile_b, int32_t *stage_words);
+
 /* Dense kind::mxf4 (packed FP4) tensor-core rate of `device` in TFLOP/s (2 per
  * multiply-accumulate), measured now: one CTA per SM issues back-to-back
  * M=128 x N=256 x K=64 MMAs; best of 3 timed launches.  It is the roofline
  * denominator of the tensor-core counting kernel.  No counterpart in the
  * reference. */
 gepi_status gepi_tensor_peak_tflops(int32_t device, double *tflops);
+
+/* The same measurement for each exact FP4 encoding of 0/1 operands (E2M1 A
+ * and B, unit block scales): GEPI_PEAK_MXF4 = kind::mxf4 scale_vec::2X UE8M0
+ * (the counting kernel's instruction; gepi_tensor_peak_tflops),
+ * GEPI_PEAK_MXF4NVF4_2X = kind::mxf4nvf4 scale_vec::2X UE8M0,
+ * GEPI_PEAK_MXF4NVF4_4X = kind::mxf4nvf4 scale_vec::4X UE4M3.  No counterpart
+ * in the reference. */
+enum { GEPI_PEAK_MXF4 = 0, GEPI_PEAK_MXF4NVF4_2X = 1, GEPI_PEAK_MXF4NVF4_4X = 2 };
+gepi_status gepi_tensor_peak_probe(int32_t device, int32_t kind, double *tflops);
 
 /* ---- many scans at once: cohort batches and the serving loop ---------------- */
 /* One scan request: SNP ranges [a0, a0+na) x [b0, b0+nb) of `planes` (na < 0 or
@@ -268,13 +307,16 @@ typedef struct gepi_scan_req {
     int32_t topmost;
     int32_t objective;
     int32_t method;
-    int32_t reserved;
+    int32_t variant;  /* 0: by `method`; else a counting variant id */
 } gepi_scan_req;
 
 /* Runs `n` requests together on the device of their plane sets (all on one
  * device; plane sets may differ, so a call scans many cohorts): every request
- * walks its tile list in its own adaptive batches on its own stream, and each
- * engine step launches the next batch of every unfinished request at once.
+ * walks its tile list in its own adaptive batches, and each engine step -- one
+ * CUDA graph replay -- runs the next batch of every unfinished request in ONE
+ * persistent counting launch per kernel group (CTAs claim the tiles of all
+ * requests from one work list with an atomic counter), then every request's
+ * threshold select in one chain of batched launches.
  * Replaces a loop of one reference process per cohort (the batch loop of
  * launch_process_gpu_1, src/kernels/kernel1.cu:387-483, run per cohort).
  * tops[i] receives reqs[i].topmost results; stats (may be NULL) receives one
@@ -284,14 +326,28 @@ typedef struct gepi_scan_req {
 gepi_status gepi_scan_batch(const gepi_scan_req *reqs, int32_t n, gepi_result *const *tops,
                             gepi_scan_stats *stats);
 
+/* Launch counts of the last gepi_scan_batch call on `device`: engine steps,
+ * counting launches (one per kernel group present in a step: the tensor-core
+ * kernel per objective, the popcount kernel per variant), select launches
+ * (20 per step, batched over every request) and step-graph replays.  No
+ * counterpart in the reference. */
+typedef struct gepi_batch_stats {
+    int64_t steps;
+    int64_t count_launches;
+    int64_t select_launches;
+    int64_t graph_launches;
+} gepi_batch_stats;
+gepi_status gepi_scan_batch_stats(int32_t device, gepi_batch_stats *out);
+
 /* Serving loop: a thread that admits submitted requests first-in first-out
  * while their device footprint (2 candidate buffers each: 256 MiB at topmost
  * <= 512 Ki) fits `hbm_budget_bytes` (0: 16 GiB; the oldest request is always
  * admitted when nothing runs), and runs all admitted requests together as
- * gepi_scan_batch does, admitting new ones between engine steps.  Batches are
- * capped at about 4 ms of device time (GEPI_QUANTUM_MS) and requests with little
- * work left run on a high-priority stream (GEPI_SERVE_POLICY=short, the default;
- * "oldest" gives the oldest request the high-priority stream).  Plane sets
+ * gepi_scan_batch does, admitting new ones between engine steps.  A step is
+ * capped at about 4 ms of device time (GEPI_QUANTUM_MS): requests with little
+ * work left get their batches -- and the first tiles of the step's work lists
+ * -- first (GEPI_SERVE_POLICY=short, the default; "oldest": the oldest
+ * requests first), every request at least one tile per step.  Plane sets
  * submitted to a server must not be used by other calls until their requests
  * are waited for.  No counterpart in the reference (it runs one scan per
  * process). */

@@ -45,9 +45,9 @@ def _requests(gepi, cohorts):
 def _direct(r):
     if r.na < 0:
         return r.planes.scan_range(0, r.planes.n_snps, 0, r.planes.n_snps, r.k,
-                                   objective=r.objective, method=r.method)
+                                   objective=r.objective, method=r.method, variant=r.variant)
     return r.planes.scan_range(r.a0, r.na, r.b0, r.nb, r.k, objective=r.objective,
-                               method=r.method)
+                               method=r.method, variant=r.variant)
 
 
 def _oracle(r, rows):
@@ -198,3 +198,53 @@ def test_sharded_scan_merges_to_whole_scan(gepi, tmp_path, shards, objective):
         probs = H.compare_ranked(items(merged), gk, items(whole), wk, k, rtol=1e-6)
         assert not probs, probs[:5]
     pl.close()
+
+
+def test_batch_runs_one_counting_launch_per_step(gepi):
+    """Many cohorts of one kernel group: every engine step is one graph replay
+    holding ONE persistent counting launch over all of them (tiles claimed from
+    one work list with an atomic counter) and one chain of 20 batched select
+    launches; every list equals its direct scan."""
+    pls = []
+    for i in range(12):
+        spec = gepi.SynthSpec(n_snps=300 + 53 * i, n_cases=200 + 97 * i, n_controls=300 + 31 * i,
+                              missing=0.02, n_planted=1, seed=700 + i)
+        bed, ph, _ = gepi.synth_bed(spec)
+        pls.append(gepi.Planes.from_bed(bed, spec.n_snps, ph))
+    reqs = [gepi.ScanRequest(p, 150, variant=4) for p in pls]
+    got, stats = gepi.scan_batch(reqs, with_stats=True)
+    bs = gepi.scan_batch_stats(0)
+    assert bs["steps"] >= max(s["batches"] for s in stats)
+    assert 1 <= bs["count_launches"] <= bs["steps"]
+    assert bs["select_launches"] == 20 * bs["steps"]
+    assert bs["graph_launches"] == bs["steps"]
+    for r, g, st in zip(reqs, got, stats):
+        assert g.tobytes() == _direct(r).tobytes()
+        assert st["variant"] == 4 and st["count_launches"] <= bs["count_launches"]
+    for p in pls:
+        p.close()
+
+
+def test_batch_mixes_variants_and_objectives(gepi):
+    """Requests of every counting variant and both objectives in one call: one
+    counting launch per (kernel group) and step, every list byte-identical to
+    its direct scan."""
+    pls = []
+    for i in range(4):
+        spec = gepi.SynthSpec(n_snps=150 + 40 * i, n_cases=150 + 60 * i, n_controls=170 + 20 * i,
+                              missing=0.03, n_planted=1, seed=800 + i)
+        bed, ph, _ = gepi.synth_bed(spec)
+        pls.append(gepi.Planes.from_bed(bed, spec.n_snps, ph))
+    reqs = []
+    for i, p in enumerate(pls):
+        for v in (1, 2, 3, 4):
+            reqs.append(gepi.ScanRequest(p, 120, variant=v, objective=(i + v) % 2))
+    reqs.append(gepi.ScanRequest(pls[0], 90, a0=20, na=60, b0=10, nb=70, variant=3))
+    got, stats = gepi.scan_batch(reqs, with_stats=True)
+    bs = gepi.scan_batch_stats(0)
+    assert bs["count_launches"] <= 5 * bs["steps"]
+    for r, g, st in zip(reqs, got, stats):
+        assert g.tobytes() == _direct(r).tobytes(), (r.variant, r.objective)
+        assert st["variant"] == r.variant
+    for p in pls:
+        p.close()

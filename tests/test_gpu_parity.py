@@ -54,20 +54,51 @@ SHAPES = [
 
 
 METHODS = {"popc": 1, "tensor": 2}
+VARIANTS = [1, 2, 3, 4]  # popc 32x32 w32, popc 32x32 w16, popc 64x32 w32, tensor 80x64 w12
 
 
-@pytest.mark.parametrize("method", sorted(METHODS))
+@pytest.mark.parametrize("variant", VARIANTS)
 @pytest.mark.parametrize("kw", SHAPES, ids=[f"s{k['n_cases'] + k['n_controls']}" for k in SHAPES])
-def test_pair_counts_bit_exact(gepi, tmp_path, kw, method):
+def test_pair_counts_bit_exact(gepi, tmp_path, kw, variant):
+    """Every counting variant (kernel, tile shape, words per stage) gives the
+    oracle's Gram counts bit for bit."""
     pl, rows, fs, _ = make_planes(gepi, kw, tmp_path)
     N = fs.n_lines
-    got = pl.pair_counts(0, N, 0, N, method=METHODS[method])
+    m = gepi.variant_method(variant)
+    got = pl.pair_counts(0, N, 0, N, method=m)
     want = H.oracle_pair_gram(rows, 0, N, 0, N)
     assert np.array_equal(got, want)
     # an unaligned sub-rectangle crossing tile boundaries
     a0, na, b0, nb = 3, min(N - 3, 37), 1, min(N - 1, 33)
-    got = pl.pair_counts(a0, na, b0, nb, method=METHODS[method])
+    got = pl.pair_counts(a0, na, b0, nb, method=m)
     assert np.array_equal(got, H.oracle_pair_gram(rows, a0, na, b0, nb))
+    pl.close()
+
+
+@pytest.mark.parametrize("kw", [
+    dict(n_snps=300, n_cases=400, n_controls=350, missing=0.02, seed=77),
+    dict(n_snps=130, n_cases=1300, n_controls=900, missing=0.03, n_planted=2, seed=78),
+])
+def test_every_variant_returns_the_same_list(gepi, tmp_path, kw):
+    """The autotuner's candidates are interchangeable: each variant's ranked
+    list (and range list) is byte-identical and equals the oracle's."""
+    pl, rows, fs, _ = make_planes(gepi, kw, tmp_path)
+    k = 400
+    want, _, _ = H.oracle_topk(rows, k)
+    lists = []
+    for v in VARIANTS:
+        got = pl.scan(k, variant=v)
+        st = pl.last_stats()
+        assert st["variant"] == v and st["tile_snps"] == gepi.variant_shape(v)["tile_a"]
+        assert_same_topk(got, want)
+        lists.append(got.tobytes())
+    assert len(set(lists)) == 1
+    ranges = {pl.scan_range(40, 70, 5, 60, 150, method=0).tobytes()}
+    for v in VARIANTS:
+        r = gepi.ScanRequest(pl, 150, a0=40, na=70, b0=5, nb=60, variant=v)
+        (got,) = gepi.scan_batch([r])
+        ranges.add(got.tobytes())
+    assert len(ranges) == 1
     pl.close()
 
 
@@ -144,9 +175,14 @@ def test_scan_is_deterministic_and_method_independent(gepi, tmp_path):
 
 
 def test_autotune_choice_drives_auto(gepi, tmp_path):
-    """METHOD_AUTO uses the autotuner's pick; both methods give the same list."""
+    """METHOD_AUTO uses the autotuner's pick -- the fastest timed variant --
+    and every method gives the same list."""
     kw = dict(n_snps=400, n_cases=600, n_controls=700, missing=0.02, seed=91)
     pl, rows, fs, _ = make_planes(gepi, kw, tmp_path)
+    rep_ = pl.autotune_variants()
+    ms = rep_["ms"]
+    assert all(v > 0 for v in ms.values()), ms
+    assert rep_["name"] == min(ms, key=ms.get)
     t = pl.autotune()
     assert t["method"] in (METHODS["popc"], METHODS["tensor"])
     assert t["popc_ms"] > 0 and t["tensor_ms"] > 0
@@ -154,6 +190,7 @@ def test_autotune_choice_drives_auto(gepi, tmp_path):
     assert pl.autotune() == t  # cached per plane set
     a = pl.scan(300)
     assert pl.last_stats()["method"] == t["method"]
+    assert pl.last_stats()["variant"] == rep_["variant"]
     b = pl.scan(300, method=METHODS["popc"] + METHODS["tensor"] - t["method"])
     assert a.tobytes() == b.tobytes()
     want, _, _ = H.oracle_topk(rows, 300)

@@ -32,9 +32,24 @@ def test_library_exports_every_header_symbol(gepi):
 
 def test_abi_version_and_status_strings(gepi):
     L = gepi.lib()
-    assert L.gepi_abi_version() == 1
+    assert L.gepi_abi_version() == 2
     assert L.gepi_status_string(0) == b"ok"
     assert L.gepi_status_string(6) == b"phenotype class 1 or 2 is empty"
+
+
+def test_counting_variants_and_struct_layouts(gepi):
+    """The counting-variant table (names, shapes) and the ctypes mirrors of the
+    structs that carry a variant match the header's layout."""
+    import ctypes
+
+    names = [gepi.variant_name(v) for v in range(1, gepi.NUM_VARIANTS + 1)]
+    assert names == ["popc_32x32_w32", "popc_32x32_w16", "popc_64x32_w32", "tensor_80x64_w12"]
+    assert gepi.variant_name(0) == "" and gepi.variant_name(gepi.NUM_VARIANTS + 1) == ""
+    assert gepi.variant_shape(3) == {"method": 1, "tile_a": 64, "tile_b": 32, "stage_words": 32}
+    assert gepi.variant_shape(4) == {"method": 2, "tile_a": 80, "tile_b": 64, "stage_words": 12}
+    assert ctypes.sizeof(gepi._Params) == 48 and gepi._Params.variant.offset == 20
+    assert ctypes.sizeof(gepi._ScanReq) == 40 and gepi._ScanReq.variant.offset == 36
+    assert gepi._ScanStats.variant.offset == 80 and ctypes.sizeof(gepi._ScanStats) == 88
 
 
 def test_result_layout_matches_interaction_result(gepi):

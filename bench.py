@@ -142,7 +142,7 @@ def measured_peaks():
 # capture (dram__bytes_read.sum + dram__bytes_write.sum of a whole launch / its
 # tiles); the operand blocks are re-read from L2, so traffic grows with the tiles
 # a launch processes and roofline.traffic scales it to the average launch.
-TC_DRAM_BYTES_PER_TILE = None
+TC_DRAM_BYTES_PER_TILE = 50815.0
 
 
 def synth_fileset(cfg: dict, seed: int) -> str:

@@ -139,10 +139,11 @@ def measured_peaks():
 
 
 # DRAM bytes per 80 x 64 tile of tc_tile_kernel at 10,000 samples, from one ncu
-# capture (dram__bytes_read.sum + dram__bytes_write.sum of a whole launch / its
-# tiles); the operand blocks are re-read from L2, so traffic grows with the tiles
-# a launch processes and roofline.traffic scales it to the average launch.
-TC_DRAM_BYTES_PER_TILE = 50815.0
+# capture of the 40,000-SNP profiling scan (dram__bytes_read.sum +
+# dram__bytes_write.sum of its 8 launches / its 156,750 tiles, mean of 5 scans);
+# the operand blocks are re-read from L2, so traffic grows with the tiles a
+# launch processes and roofline.traffic scales it to the average launch.
+TC_DRAM_BYTES_PER_TILE = 51213.0
 
 
 def synth_fileset(cfg: dict, seed: int) -> str:

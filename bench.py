@@ -557,6 +557,7 @@ def run_serving(args):
         levels = []
         with ClockSampler(local) as clk:
             for load in c["loads"]:
+                st0 = srv.stats()
                 rate = load * peak_rps
                 gaps = rng.exponential(1.0 / rate, size=nreq)
                 infos = [None] * nreq
@@ -581,6 +582,8 @@ def run_serving(args):
                     ready.release()
                 th.join()
                 span = time.perf_counter() - t0
+                st1 = srv.stats()
+                steps = max(1, st1["steps"] - st0["steps"])
                 lat = [x["latency_ms"] for x in infos]
                 slow = [x["latency_ms"] / max(a, 1e-3) for x, a in zip(infos, alone)]
                 levels.append({
@@ -588,7 +591,11 @@ def run_serving(args):
                     "p99_ms": pct(lat, 0.99), "pair_tests_per_s": sum(pairs) / span,
                     "p99_over_alone_p99": pct(lat, 0.99) / pct(alone, 0.99),
                     "slowdown_p50": pct(slow, 0.5), "slowdown_p99": pct(slow, 0.99),
-                    "queue_p99_ms": pct([x["queue_ms"] for x in infos], 0.99)})
+                    "queue_p99_ms": pct([x["queue_ms"] for x in infos], 0.99),
+                    "engine": {"steps": st1["steps"] - st0["steps"],
+                               "device_ms_per_step": (st1["device_ms"] - st0["device_ms"]) / steps,
+                               "host_ms_per_step": (st1["wall_ms"] - st0["wall_ms"]) / steps,
+                               "gpu_busy": (st1["device_ms"] - st0["device_ms"]) / (1e3 * span)}})
     at80 = min(levels, key=lambda L: abs(L["offered_load"] - 0.8))
     line = {
         "metric": "p50/p99 request latency, served mixed stream at 80% of peak offered load",
@@ -603,6 +610,9 @@ def run_serving(args):
                                 "arrivals"),
                    "matrices": [[n, s] for _, n, s in mats]},
         "clocks": clk.summary(),
+        "policy": {"order": os.environ.get("GEPI_SERVE_POLICY", "deadline"),
+                   "slack": float(os.environ.get("GEPI_SERVE_SLACK", "1.5")),
+                   "quantum_ms": float(os.environ.get("GEPI_QUANTUM_MS", "4"))},
         "alone": {"p50_ms": pct(alone, 0.5), "p99_ms": pct(alone, 0.99)},
         "peak": {"requests_per_s": peak_rps, "pair_tests_per_s": sum(pairs) / burst_s},
         "levels": levels,

@@ -90,7 +90,8 @@ class _ScanReq(ctypes.Structure):
 
 class _BatchStats(ctypes.Structure):
     _fields_ = [("steps", ctypes.c_int64), ("count_launches", ctypes.c_int64),
-                ("select_launches", ctypes.c_int64), ("graph_launches", ctypes.c_int64)]
+                ("select_launches", ctypes.c_int64), ("graph_launches", ctypes.c_int64),
+                ("device_ms", ctypes.c_double), ("wall_ms", ctypes.c_double)]
 
 
 class _TuneReport(ctypes.Structure):
@@ -181,6 +182,7 @@ def lib():
     L.gepi_server_create.argtypes = [i32, sz, PP]
     L.gepi_server_submit.argtypes = [P, ctypes.POINTER(_ScanReq), ctypes.POINTER(u64)]
     L.gepi_server_wait.argtypes = [P, u64, P, ctypes.POINTER(_RequestInfo)]
+    L.gepi_server_stats.argtypes = [P, ctypes.POINTER(_BatchStats)]
     L.gepi_server_destroy.argtypes = [P]
     L.gepi_server_destroy.restype = None
     L.gepi_fisher_pval.argtypes = [i32, i32, i32, i32]
@@ -197,7 +199,7 @@ def lib():
               "gepi_last_scan_stats", "gepi_last_scan_values", "gepi_process_gpu_1_noalloc", "gepi_planes_autotune",
               "gepi_tensor_peak_tflops", "gepi_tensor_peak_probe", "gepi_planes_autotune_variants",
               "gepi_count_variant_shape", "gepi_scan_batch_stats", "gepi_scan_batch", "gepi_scan_progress", "gepi_shard_range", "gepi_merge_results", "gepi_server_create",
-              "gepi_server_submit", "gepi_server_wait",
+              "gepi_server_submit", "gepi_server_wait", "gepi_server_stats",
               "gepi_synth_bed", "gepi_synth_write"):
         getattr(L, f).restype = i32
     _lib = L
@@ -558,8 +560,9 @@ def scan_batch(reqs, with_stats: bool = False):
 
 
 def scan_batch_stats(device: int = 0) -> dict:
-    """Launch counts of the last scan_batch call on `device` (engine steps,
-    counting launches, batched select launches, step-graph replays)."""
+    """Counters of the last scan_batch call on `device`: engine steps,
+    counting launches, batched select launches, step-graph replays, and the
+    steps' device and host milliseconds."""
     st = _BatchStats()
     _check(lib().gepi_scan_batch_stats(device, ctypes.byref(st)))
     return {f: getattr(st, f) for f, _ in _BatchStats._fields_}
@@ -589,6 +592,12 @@ class Server:
         info = _RequestInfo()
         _check(lib().gepi_server_wait(self._h, ticket, _ptr(tops), ctypes.byref(info)))
         return tops, {f: getattr(info, f) for f, _ in _RequestInfo._fields_ if f != "reserved"}
+
+    def stats(self) -> dict:
+        """The server engine's counters since creation (gepi_server_stats)."""
+        st = _BatchStats()
+        _check(lib().gepi_server_stats(self._h, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in _BatchStats._fields_}
 
     def close(self):
         if self._h:

@@ -133,15 +133,22 @@ struct Job {
     Clock::time_point t_submit, t_admit, t_done;
 };
 
-// Which requests' tiles go first in a step and get the quantum first: those
-// with little work left (shortest first), or the oldest.
-enum class Policy { ShortFirst, Oldest };
+// Which requests' tiles go first in a step and get the quantum first:
+//  * Deadline: earliest deadline first, a request's deadline being its
+//    submission time plus `slack` times its estimated device time alone
+//    (tiles x measured ms per tile, plus about one step).  Short requests
+//    pass long ones, but a long request that has waited about slack x its own
+//    time goes ahead of newer short ones, which bounds the latency of the
+//    long requests -- the tail of a mixed stream.
+//  * ShortFirst: least work left first (shortest remaining time).
+//  * Oldest: first come, first served.
+enum class Policy { Deadline, ShortFirst, Oldest };
 
 class Engine {
    public:
     // quantum_ms > 0 caps each step at about that much device time.
-    Engine(int device, double quantum_ms, Policy policy = Policy::ShortFirst)
-        : device_(device), quantum_ms_(quantum_ms), policy_(policy) {}
+    Engine(int device, double quantum_ms, Policy policy = Policy::Deadline, double slack = 1.5)
+        : device_(device), quantum_ms_(quantum_ms), policy_(policy), slack_(slack) {}
     ~Engine();
     gepi_status init();
     // Counting variant, plane-set tables and the device tile list: may run on
@@ -170,8 +177,11 @@ class Engine {
 
     int device_ = 0, num_sms_ = 0;
     double quantum_ms_ = 0.0;
-    Policy policy_ = Policy::ShortFirst;
-    cudaStream_t stream_ = nullptr, upload_ = nullptr;
+    Policy policy_ = Policy::Deadline;
+    double slack_ = 1.5;
+    // stream_: the steps; upload_: tile lists; fin_: read-back of finished
+    // requests' candidates while the next step runs
+    cudaStream_t stream_ = nullptr, upload_ = nullptr, fin_ = nullptr;
     cudaEvent_t ev_[3] = {nullptr, nullptr, nullptr};  // step start, counting done, step done
     // per-slot device state: scan state, radix-select scratch
     int nslots_ = 0;
@@ -216,6 +226,7 @@ Engine::~Engine() {
         cudaStreamSynchronize(upload_);
         cudaStreamDestroy(upload_);
     }
+    if (fin_) cudaStreamDestroy(fin_);
     if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -225,6 +236,7 @@ gepi_status Engine::init() {
     GEPI_CUDA(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, device_));
     GEPI_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
     GEPI_CUDA(cudaStreamCreateWithFlags(&upload_, cudaStreamNonBlocking));
+    GEPI_CUDA(cudaStreamCreateWithFlags(&fin_, cudaStreamNonBlocking));
     for (cudaEvent_t &e : ev_) GEPI_CUDA(cudaEventCreate(&e));
     GEPI_CUDA(cudaMallocHost(&h_queues_, sizeof(WorkQueue) * kGroups));
     return ensure_slots(16);
@@ -464,10 +476,13 @@ gepi_status Engine::admit(Job &j) {
     init.lp_thr = INFINITY;
     init.tau_f = -INFINITY;
     init.tau_val = -INFINITY;
-    h_states_[j.slot] = init;  // no step in flight: the read-back buffer is free
+    // No step is in flight (admission happens between steps), so the slot of
+    // the pinned read-back buffer is free; the upload is ordered before the
+    // next step on the engine's stream, and that step's read-back -- which
+    // overwrites the buffer -- after the upload.
+    h_states_[j.slot] = init;
     GEPI_CUDA(cudaMemcpyAsync(d_states_ + j.slot, h_states_ + j.slot, sizeof(ScanState),
                               cudaMemcpyHostToDevice, stream_));
-    GEPI_CUDA(cudaStreamSynchronize(stream_));
 
     // as in the direct scan: the same select budget, trigger and first batch
     const double tests_per_tile = 20.0 * j.TA * j.TB;
@@ -509,11 +524,13 @@ gepi_status Engine::finish(std::vector<Job *> &jobs) {
     for (size_t i = 0; i < jobs.size(); ++i) {
         Job &j = *jobs[i];
         host[i].resize(j.count);
-        if (j.count)  // pageable destination: ordered on the stream
+        // the request's last step has completed, and its buffers are not
+        // part of the step that may be running on the engine's stream
+        if (j.count)
             GEPI_CUDA(cudaMemcpyAsync(host[i].data(), j.buf->cand[j.cur], (size_t)j.count * sizeof(Cand),
-                                      cudaMemcpyDeviceToHost, stream_));
+                                      cudaMemcpyDeviceToHost, fin_));
     }
-    GEPI_CUDA(cudaStreamSynchronize(stream_));
+    GEPI_CUDA(cudaStreamSynchronize(fin_));
     for (size_t i = 0; i < jobs.size(); ++i) {
         Job &j = *jobs[i];
         const int k = j.rq.k;
@@ -547,20 +564,36 @@ void Engine::size_next_batch(Job &j, uint32_t appended, size_t nbt) {
 }
 
 // This step's batch of every running request: its natural batch; under a
-// device-time quantum the requests, in policy order (least work left first,
-// or oldest first), fill the quantum, each getting at least one tile.  The
-// order is also the order of their tiles in the work lists, so the CTAs claim
-// the first requests' tiles first.
+// device-time quantum the requests, in policy order, fill the quantum, each
+// getting at least one tile.  The order is also the order of their tiles in
+// the work lists, so the CTAs claim the first requests' tiles first.
 void Engine::plan(std::vector<Job *> &run) {
     auto left = [&](const Job *j) {
         return (double)(j->ntiles - j->next) * j->weight * ms_per_weight_[j->group];
     };
-    if (policy_ == Policy::Oldest)
+    auto arrival = [](const Job *j) {  // submission (serving) or admission (batch)
+        const Clock::time_point t = j->t_submit.time_since_epoch().count() ? j->t_submit : j->t_admit;
+        return std::chrono::duration<double, std::milli>(t.time_since_epoch()).count();
+    };
+    if (policy_ == Policy::Oldest) {
         std::stable_sort(run.begin(), run.end(),
-                         [](const Job *a, const Job *b) { return a->t_admit < b->t_admit; });
-    else
+                         [&](const Job *a, const Job *b) { return arrival(a) < arrival(b); });
+    } else if (policy_ == Policy::ShortFirst) {
         std::stable_sort(run.begin(), run.end(),
                          [&](const Job *a, const Job *b) { return left(a) < left(b); });
+    } else {
+        // estimated device time alone: every tile at the measured cost, plus
+        // about one millisecond of fixed cost per request
+        std::vector<std::pair<double, Job *>> key;
+        key.reserve(run.size());
+        for (Job *j : run) {
+            const double alone = (double)j->ntiles * j->weight * ms_per_weight_[j->group] + 1.0;
+            key.emplace_back(arrival(j) + slack_ * alone, j);
+        }
+        std::stable_sort(key.begin(), key.end(),
+                         [](const auto &a, const auto &b) { return a.first < b.first; });
+        for (size_t i = 0; i < run.size(); ++i) run[i] = key[i].second;
+    }
     double room = quantum_ms_;
     for (Job *j : run) {
         size_t nbt = std::min(j->batch, j->ntiles - j->next);
@@ -576,6 +609,7 @@ void Engine::plan(std::vector<Job *> &run) {
 
 void Engine::step(std::vector<Job *> &active) {
     DeviceGuard g(device_);
+    const Clock::time_point t_step = Clock::now();
     // requests with every tile counted and no select pending finish; the rest
     // run a batch (possibly empty: only the final select is left)
     std::vector<Job *> fin, run;
@@ -594,11 +628,18 @@ void Engine::step(std::vector<Job *> &active) {
             j->t_done = Clock::now();
         }
     };
-    if (!fin.empty()) {
+    // the finished requests' results are read back and ranked while the
+    // step of the others runs
+    auto finish_all = [&]() {
+        if (fin.empty()) return;
         const gepi_status st = finish(fin);
         if (st != GEPI_OK) fail_all(fin, st);
+    };
+    if (run.empty()) {
+        finish_all();
+        counters.wall_ms += ms_between(t_step, Clock::now());
+        return;
     }
-    if (run.empty()) return;
     plan(run);
 
     // the step's descriptors
@@ -663,6 +704,7 @@ void Engine::step(std::vector<Job *> &active) {
         sj.active = 1;
     }
     gepi_status st = launch_step(mask);
+    finish_all();
     counters.steps += 1;
     // on any failure below, the step's device work finishes before the
     // requests -- and their buffers -- are released
@@ -693,8 +735,10 @@ void Engine::step(std::vector<Job *> &active) {
     if (st != GEPI_OK) {
         drain();
         fail_all(run, st);
+        counters.wall_ms += ms_between(t_step, Clock::now());
         return;
     }
+    counters.device_ms += step_ms;
     // device cost per unit of tile weight, per group (for the quantum)
     {
         double w[kGroups] = {0, 0, 0, 0, 0};
@@ -749,6 +793,7 @@ void Engine::step(std::vector<Job *> &active) {
             size_next_batch(*j, appended, nbt);
         }
     }
+    counters.wall_ms += ms_between(t_step, Clock::now());
 }
 
 // ---- the device engines used by gepi_scan_batch -----------------------------
@@ -810,6 +855,15 @@ Policy env_policy(Policy dflt) {
     if (const char *e = std::getenv("GEPI_SERVE_POLICY")) {
         if (!std::strcmp(e, "oldest")) return Policy::Oldest;
         if (!std::strcmp(e, "short")) return Policy::ShortFirst;
+        if (!std::strcmp(e, "deadline")) return Policy::Deadline;
+    }
+    return dflt;
+}
+
+double env_slack(double dflt) {
+    if (const char *e = std::getenv("GEPI_SERVE_SLACK")) {
+        const double v = std::atof(e);
+        if (v >= 0.0) return v;
     }
     return dflt;
 }
@@ -896,6 +950,7 @@ struct gepi_server {
     std::map<uint64_t, std::unique_ptr<gepi::Job>> jobs;
     uint64_t next_ticket = 1;
     bool stop = false;
+    gepi_batch_stats stats{};  // the engine's counters, copied under mu between steps
 
     void run();
 };
@@ -910,6 +965,7 @@ void gepi_server::run() {
     for (;;) {
         {
             std::unique_lock<std::mutex> lk(mu);
+            stats = engine->counters;
             for (;;) {
                 while (!pending.empty()) {
                     Job *j = pending.front();
@@ -964,7 +1020,8 @@ gepi_status gepi_server_create(int32_t device, size_t hbm_budget_bytes, gepi_ser
     srv->device = device;
     srv->budget = hbm_budget_bytes ? hbm_budget_bytes : (16ull << 30);
     srv->engine =
-        std::make_unique<Engine>(device, env_quantum_ms(4.0), env_policy(Policy::ShortFirst));
+        std::make_unique<Engine>(device, env_quantum_ms(4.0), env_policy(Policy::Deadline),
+                                 env_slack(1.5));
     GEPI_TRY(srv->engine->init());
     gepi_server *p = srv.get();
     p->thread = std::thread([p] { p->run(); });
@@ -1027,6 +1084,14 @@ gepi_status gepi_server_wait(gepi_server *srv, uint64_t ticket, gepi_result *top
     }
     if (j->status != GEPI_OK) return set_error(j->status, j->error);
     std::memcpy(tops, j->tops, sizeof(gepi_result) * (size_t)j->rq.k);
+    return GEPI_OK;
+}
+
+gepi_status gepi_server_stats(gepi_server *srv, gepi_batch_stats *out) {
+    clear_error();
+    if (!srv || !out) return set_error(GEPI_ERR_ARG, "gepi_server_stats: bad argument");
+    std::lock_guard<std::mutex> lk(srv->mu);
+    *out = srv->stats;
     return GEPI_OK;
 }
 

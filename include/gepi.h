@@ -329,13 +329,17 @@ gepi_status gepi_scan_batch(const gepi_scan_req *reqs, int32_t n, gepi_result *c
 /* Launch counts of the last gepi_scan_batch call on `device`: engine steps,
  * counting launches (one per kernel group present in a step: the tensor-core
  * kernel per objective, the popcount kernel per variant), select launches
- * (20 per step, batched over every request) and step-graph replays.  No
- * counterpart in the reference. */
+ * (20 per step, batched over every request) and step-graph replays; the
+ * device time of the steps (upload to read-back, CUDA events) and the host
+ * time spent in them (planning to results consumed), in ms.  No counterpart
+ * in the reference. */
 typedef struct gepi_batch_stats {
     int64_t steps;
     int64_t count_launches;
     int64_t select_launches;
     int64_t graph_launches;
+    double device_ms;
+    double wall_ms;
 } gepi_batch_stats;
 gepi_status gepi_scan_batch_stats(int32_t device, gepi_batch_stats *out);
 
@@ -344,13 +348,16 @@ gepi_status gepi_scan_batch_stats(int32_t device, gepi_batch_stats *out);
  * <= 512 Ki) fits `hbm_budget_bytes` (0: 16 GiB; the oldest request is always
  * admitted when nothing runs), and runs all admitted requests together as
  * gepi_scan_batch does, admitting new ones between engine steps.  A step is
- * capped at about 4 ms of device time (GEPI_QUANTUM_MS): requests with little
- * work left get their batches -- and the first tiles of the step's work lists
- * -- first (GEPI_SERVE_POLICY=short, the default; "oldest": the oldest
- * requests first), every request at least one tile per step.  Plane sets
- * submitted to a server must not be used by other calls until their requests
- * are waited for.  No counterpart in the reference (it runs one scan per
- * process). */
+ * capped at about 4 ms of device time (GEPI_QUANTUM_MS); the requests get
+ * their batches -- and the first tiles of the step's work lists -- in policy
+ * order, every request at least one tile per step.  GEPI_SERVE_POLICY:
+ * "deadline" (the default) orders by submission time + GEPI_SERVE_SLACK
+ * (default 1.5) x the request's estimated device time alone, so short
+ * requests pass long ones until a long one has waited about 1.5x its own
+ * time; "short": least work left first; "oldest": first come, first served.
+ * Plane sets submitted to a server must not be used by other calls until
+ * their requests are waited for.  No counterpart in the reference (it runs
+ * one scan per process). */
 typedef struct gepi_server gepi_server;
 typedef struct gepi_request_info {
     double queue_ms;    /* submit -> admission                          */
@@ -368,6 +375,9 @@ gepi_status gepi_server_submit(gepi_server *srv, const gepi_scan_req *req, uint6
  * Each ticket is waited for once. */
 gepi_status gepi_server_wait(gepi_server *srv, uint64_t ticket, gepi_result *tops,
                              gepi_request_info *info);
+/* The server's engine counters since it was created (the fields of
+ * gepi_batch_stats), as of the last completed step. */
+gepi_status gepi_server_stats(gepi_server *srv, gepi_batch_stats *out);
 /* Finishes admitted requests, fails queued ones, stops the thread.  No wait
  * may be in progress. */
 void gepi_server_destroy(gepi_server *srv);

@@ -2,6 +2,7 @@
 loop (gepi_server_*).  Every request's results must equal, bit for bit, the
 direct gepi_scan_range call with the same arguments, and the oracle's."""
 import threading
+import time
 
 import numpy as np
 import pytest
@@ -93,13 +94,13 @@ def test_batch_exact_under_candidate_overflow(gepi, tmp_path, cap, monkeypatch):
         pl.close()
 
 
-@pytest.mark.parametrize("policy", ["short", "oldest"])
+@pytest.mark.parametrize("policy", ["deadline", "short", "oldest"])
 @pytest.mark.parametrize("budget", [0, 1])
 def test_server_same_result_alone_and_mixed(gepi, tmp_path, budget, policy, monkeypatch):
     """A request gives the same results served alone as among others
     submitted concurrently from several threads (budget 1 byte: one request
-    admitted at a time; 0: the default budget, all together), under either
-    scheduling policy and a 1 ms batch quantum."""
+    admitted at a time; 0: the default budget, all together), under every
+    scheduling policy and a 1 ms batch quantum; the server's counters add up."""
     monkeypatch.setenv("GEPI_SERVE_POLICY", policy)
     monkeypatch.setenv("GEPI_QUANTUM_MS", "1")
     cohorts = _cohorts(gepi, tmp_path)
@@ -127,6 +128,12 @@ def test_server_same_result_alone_and_mixed(gepi, tmp_path, budget, policy, monk
         # and all at once from one thread
         tickets = [srv.submit(r) for r in reversed(reqs)]
         burst = [srv.wait(t)[0] for t in tickets][::-1]
+        time.sleep(0.05)  # the loop copies its counters before it next sleeps
+        st = srv.stats()
+    assert st["steps"] >= len(reqs) // 2
+    assert st["graph_launches"] == st["steps"]
+    assert st["select_launches"] == 20 * st["steps"]
+    assert 0.0 < st["device_ms"] <= st["wall_ms"]
     for r, a, m, b in zip(reqs, alone, mixed, burst):
         d = _direct(r)
         assert a.tobytes() == d.tobytes()

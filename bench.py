@@ -592,6 +592,10 @@ def run_serving(args):
                     "p99_over_alone_p99": pct(lat, 0.99) / pct(alone, 0.99),
                     "slowdown_p50": pct(slow, 0.5), "slowdown_p99": pct(slow, 0.99),
                     "queue_p99_ms": pct([x["queue_ms"] for x in infos], 0.99),
+                    # the requests that set the tail: latency, alone, queue (ms), pairs
+                    "slowest": [[round(infos[i]["latency_ms"], 1), round(alone[i], 1),
+                                 round(infos[i]["queue_ms"], 1), int(pairs[i])]
+                                for i in sorted(range(nreq), key=lambda i: -infos[i]["latency_ms"])[:6]],
                     "engine": {"steps": st1["steps"] - st0["steps"],
                                "device_ms_per_step": (st1["device_ms"] - st0["device_ms"]) / steps,
                                "host_ms_per_step": (st1["wall_ms"] - st0["wall_ms"]) / steps,
@@ -610,7 +614,7 @@ def run_serving(args):
                                 "arrivals"),
                    "matrices": [[n, s] for _, n, s in mats]},
         "clocks": clk.summary(),
-        "policy": {"order": os.environ.get("GEPI_SERVE_POLICY", "deadline"),
+        "policy": {"order": os.environ.get("GEPI_SERVE_POLICY", "short"),
                    "slack": float(os.environ.get("GEPI_SERVE_SLACK", "1.5")),
                    "quantum_ms": float(os.environ.get("GEPI_QUANTUM_MS", "4"))},
         "alone": {"p50_ms": pct(alone, 0.5), "p99_ms": pct(alone, 0.99)},

@@ -445,6 +445,17 @@ __device__ __forceinline__ float u16f(uint16_t v) {
     return __uint_as_float(0x4B000000u | (uint32_t)v) - 8388608.0f;
 }
 
+// Two accumulator counts (FP32 bit patterns of exact integers below 2^16) as
+// one word of two 16-bit counts, lo | hi << 16: adding 2^23 puts each count in
+// the low mantissa bits (exact, so the rounding mode does not matter), and one
+// byte permute takes the two low halves -- two FMA-pipe adds and one ALU
+// instruction instead of two conversion-unit instructions, a shift and an or.
+__device__ __forceinline__ uint32_t pack_counts(uint32_t lo, uint32_t hi) {
+    const uint32_t a = __float_as_uint(__uint_as_float(lo) + 8388608.0f);
+    const uint32_t b = __float_as_uint(__uint_as_float(hi) + 8388608.0f);
+    return __byte_perm(a, b, 0x5410);
+}
+
 // Count of function f (AND, NAND, ANDN, NANDN, XOR) from n11 and the margins.
 __device__ __forceinline__ int fun_count(int n11, int r, int c, int tot, int f) {
     switch (f) {
@@ -675,8 +686,7 @@ struct TcScorer {
 #pragma unroll
                     for (int m = 0; m < 4; ++m)
                         rw[qq * (kB / 2) + 4 * gl + m] =
-                            __float2uint_rn(__uint_as_float(v[6 * m + qq])) |
-                            (__float2uint_rn(__uint_as_float(v[6 * m + 3 + qq])) << 16);
+                            pack_counts(v[6 * m + qq], v[6 * m + 3 + qq]);
             }
             tc_fence_before();
             __syncwarp();
@@ -1066,8 +1076,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
 #pragma unroll
                         for (int m = 0; m < 4; ++m)
                             rw[qq * (kB / 2) + 4 * gl + m] =
-                                __float2uint_rn(__uint_as_float(v[6 * m + qq])) |
-                                (__float2uint_rn(__uint_as_float(v[6 * m + 3 + qq])) << 16);
+                                pack_counts(v[6 * m + qq], v[6 * m + 3 + qq]);
                 }
                 tc_fence_before();
                 __syncwarp();

@@ -272,7 +272,17 @@ __device__ __forceinline__ void append_candidate(const ScanCtx &ctx, double valu
                                                  int rB, int fun, int w, int x, int y, int z) {
     unsigned long long key = key_of(value);
     if (key < ctx.st->tau_key) return;
-    uint32_t idx = atomicAdd(&ctx.st->count, 1u);
+    // One atomic per group of lanes appending together: in a scan's first
+    // batch, with no threshold yet, every test of a tile is appended, and one
+    // atomic per test on the one counter would serialise them.
+    const unsigned grp = __activemask();
+    unsigned lane;
+    asm("mov.u32 %0, %%laneid;" : "=r"(lane));
+    const int leader = __ffs(grp) - 1;
+    uint32_t base = 0;
+    if ((int)lane == leader) base = atomicAdd(&ctx.st->count, (uint32_t)__popc(grp));
+    base = __shfl_sync(grp, base, leader);
+    const uint32_t idx = base + (uint32_t)__popc(grp & ((1u << lane) - 1u));
     if (idx >= ctx.cap) {
         ctx.st->overflow = 1u;
         return;

@@ -14,9 +14,11 @@
 //     kernel of a variant for every popcount request of that variant -- whose
 //     CTAs (pairs) claim tiles from the concatenated work list with an atomic
 //     counter,
-//   * one chain of 20 batched select launches over every request (gridDim.y =
-//     request), each request's select decided on the device from its scan
-//     state exactly as the direct scan decides it on the host,
+//   * one chain of 20 batched select launches over every request (the small
+//     ones with gridDim.y = request, the histogram and compaction passes on
+//     the whole grid walking the requests in turn), each request's select
+//     decided on the device from its scan state exactly as the direct scan
+//     decides it on the host,
 //   * a read-back of every request's scan state.
 // The graph is captured once per set of kernel groups and slot capacity and
 // replayed with new descriptors every step.  Between steps the host sizes
@@ -134,20 +136,20 @@ struct Job {
 };
 
 // Which requests' tiles go first in a step and get the quantum first:
+//  * ShortFirst: least work left first (shortest remaining time; the server's
+//    default, the lowest tail latency measured on a mixed stream);
 //  * Deadline: earliest deadline first, a request's deadline being its
 //    submission time plus `slack` times its estimated device time alone
-//    (tiles x measured ms per tile, plus about one step).  Short requests
-//    pass long ones, but a long request that has waited about slack x its own
-//    time goes ahead of newer short ones, which bounds the latency of the
-//    long requests -- the tail of a mixed stream.
-//  * ShortFirst: least work left first (shortest remaining time).
+//    (tiles x measured ms per tile, plus about one millisecond): a long
+//    request goes ahead of newer short ones once it has waited about slack x
+//    its own time, so its latency approaches (1 + slack) x its time alone;
 //  * Oldest: first come, first served.
-enum class Policy { Deadline, ShortFirst, Oldest };
+enum class Policy { ShortFirst, Deadline, Oldest };
 
 class Engine {
    public:
     // quantum_ms > 0 caps each step at about that much device time.
-    Engine(int device, double quantum_ms, Policy policy = Policy::Deadline, double slack = 1.5)
+    Engine(int device, double quantum_ms, Policy policy = Policy::ShortFirst, double slack = 1.5)
         : device_(device), quantum_ms_(quantum_ms), policy_(policy), slack_(slack) {}
     ~Engine();
     gepi_status init();
@@ -177,7 +179,7 @@ class Engine {
 
     int device_ = 0, num_sms_ = 0;
     double quantum_ms_ = 0.0;
-    Policy policy_ = Policy::Deadline;
+    Policy policy_ = Policy::ShortFirst;
     double slack_ = 1.5;
     // stream_: the steps; upload_: tile lists; fin_: read-back of finished
     // requests' candidates while the next step runs
@@ -739,17 +741,37 @@ void Engine::step(std::vector<Job *> &active) {
         return;
     }
     counters.device_ms += step_ms;
-    // device cost per unit of tile weight, per group (for the quantum)
+    // Device cost per unit of tile weight, per group (for the quantum and the
+    // deadlines).  A launch of few tiles leaves most SMs idle and its fixed
+    // cost dominates, so its time over its weight overstates the cost of a
+    // tile: such a step may only lower the estimate; steps of at least two
+    // tiles per SM set it.
     {
         double w[kGroups] = {0, 0, 0, 0, 0};
-        for (Job *j : run) w[j->group] += (double)j->inflight * j->weight;
+        size_t nt[kGroups] = {0, 0, 0, 0, 0};
+        for (Job *j : run) {
+            w[j->group] += (double)j->inflight * j->weight;
+            nt[j->group] += j->inflight;
+        }
         double wsum = 0.0;
-        for (double v : w) wsum += v;
+        size_t tsum = 0;
+        for (int q = 0; q < kGroups; ++q) {
+            wsum += w[q];
+            tsum += nt[q];
+        }
         if (wsum > 0.0 && count_ms > 0.f) {
             const double per = (double)count_ms / wsum;
-            for (int q = 0; q < kGroups; ++q)
-                if (w[q] > 0.0)
-                    ms_per_weight_[q] = ms_per_weight_[q] > 0.0 ? 0.5 * (ms_per_weight_[q] + per) : per;
+            const bool full = tsum >= 2 * (size_t)num_sms_;
+            for (int q = 0; q < kGroups; ++q) {
+                if (w[q] <= 0.0) continue;
+                double &e = ms_per_weight_[q];
+                if (e <= 0.0)
+                    e = per;
+                else if (full)
+                    e = 0.5 * (e + per);
+                else if (per < e)
+                    e = per;
+            }
         }
     }
     for (Job *j : run) {
@@ -1020,7 +1042,7 @@ gepi_status gepi_server_create(int32_t device, size_t hbm_budget_bytes, gepi_ser
     srv->device = device;
     srv->budget = hbm_budget_bytes ? hbm_budget_bytes : (16ull << 30);
     srv->engine =
-        std::make_unique<Engine>(device, env_quantum_ms(4.0), env_policy(Policy::Deadline),
+        std::make_unique<Engine>(device, env_quantum_ms(4.0), env_policy(Policy::ShortFirst),
                                  env_slack(1.5));
     GEPI_TRY(srv->engine->init());
     gepi_server *p = srv.get();

@@ -53,7 +53,7 @@ cudaError_t run_select_compact(Cand *in, Cand *out, ScanState *st, void *sel, ui
 size_t sel_state_bytes();
 constexpr int kSelectLaunches = 20;  // init + 8 x (histogram, pick) + apply + compact + count
 // The selects of every request of an engine step, decided on the device
-// (gridDim.y = request; 20 launches whatever the number of requests).
+// (20 launches whatever the number of requests).
 cudaError_t run_select_batch(SelJob *jobs, int njobs, int num_sms, cudaStream_t stream);
 
 // Counting variants: a counting kernel with its tile shape and plane words per

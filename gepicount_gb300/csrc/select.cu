@@ -183,7 +183,7 @@ cudaError_t run_select_compact(Cand *in, Cand *out, ScanState *st, void *sel_raw
 size_t sel_state_bytes() { return sizeof(SelState); }
 
 // ---- batched selects: one chain of launches for every request of an engine
-// step (gridDim.y = request), replayed from a CUDA graph.  Each request's
+// step, replayed from a CUDA graph.  Each request's
 // select is decided on the device from its scan state, exactly as the direct
 // scan decides it on the host (scan.cu):
 //   overflow in this batch             -> select over the first `cap` entries,
@@ -196,7 +196,7 @@ size_t sel_state_bytes() { return sizeof(SelState); }
 // The mode taken is left in ScanState::sel_mode for the host.
 
 // Slots without a request this step (active = 0) carry null state and
-// scratch pointers: every batched kernel returns before touching them.
+// scratch pointers: every batched kernel skips them before touching them.
 __global__ void bsel_init_kernel(SelJob *jobs) {
     SelJob &j = jobs[blockIdx.y];
     if (!j.active) return;
@@ -220,24 +220,31 @@ __global__ void bsel_init_kernel(SelJob *jobs) {
     for (int i = threadIdx.x; i < 256; i += blockDim.x) sel->hist[i] = 0u;
 }
 
-__global__ void bsel_hist_kernel(const SelJob *jobs, int shift) {
-    const SelJob &j = jobs[blockIdx.y];
-    if (!j.active) return;
-    SelState *sel = j.sel;
+// The histogram passes and the compaction run on a 1-D grid (4 CTAs per SM)
+// that walks the slots in turn, so each request's pass gets the whole GPU
+// whatever the slot capacity; the per-slot branches are uniform across a CTA
+// (every thread reads the same descriptor and scratch words).
+__global__ void bsel_hist_kernel(const SelJob *jobs, int njobs, int shift) {
     __shared__ uint32_t h[256];
-    if (sel->krem == 0) return;
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0u;
-    __syncthreads();
-    const uint32_t n = sel->n;
-    const unsigned long long prefix = sel->prefix, mask = sel->mask;
-    const Cand *__restrict__ cand = j.in;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        unsigned long long key = cand[i].key;
-        if ((key & mask) == prefix) atomicAdd(&h[(key >> shift) & 255u], 1u);
+    for (int q = 0; q < njobs; ++q) {
+        const SelJob &j = jobs[q];
+        if (!j.active) continue;
+        SelState *sel = j.sel;
+        if (sel->krem == 0) continue;
+        for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0u;
+        __syncthreads();
+        const uint32_t n = sel->n;
+        const unsigned long long prefix = sel->prefix, mask = sel->mask;
+        const Cand *__restrict__ cand = j.in;
+        for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+            unsigned long long key = cand[i].key;
+            if ((key & mask) == prefix) atomicAdd(&h[(key >> shift) & 255u], 1u);
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < 256; i += blockDim.x)
+            if (h[i]) atomicAdd(&sel->hist[i], h[i]);
+        __syncthreads();  // h is cleared for the next slot
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i < 256; i += blockDim.x)
-        if (h[i]) atomicAdd(&sel->hist[i], h[i]);
 }
 
 __global__ void bsel_pick_kernel(const SelJob *jobs, int shift) {
@@ -252,12 +259,14 @@ __global__ void bsel_apply_kernel(const SelJob *jobs) {
     sel_apply(j.st, j.sel, j.objective, j.lp_margin);
 }
 
-__global__ void bcompact_kernel(const SelJob *jobs) {
-    const SelJob &j = jobs[blockIdx.y];
-    if (!j.active) return;
-    const int mode = (int)j.sel->pad;
-    if (!mode) return;
-    compact_range(j.in, j.out, j.st, j.sel, mode == 2 ? j.count_before : 0xFFFFFFFFu);
+__global__ void bcompact_kernel(const SelJob *jobs, int njobs) {
+    for (int q = 0; q < njobs; ++q) {
+        const SelJob &j = jobs[q];
+        if (!j.active) continue;
+        const int mode = (int)j.sel->pad;
+        if (!mode) continue;
+        compact_range(j.in, j.out, j.st, j.sel, mode == 2 ? j.count_before : 0xFFFFFFFFu);
+    }
 }
 
 __global__ void bset_count_kernel(const SelJob *jobs) {
@@ -269,14 +278,14 @@ __global__ void bset_count_kernel(const SelJob *jobs) {
 
 cudaError_t run_select_batch(SelJob *jobs, int njobs, int num_sms, cudaStream_t stream) {
     if (njobs <= 0) return cudaSuccess;
-    const int gx = std::max(1, (num_sms * 4 + njobs - 1) / njobs);
+    const int grid = num_sms * 4;
     bsel_init_kernel<<<dim3(1, njobs), 256, 0, stream>>>(jobs);
     for (int shift = 56; shift >= 0; shift -= 8) {
-        bsel_hist_kernel<<<dim3(gx, njobs), 256, 0, stream>>>(jobs, shift);
+        bsel_hist_kernel<<<grid, 256, 0, stream>>>(jobs, njobs, shift);
         bsel_pick_kernel<<<dim3(1, njobs), 32, 0, stream>>>(jobs, shift);
     }
     bsel_apply_kernel<<<dim3(1, njobs), 1, 0, stream>>>(jobs);
-    bcompact_kernel<<<dim3(gx, njobs), 256, 0, stream>>>(jobs);
+    bcompact_kernel<<<grid, 256, 0, stream>>>(jobs, njobs);
     bset_count_kernel<<<dim3(1, njobs), 1, 0, stream>>>(jobs);
     return cudaGetLastError();
 }

@@ -351,10 +351,9 @@ gepi_status gepi_scan_batch_stats(int32_t device, gepi_batch_stats *out);
  * capped at about 4 ms of device time (GEPI_QUANTUM_MS); the requests get
  * their batches -- and the first tiles of the step's work lists -- in policy
  * order, every request at least one tile per step.  GEPI_SERVE_POLICY:
- * "deadline" (the default) orders by submission time + GEPI_SERVE_SLACK
- * (default 1.5) x the request's estimated device time alone, so short
- * requests pass long ones until a long one has waited about 1.5x its own
- * time; "short": least work left first; "oldest": first come, first served.
+ * "short" (the default): least work left first; "deadline": by submission
+ * time + GEPI_SERVE_SLACK (default 1.5) x the request's estimated device time
+ * alone; "oldest": first come, first served.
  * Plane sets submitted to a server must not be used by other calls until
  * their requests are waited for.  No counterpart in the reference (it runs
  * one scan per process). */

@@ -365,37 +365,65 @@ __device__ __forceinline__ uint32_t rowpair_bounds(const float *G0, const float 
     // side carries at most seven float roundings (products below 2^128: t_k^2
     // <= (y z)^2, prod c_l <= (m / 4)^4), so a 1 + 2^-18 factor on the sum keeps
     // the comparison conservative.
+    //
+    // The row pairs (2s+i, 2t) and (2s+i, 2t+1) are computed side by side in
+    // the halves of packed FP32x2 instructions (FFMA2 / FADD2 / FMUL2, rounded
+    // per component as the scalar instructions are), in the same operations
+    // and order as one row pair alone: half the issue slots for the bulk of
+    // the bound, which the scoring warps share with the producers.
     const float th = theta * yzm;
+    const float2 zz = make_float2(z, z), nyy = make_float2(-y, -y), neg1 = make_float2(-1.f, -1.f);
+    const float2 Cj = make_float2(C[0], C[1]), nCj = make_float2(-C[0], -C[1]);
+    const float2 CTj = make_float2(CT[0], CT[1]), nCTj = make_float2(-CT[0], -CT[1]);
+    const float2 slack = make_float2(1.0000038146972656f, 1.0000038146972656f);  // 1 + 2^-18
+    const float2 thh = make_float2(th, th);
     uint32_t ok = 0;
 #pragma unroll
     for (int i = 0; i < 2; ++i) {
+        const float2 a11 = make_float2(G0[i * 3], G0[i * 3 + 1]);
+        const float2 b11 = make_float2(G1[i * 3], G1[i * 3 + 1]);
+        const float2 Ri = make_float2(R[i], R[i]), nRi = make_float2(-R[i], -R[i]);
+        const float2 RTi = make_float2(RT[i], RT[i]);
+        const float mr = m - RT[i];
+        const float2 mri = make_float2(mr, mr);
+        const float2 D11 = __ffma2_rn(b11, nyy, __fmul2_rn(a11, zz));  // a11 z - b11 y
+        const float2 c11 = __fadd2_rn(a11, b11);
+        float2 D[4];
+        D[0] = D11;
+        D[1] = __ffma2_rn(D11, neg1, Ri);                 // R_i - D11
+        D[2] = __ffma2_rn(D11, neg1, Cj);                 // C_j - D11
+        D[3] = __fadd2_rn(__fadd2_rn(D11, nRi), nCj);     // D11 - R_i - C_j
+        const float2 u1 = __ffma2_rn(c11, neg1, RTi);     // RT_i - c11
+        const float2 u2 = __ffma2_rn(c11, neg1, CTj);     // CT_j - c11
+        const float2 u3 = __fadd2_rn(__fadd2_rn(mri, nCTj), c11);  // m - RT_i - CT_j + c11
+        const float2 c0 = make_float2(fmaxf(c11.x, 1.f), fmaxf(c11.y, 1.f));
+        const float2 c1 = make_float2(fmaxf(u1.x, 1.f), fmaxf(u1.y, 1.f));
+        const float2 c2 = make_float2(fmaxf(u2.x, 1.f), fmaxf(u2.y, 1.f));
+        const float2 c3 = make_float2(fmaxf(u3.x, 1.f), fmaxf(u3.y, 1.f));
+        const float2 c01 = __fmul2_rn(c0, c1), c23 = __fmul2_rn(c2, c3);
+        const float2 P[4] = {__fmul2_rn(c1, c23), __fmul2_rn(c0, c23), __fmul2_rn(c3, c01),
+                             __fmul2_rn(c2, c01)};
+        float2 S = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int j = 0; j < 2; ++j) {
-            const float a11 = G0[i * 3 + j], b11 = G1[i * 3 + j];
-            const float D11 = a11 * z - b11 * y, c11 = a11 + b11;
-            const float D[4] = {D11, R[i] - D11, C[j] - D11, D11 - R[i] - C[j]};
-            const float c0 = fmaxf(c11, 1.f), c1 = fmaxf(RT[i] - c11, 1.f),
-                        c2 = fmaxf(CT[j] - c11, 1.f), c3 = fmaxf(m - RT[i] - CT[j] + c11, 1.f);
-            const float c01 = c0 * c1, c23 = c2 * c3;
-            const float P[4] = {c1 * c23, c0 * c23, c3 * c01, c2 * c01};
-            float S = 0.f;
-#pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const float t = fabsf(D[k]) + E;
-                S = fmaf(t * t, P[k], S);
-            }
-            S *= 1.0000038146972656f;  // 1 + 2^-18
-            const float pc = c01 * c23;
-            bool pass;
-            if (objective == 0) {
-                pass = S >= th * pc;
-            } else {
-                // chi^2 itself (one division, its error inside the same factor)
-                const float lo = -m * log1pf(__fdividef(S, pc) / yzm) - lfix;
-                pass = lo - (1e-4f * fabsf(lo) + 1e-2f) <= lp_thr;
-            }
-            ok |= (uint32_t)pass << (2 * i + j);
+        for (int k = 0; k < 4; ++k) {
+            const float2 t = make_float2(fabsf(D[k].x) + E, fabsf(D[k].y) + E);
+            S = __ffma2_rn(__fmul2_rn(t, t), P[k], S);
         }
+        S = __fmul2_rn(S, slack);
+        const float2 pc = __fmul2_rn(c01, c23);
+        bool pass0, pass1;
+        if (objective == 0) {
+            const float2 tp = __fmul2_rn(thh, pc);
+            pass0 = S.x >= tp.x;
+            pass1 = S.y >= tp.y;
+        } else {
+            // chi^2 itself (one division, its error inside the same factor)
+            const float lo0 = -m * log1pf(__fdividef(S.x, pc.x) / yzm) - lfix;
+            const float lo1 = -m * log1pf(__fdividef(S.y, pc.y) / yzm) - lfix;
+            pass0 = lo0 - (1e-4f * fabsf(lo0) + 1e-2f) <= lp_thr;
+            pass1 = lo1 - (1e-4f * fabsf(lo1) + 1e-2f) <= lp_thr;
+        }
+        ok |= ((uint32_t)pass0 | ((uint32_t)pass1 << 1)) << (2 * i);
     }
     return ok & (diag ? 0xDu : 0xFu);
 }

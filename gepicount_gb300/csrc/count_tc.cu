@@ -439,21 +439,25 @@ static __device__ __noinline__ void tc_refine(const ScanCtx &ctx, int rA, int rB
     exact_test(ctx, rA, rB, f, w, x, y, z);
 }
 
-// A 16-bit count as a float: 2^23 + v has v in its low mantissa bits (an ALU
-// or and an FMA-pipe subtract instead of a conversion-unit instruction).
-__device__ __forceinline__ float u16f(uint16_t v) {
-    return __uint_as_float(0x4B000000u | (uint32_t)v) - 8388608.0f;
+// Two 16-bit counts as floats: 2^23 + v has v in its low mantissa bits (an
+// ALU or each and one packed FMA-pipe subtract, exact, instead of two
+// conversion-unit instructions).
+__device__ __forceinline__ float2 u16f2(uint16_t a, uint16_t b) {
+    return __fadd2_rn(make_float2(__uint_as_float(0x4B000000u | (uint32_t)a),
+                                  __uint_as_float(0x4B000000u | (uint32_t)b)),
+                      make_float2(-8388608.0f, -8388608.0f));
 }
 
 // Two accumulator counts (FP32 bit patterns of exact integers below 2^16) as
 // one word of two 16-bit counts, lo | hi << 16: adding 2^23 puts each count in
 // the low mantissa bits (exact, so the rounding mode does not matter), and one
-// byte permute takes the two low halves -- two FMA-pipe adds and one ALU
-// instruction instead of two conversion-unit instructions, a shift and an or.
+// byte permute takes the two low halves -- one packed FMA-pipe add and one
+// ALU instruction instead of two conversion-unit instructions, a shift and an
+// or.
 __device__ __forceinline__ uint32_t pack_counts(uint32_t lo, uint32_t hi) {
-    const uint32_t a = __float_as_uint(__uint_as_float(lo) + 8388608.0f);
-    const uint32_t b = __float_as_uint(__uint_as_float(hi) + 8388608.0f);
-    return __byte_perm(a, b, 0x5410);
+    const float2 ab = __fadd2_rn(make_float2(__uint_as_float(lo), __uint_as_float(hi)),
+                                 make_float2(8388608.0f, 8388608.0f));
+    return __byte_perm(__float_as_uint(ab.x), __float_as_uint(ab.y), 0x5410);
 }
 
 // Count of function f (AND, NAND, ANDN, NANDN, XOR) from n11 and the margins.
@@ -721,8 +725,10 @@ struct TcScorer {
             for (int pp = 0; pp < 3; ++pp)
 #pragma unroll
                 for (int qq = 0; qq < 3; ++qq) {
-                    G[pp * 3 + qq] = u16f(xr[pp * kTcXPitch + qq * kB]);
-                    G[9 + pp * 3 + qq] = u16f(xr[pp * kTcXPitch + 3 * kB + qq * kB]);
+                    const float2 g2 = u16f2(xr[pp * kTcXPitch + qq * kB],
+                                           xr[pp * kTcXPitch + 3 * kB + qq * kB]);  // class 0, 1
+                    G[pp * 3 + qq] = g2.x;
+                    G[9 + pp * 3 + qq] = g2.y;
                 }
             const uint32_t rp = rowpair_bounds(G, G + 9, sA == sBt, OBJ, theta, lp_thr);
             if (!rp) continue;
@@ -1115,8 +1121,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
                 for (int pp = 0; pp < 3; ++pp)
 #pragma unroll
                     for (int qq = 0; qq < 3; ++qq) {
-                        G[pp * 3 + qq] = u16f(xr[pp * kTcXPitch + qq * kB]);
-                        G[9 + pp * 3 + qq] = u16f(xr[pp * kTcXPitch + 3 * kB + qq * kB]);
+                        const float2 g2 = u16f2(xr[pp * kTcXPitch + qq * kB],
+                                               xr[pp * kTcXPitch + 3 * kB + qq * kB]);  // class 0, 1
+                        G[pp * 3 + qq] = g2.x;
+                        G[9 + pp * 3 + qq] = g2.y;
                     }
                 const uint32_t rp = rowpair_bounds(G, G + 9, sA == sBt, OBJ, theta, lp_thr);
                 if (!rp) continue;

@@ -351,14 +351,14 @@ __device__ __forceinline__ uint32_t rowpair_bounds(const float *G0, const float 
     // y z 2^-19 of its exact value (each product is at most y z, and at most
     // four rounded terms enter), the margin E added to |D_k|.
     const float E = yz * 1.9073486328125e-06f;  // 2^-19
-    float R[2], RT[2], C[2], CT[2];
-#pragma unroll
-    for (int i = 0; i < 2; ++i) {
-        R[i] = G0[i * 3 + 2] * z - G1[i * 3 + 2] * y;
-        RT[i] = G0[i * 3 + 2] + G1[i * 3 + 2];
-        C[i] = G0[6 + i] * z - G1[6 + i] * y;
-        CT[i] = G0[6 + i] + G1[6 + i];
-    }
+    const float2 zz = make_float2(z, z), nyy = make_float2(-y, -y), neg1 = make_float2(-1.f, -1.f);
+    // (R_0, R_1), (RT_0, RT_1), (C_0, C_1), (CT_0, CT_1) in packed FP32x2
+    // instructions (rounded per component as the scalar ones are)
+    const float2 aR = make_float2(G0[2], G0[5]), bR = make_float2(G1[2], G1[5]);
+    const float2 aC = make_float2(G0[6], G0[7]), bC = make_float2(G1[6], G1[7]);
+    const float2 R2 = __ffma2_rn(bR, nyy, __fmul2_rn(aR, zz)), RT2 = __fadd2_rn(aR, bR);
+    const float2 Cj = __ffma2_rn(bC, nyy, __fmul2_rn(aC, zz)), CTj = __fadd2_rn(aC, bC);
+    const float R[2] = {R2.x, R2.y}, RT[2] = {RT2.x, RT2.y};
     // S = sum_k t_k^2 / c_k is compared in product form, sum_k t_k^2 P_k with
     // P_k the product of the other three c_l (c_l clamped to 1), against
     // theta y z m prod c_l: no reciprocals.  Every quantity is positive; each
@@ -372,9 +372,7 @@ __device__ __forceinline__ uint32_t rowpair_bounds(const float *G0, const float 
     // and order as one row pair alone: half the issue slots for the bulk of
     // the bound, which the scoring warps share with the producers.
     const float th = theta * yzm;
-    const float2 zz = make_float2(z, z), nyy = make_float2(-y, -y), neg1 = make_float2(-1.f, -1.f);
-    const float2 Cj = make_float2(C[0], C[1]), nCj = make_float2(-C[0], -C[1]);
-    const float2 CTj = make_float2(CT[0], CT[1]), nCTj = make_float2(-CT[0], -CT[1]);
+    const float2 nCj = __fmul2_rn(Cj, neg1), nCTj = __fmul2_rn(CTj, neg1);
     const float2 slack = make_float2(1.0000038146972656f, 1.0000038146972656f);  // 1 + 2^-18
     const float2 thh = make_float2(th, th);
     uint32_t ok = 0;

@@ -381,6 +381,8 @@ __device__ __forceinline__ uint32_t tc_stage1(const ScanCtx &ctx, const float *G
     const float y = G0[8], z = G1[8];
     const float m = y + z, yz = y * z;
     uint32_t mask = 0;
+    // unrolled: constant indices keep the counts in registers
+#pragma unroll
     for (int r = 0; r < 4; ++r) {
         if (!((rp >> r) & 1u)) continue;
         const int i = r >> 1, j = r & 1;
@@ -458,6 +460,15 @@ __device__ __forceinline__ uint32_t pack_counts(uint32_t lo, uint32_t hi) {
     const float2 ab = __fadd2_rn(make_float2(__uint_as_float(lo), __uint_as_float(hi)),
                                  make_float2(8388608.0f, 8388608.0f));
     return __byte_perm(__float_as_uint(ab.x), __float_as_uint(ab.y), 0x5410);
+}
+
+// Cells of row pair (2s+ri, 2t+rj) in one class's 3 x 3 Gram G -- n11 and the
+// two margins -- selected in registers: a runtime index into G would place all
+// of G in local memory, stored on every round.
+__device__ __forceinline__ void gram_cells(const float *G, int ri, int rj, int &n11, int &r, int &c) {
+    n11 = (int)(ri ? (rj ? G[4] : G[3]) : (rj ? G[1] : G[0]));
+    r = (int)(ri ? G[5] : G[2]);
+    c = (int)(rj ? G[7] : G[6]);
 }
 
 // Count of function f (AND, NAND, ANDN, NANDN, XOR) from n11 and the margins.
@@ -738,9 +749,11 @@ struct TcScorer {
                 const int bit = __ffs(mask) - 1;
                 mask &= mask - 1;
                 const int rpi = bit / 5, f = bit - 5 * rpi, ri = rpi >> 1, rj = rpi & 1;
-                const int w = fun_count((int)G[ri * 3 + rj], (int)G[ri * 3 + 2], (int)G[6 + rj], y, f);
-                const int x = fun_count((int)G[9 + ri * 3 + rj], (int)G[9 + ri * 3 + 2],
-                                        (int)G[15 + rj], z, f);
+                int n11, rr, cc;
+                gram_cells(G, ri, rj, n11, rr, cc);
+                const int w = fun_count(n11, rr, cc, y, f);
+                gram_cells(G + 9, ri, rj, n11, rr, cc);
+                const int x = fun_count(n11, rr, cc, z, f);
                 tc_refine<OBJ>(ctx, 2 * sA + ri, 2 * sBt + rj, f, w, x, y, z);
             }
         }
@@ -1134,9 +1147,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
                     const int bit = __ffs(mask) - 1;
                     mask &= mask - 1;
                     const int rpi = bit / 5, f = bit - 5 * rpi, ri = rpi >> 1, rj = rpi & 1;
-                    const int w = fun_count((int)G[ri * 3 + rj], (int)G[ri * 3 + 2], (int)G[6 + rj], y, f);
-                    const int x = fun_count((int)G[9 + ri * 3 + rj], (int)G[9 + ri * 3 + 2],
-                                            (int)G[15 + rj], z, f);
+                    int n11, rr, cc;
+                    gram_cells(G, ri, rj, n11, rr, cc);
+                    const int w = fun_count(n11, rr, cc, y, f);
+                    gram_cells(G + 9, ri, rj, n11, rr, cc);
+                    const int x = fun_count(n11, rr, cc, z, f);
                     tc_refine<OBJ>(ctx, 2 * sA + ri, 2 * sBt + rj, f, w, x, y, z);
                 }
             }

@@ -1185,8 +1185,9 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
 // odd CTA).  A request index < 0 ends the pair's work.
 //
 // Slots are reused without an "empty" barrier because the claimer cannot get
-// kTcRing tiles ahead of the slowest reader: claiming tile K waits for the
-// packed-ring slot of K's first chunk, so the even CTA's producers have loaded
+// kTcRing tiles ahead of the slowest reader: publishing tile K (writing its
+// ring slot) waits for the packed-ring slot of K's first chunk, so the even
+// CTA's producers have loaded
 // chunk g - 4 (g = K's first chunk), hence waited for the MMAs of chunk g - 7,
 // which the MMA thread issued only after both CTAs' producers finished chunk
 // g - 7 and both CTAs' scoring warps released the accumulator of the tile
@@ -1280,17 +1281,28 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
         if (lane == 0) {
             int idx = 0, issued = 0;
             const uint32_t peer_ring = cluster_addr(ring, 1), peer_bar = cluster_addr(ring_bar, 1);
+            // The even CTA claims tile k + 1 (atomic and work-list search) right
+            // after issuing tile k's first copy, so their latency overlaps the
+            // tile's copies; it is published -- as before -- only once the
+            // packed-ring slot of its first chunk is free.
+            int4 claimed = make_int4(-1, 0, 0, 0);
+            bool have_claim = false;
             for (int k = 0;; ++k) {
                 const int slot = k % kTcRing;
                 int4 d;
                 if (rank == 0) {
-                    // claim only once the packed-ring slot of the tile's first chunk is free
+                    // publish only once the packed-ring slot of the tile's first chunk is free
                     const uint32_t j = (uint32_t)idx % kTcPStages;
                     if (!mbar_wait(&S.pempty[j], (((uint32_t)idx / kTcPStages) & 1) ^ 1, S.abort_flag,
                                    S.err, 6, S.budget))
                         break;
-                    const int t = (int)atomicAdd(&q->next, 1u);
-                    d = resolve_work(reqs, q, t);
+                    if (have_claim) {
+                        d = claimed;
+                    } else {
+                        const int t = (int)atomicAdd(&q->next, 1u);
+                        d = resolve_work(reqs, q, t);
+                    }
+                    have_claim = false;
                     ring[slot] = d;
                     asm volatile("st.shared::cluster.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(
                                      peer_ring + (uint32_t)(slot * sizeof(int4))),
@@ -1310,11 +1322,16 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
                 const size_t brow = (size_t)3 * (R.b0 + d.z * kTcBSnps) + kTcBRows * rank;
                 bool ok = true;
                 for (int c = 0; c < cm.nchunks; ++c, ++idx) {
-                    // the even CTA waited for its first chunk's slot before claiming
+                    // the even CTA waited for its first chunk's slot before publishing
                     ok = tc_copy_chunk(tc_smem, S, idx, R.blk, R.rows_pad, c, arow, brow,
                                        !(rank == 0 && c == 0));
                     if (!ok) break;
                     issued = idx + 1;
+                    if (rank == 0 && c == 0) {
+                        const int t = (int)atomicAdd(&q->next, 1u);
+                        claimed = resolve_work(reqs, q, t);
+                        have_claim = true;
+                    }
                 }
                 if (!ok) break;
             }

@@ -19,6 +19,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -137,24 +138,56 @@ void planes_free(gepi_planes *pl) {
     pl->stream = nullptr;
 }
 
+// The scoring tables of a sample count (the fixed-point T(n) table takes
+// milliseconds to build), kept for the process: plane sets of one cohort size
+// -- one per step of an end-to-end loop, or many cohorts of one study -- build
+// them once.  At most kTableCacheBytes are kept; a full cache starts over.
+struct ScoreTables {
+    int F = 0;
+    std::vector<uint64_t> T;
+    std::vector<double> lf;
+    std::vector<float> lf32;
+};
+constexpr size_t kTableCacheBytes = 64ull << 20;
+
+std::shared_ptr<const ScoreTables> score_tables(int64_t nmax) {
+    static std::mutex mu;
+    static std::map<int64_t, std::shared_ptr<const ScoreTables>> cache;
+    static size_t bytes = 0;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find(nmax);
+        if (it != cache.end()) return it->second;
+    }
+    auto t = std::make_shared<ScoreTables>();
+    t->F = tfix_bits(nmax);
+    build_tfix(nmax, t->F, t->T);
+    build_lfact(nmax, t->lf, t->lf32);
+    const size_t b = t->T.size() * 8 + t->lf.size() * 8 + t->lf32.size() * 4;
+    std::lock_guard<std::mutex> lk(mu);
+    if (bytes + b > kTableCacheBytes) {
+        cache.clear();
+        bytes = 0;
+    }
+    if (cache.emplace(nmax, t).second) bytes += b;
+    return t;
+}
+
 gepi_status ensure_tables(gepi_planes *pl) {
     if (pl->d_T) return GEPI_OK;
     const int64_t nmax = (int64_t)pl->S0 + pl->S1;
-    pl->F = tfix_bits(nmax);
-    std::vector<uint64_t> T;
-    build_tfix(nmax, pl->F, T);
-    std::vector<double> lf;
-    std::vector<float> lf32;
-    build_lfact(nmax, lf, lf32);
-    pl->lf_max = (float)lf.back();
-    GEPI_CUDA(pool_alloc(pl->device, &pl->d_T, T.size() * 8, pl->stream));
-    GEPI_CUDA(pool_alloc(pl->device, &pl->d_lf, lf.size() * 8, pl->stream));
-    GEPI_CUDA(pool_alloc(pl->device, &pl->d_lf32, lf32.size() * 4, pl->stream));
-    GEPI_CUDA(cudaMemcpyAsync(pl->d_T, T.data(), T.size() * 8, cudaMemcpyHostToDevice, pl->stream));
-    GEPI_CUDA(cudaMemcpyAsync(pl->d_lf, lf.data(), lf.size() * 8, cudaMemcpyHostToDevice, pl->stream));
-    GEPI_CUDA(cudaMemcpyAsync(pl->d_lf32, lf32.data(), lf32.size() * 4, cudaMemcpyHostToDevice,
+    const std::shared_ptr<const ScoreTables> t = score_tables(nmax);
+    pl->F = t->F;
+    pl->lf_max = (float)t->lf.back();
+    GEPI_CUDA(pool_alloc(pl->device, &pl->d_T, t->T.size() * 8, pl->stream));
+    GEPI_CUDA(pool_alloc(pl->device, &pl->d_lf, t->lf.size() * 8, pl->stream));
+    GEPI_CUDA(pool_alloc(pl->device, &pl->d_lf32, t->lf32.size() * 4, pl->stream));
+    GEPI_CUDA(cudaMemcpyAsync(pl->d_T, t->T.data(), t->T.size() * 8, cudaMemcpyHostToDevice, pl->stream));
+    GEPI_CUDA(cudaMemcpyAsync(pl->d_lf, t->lf.data(), t->lf.size() * 8, cudaMemcpyHostToDevice,
                               pl->stream));
-    GEPI_CUDA(cudaStreamSynchronize(pl->stream));  // the host tables go out of scope
+    GEPI_CUDA(cudaMemcpyAsync(pl->d_lf32, t->lf32.data(), t->lf32.size() * 4, cudaMemcpyHostToDevice,
+                              pl->stream));
+    GEPI_CUDA(cudaStreamSynchronize(pl->stream));  // `t` may leave the cache once this returns
     return GEPI_OK;
 }
 
@@ -566,7 +599,16 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
     GEPI_TRY(resolve_variant(pl, par->method, par->variant, &cv));
     if (cv->method == GEPI_METHOD_TENSOR) GEPI_TRY(ensure_tc_blocks(pl));
     const int TA = cv->ta, TB = cv->tb;
-    std::vector<int2> tiles;
+    // kept per thread (a fresh 8 MB list per scan, config 3, costs page
+    // faults); a scan started from a progress callback of another gets its own
+    static thread_local std::vector<int2> tile_buf;
+    static thread_local int depth = 0;
+    struct Depth {
+        int &d;
+        ~Depth() { --d; }
+    } nested{++depth};
+    std::vector<int2> own;
+    std::vector<int2> &tiles = depth == 1 ? tile_buf : own;
     // progress snapshots cover band prefixes, so they keep the band order
     GEPI_TRY(pl_scan_tiles(pl, a0, a0 + na, b0, b0 + nb, TA, TB, !(prog && prog->fn), tiles));
     GEPI_TRY(upload_tiles(pl, tiles));

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -162,6 +163,11 @@ struct gepi_planes {
     void *d_sel = nullptr;
     int2 *d_tiles = nullptr;
     size_t tiles_cap = 0;
+    // the scan tile list d_tiles holds (ranges, tile shape, hot-first order);
+    // any other upload of d_tiles clears tiles_valid
+    bool tiles_valid = false;
+    std::array<int64_t, 7> tiles_key{};
+    size_t tiles_n = 0;
     std::vector<cudaEvent_t> ev;  // timing events, reused across scans
     gepi_scan_stats stats{};
     std::vector<double> last_values;  // FP64 objective of the last ranked list (gepi_last_scan_values)

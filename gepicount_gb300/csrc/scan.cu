@@ -220,6 +220,7 @@ gepi_status ensure_scan_buffers(gepi_planes *pl, int k) {
 }
 
 gepi_status upload_tiles(gepi_planes *pl, const std::vector<int2> &tiles) {
+    pl->tiles_valid = false;
     if (tiles.size() > pl->tiles_cap) {
         pool_free(pl->d_tiles, pl->stream);
         GEPI_CUDA(pool_alloc(pl->device, &pl->d_tiles, tiles.size() * sizeof(int2), pl->stream));
@@ -609,16 +610,31 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
     } nested{++depth};
     std::vector<int2> own;
     std::vector<int2> &tiles = depth == 1 ? tile_buf : own;
-    // progress snapshots cover band prefixes, so they keep the band order
-    GEPI_TRY(pl_scan_tiles(pl, a0, a0 + na, b0, b0 + nb, TA, TB, !(prog && prog->fn), tiles));
-    GEPI_TRY(upload_tiles(pl, tiles));
+    // progress snapshots cover band prefixes, so they keep the band order (and
+    // need the list on the host); other scans reuse the list already on the
+    // device when the ranges and tile shape repeat
+    const bool hot = !(prog && prog->fn);
+    const std::array<int64_t, 7> tkey{a0, (int64_t)a0 + na, b0, (int64_t)b0 + nb, TA, TB, hot ? 1 : 0};
+    size_t ntiles = 0;
+    if (hot && pl->tiles_valid && pl->tiles_key == tkey) {
+        ntiles = pl->tiles_n;
+    } else {
+        GEPI_TRY(pl_scan_tiles(pl, a0, a0 + na, b0, b0 + nb, TA, TB, hot, tiles));
+        GEPI_TRY(upload_tiles(pl, tiles));
+        ntiles = tiles.size();
+        if (hot) {
+            pl->tiles_valid = true;
+            pl->tiles_key = tkey;
+            pl->tiles_n = ntiles;
+        }
+    }
     GEPI_TRY(ensure_events(pl, 4));
     gepi_scan_stats &S = pl->stats;
     S = gepi_scan_stats{};
     S.method = cv->method;
     S.tile_snps = TA;
     S.variant = cv->id;
-    S.tiles = tiles.size();
+    S.tiles = ntiles;
     {
         // pairs (s, t), t < s, s in A, t in B; and SNPs in both ranges
         const int64_t ia0 = a0, ia1 = (int64_t)a0 + na, ib0 = b0, ib1 = (int64_t)b0 + nb;
@@ -656,7 +672,6 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
     ctx.cap = pl->cap;
     ctx.st = pl->d_state;
 
-    const size_t ntiles = tiles.size();
     const double tests_per_tile = 20.0 * TA * TB;
     const uint32_t budget = select_budget(pl->cap, k);
     const uint32_t trigger = select_trigger(budget, k);

@@ -171,6 +171,16 @@ def test_scan_is_deterministic_and_method_independent(gepi, tmp_path):
     b = pl.scan(500, method=1)
     c = pl.scan(500, method=2)
     assert a.tobytes() == b.tobytes() == c.tobytes()
+    # the plane set keeps its last scan tile list: repeats reuse it, other
+    # ranges, tile shapes and uploads (pair counts, autotuning) replace it
+    N = fs.n_lines
+    r1 = pl.scan_range(40, 200, 10, 150, 300, method=2)
+    assert_same_topk(r1, H.oracle_topk_range(rows, 80, 480, 20, 320, 300)[0])
+    assert pl.scan(500, method=2).tobytes() == a.tobytes()
+    assert np.array_equal(pl.pair_counts(0, N, 0, N, method=2), H.oracle_pair_gram(rows, 0, N, 0, N))
+    assert pl.scan(500, method=2).tobytes() == a.tobytes()
+    assert pl.scan_range(40, 200, 10, 150, 300, method=2).tobytes() == r1.tobytes()
+    assert pl.scan(500, method=1).tobytes() == a.tobytes()
     pl.close()
 
 

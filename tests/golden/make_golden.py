@@ -34,7 +34,7 @@ import gepicount_gb300 as g  # noqa: E402
 from helpers import parse_ranked  # noqa: E402
 
 SYNTH_CASES = {
-    # BASELINE config-1 shape: 1,024 SNPs x 512 samples (256/256), MAF U(0.05,0.5), 2% missing
+    # config-1 shape: 1,024 SNPs x 512 samples (256/256), MAF U(0.05,0.5), 2% missing
     "cfg1": (dict(n_snps=1024, n_cases=256, n_controls=256, maf_lo=0.05, maf_hi=0.5,
                   missing=0.02, seed=1001), 100),
     # config-2 generator (MAF U(0.01,0.5), 1% missing, 3 planted pairs) at 1,000 SNPs x 4,000

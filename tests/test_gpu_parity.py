@@ -361,7 +361,7 @@ def test_device_fisher_fp64_config2_full_size(gepi):
 
 
 def test_config2_scale_properties(gepi):
-    """BASELINE config 2 (20,000 SNPs x 4,000 samples, 3 planted pairs, top
+    """Config 2 (20,000 SNPs x 4,000 samples, 3 planted pairs, top
     1,000): size-independent checks -- every returned count and key is the
     oracle's, the list is sorted under the tie-break, and no sampled test beats
     the k-th entry without being listed."""

@@ -309,9 +309,11 @@ constexpr size_t kHotMinTiles = 4096;  // smaller scans keep the band order
 void scan_tile_order(int a0, int a1, int b0, int b1, int TA, int TB, int band,
                      const std::vector<int> &hot_a, const std::vector<int> &hot_b,
                      std::vector<int2> &out) {
-    out.clear();
     const int nat = (a1 - a0 + TA - 1) / TA, nbt = (b1 - b0 + TB - 1) / TB;
-    if (nat <= 0 || nbt <= 0) return;
+    if (nat <= 0 || nbt <= 0) {
+        out.clear();
+        return;
+    }
     if (band < 1) band = 1;
     // B tiles j < jend[i] pair with A tile i (t <= s somewhere in the tile)
     std::vector<int> jend((size_t)nat);
@@ -322,7 +324,9 @@ void scan_tile_order(int a0, int a1, int b0, int b1, int TA, int TB, int band,
         jend[(size_t)i] = std::min(nbt, e);
         total += (size_t)jend[(size_t)i];
     }
-    out.resize(total);
+    // grown only when too small (a reused buffer is then not cleared: every
+    // entry kept is written below), shrunk to the tiles written at the end
+    if (out.size() < total) out.resize(total);
     int2 *w = out.data();
     std::vector<char> isa((size_t)nat, 0), isb((size_t)nbt, 0);
     for (int i : hot_a) isa[(size_t)i] = 1;
@@ -930,16 +934,17 @@ gepi_status gepi_planes_from_bed(const uint8_t *bed, size_t bed_bytes, int n_bim
     if (st != GEPI_OK) return fail(st);
     std::vector<int32_t> perm;
     build_perm(c0, c1, pl->W0, pl->Wp, perm);
-    const size_t payload = bed_bytes - 3;
-    if ((st = check_mem(payload + perm.size() * 4, ".bed staging")) != GEPI_OK) return fail(st);
-    if (pool_alloc(device, &d_bed, payload, pl->stream) != cudaSuccess ||
+    // the whole file image is copied (with its 3-byte header) so that the
+    // copy starts where the caller's buffer does, usually on a page boundary
+    if ((st = check_mem(bed_bytes + perm.size() * 4, ".bed staging")) != GEPI_OK) return fail(st);
+    if (pool_alloc(device, &d_bed, bed_bytes, pl->stream) != cudaSuccess ||
         pool_alloc(device, &d_perm, perm.size() * 4, pl->stream) != cudaSuccess)
         return fail(set_error(GEPI_ERR_OOM, ".bed staging allocation failed"));
-    cudaError_t e = cudaMemcpyAsync(d_bed, bed + 3, payload, cudaMemcpyHostToDevice, pl->stream);
+    cudaError_t e = cudaMemcpyAsync(d_bed, bed, bed_bytes, cudaMemcpyHostToDevice, pl->stream);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(d_perm, perm.data(), perm.size() * 4, cudaMemcpyHostToDevice, pl->stream);
     if (e == cudaSuccess)
-        e = launch_decode_bed(d_bed, bps, n_bim_snps, d_perm, pl->Wp, pl->d_planes, pl->stream);
+        e = launch_decode_bed(d_bed + 3, bps, n_bim_snps, d_perm, pl->Wp, pl->d_planes, pl->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(pl->stream);
     if (e != cudaSuccess)
         return fail(set_error(GEPI_ERR_CUDA, std::string("decode: ") + cudaGetErrorString(e)));

@@ -268,6 +268,48 @@ __device__ inline double fisher_lnp(const double *__restrict__ lf, int n11, int 
     return lnp > 0.0 ? 0.0 : lnp;
 }
 
+// A lower bound on the p of fisher_lnp, against a threshold: true when the
+// observed term and up to 8 terms beyond it on its own side of the mode --
+// each at most P(obs), the hypergeometric being unimodal, so each is in the
+// sum -- already show ln p > ln_thr.  Such a test cannot reach the ranking,
+// and the exact tail sums it would cost are skipped.  The terms are walked
+// with the term ratio in FP32 and only counted while below 1 - 1e-5 of
+// P(obs); the sum is taken 1e-5 low and its log 1e-5 low, and the comparison
+// keeps a margin of 1e-7 + 1e-10 |ln_thr| nats, far above the rounding of
+// fisher_lnp, so the tests it drops are tests the exact evaluation drops.
+__device__ inline bool fisher_above(const double *__restrict__ lf, int n11, int n12, int n21,
+                                    int n22, double ln_thr) {
+    if (!(ln_thr < 0.0)) return false;  // no threshold yet
+    const int r1 = n11 + n21, r2 = n12 + n22, c1 = n11 + n12, N = r1 + r2;
+    const int lo = c1 <= r2 ? 0 : c1 - r2;
+    const int hi = c1 < r1 ? c1 : r1;
+    if (lo >= hi) return false;
+    const double lpo = __ldg(lf + r1) + __ldg(lf + r2) + __ldg(lf + c1) + __ldg(lf + (N - c1)) -
+                       __ldg(lf + N) - __ldg(lf + n11) - __ldg(lf + (r1 - n11)) -
+                       __ldg(lf + (c1 - n11)) - __ldg(lf + (r2 - c1 + n11));
+    const double margin = 1e-7 + 1e-10 * -ln_thr;
+    const double d = ln_thr + margin - lpo;  // reject when ln(sum of the terms) > d
+    if (d > 2.25) return false;              // 9 terms sum to at most 9 < e^2.25
+    auto up = [&](int x) {
+        return ((float)(r1 - x) * (float)(c1 - x)) / ((float)(x + 1) * (float)(r2 - c1 + x + 1));
+    };
+    auto down = [&](int x) {
+        return ((float)x * (float)(r2 - c1 + x)) / ((float)(r1 - x + 1) * (float)(c1 - x + 1));
+    };
+    float S = 1.f, t = 1.f;
+    const bool toward_hi = n11 < hi && up(n11) < 1.f;
+    int x = n11;
+#pragma unroll 1
+    for (int j = 0; j < 8; ++j) {
+        if (toward_hi ? x >= hi : x <= lo) break;
+        t *= toward_hi ? up(x) : down(x);
+        if (!(t < 1.f - 1e-5f)) break;  // not below P(obs): the mode's side
+        S += t;
+        x += toward_hi ? 1 : -1;
+    }
+    return (double)__logf(S * (1.f - 1e-5f)) - 1e-5 > d;
+}
+
 __device__ __forceinline__ void append_candidate(const ScanCtx &ctx, double value, int rA,
                                                  int rB, int fun, int w, int x, int y, int z) {
     unsigned long long key = key_of(value);
@@ -316,7 +358,10 @@ static __device__ __noinline__ void exact_test(const ScanCtx &ctx, int rA, int r
         if (lhs < ctx.st->tau_val * (double)m * scalbn(1.0, ctx.F) * (1.0 - 1e-12)) return;
         value = scalbn(lhs, -ctx.F) / (double)m;
     } else {
-        // print order (w, y-w, x, z-x); value = -log10 p
+        // print order (w, y-w, x, z-x); value = -log10 p, appended when
+        // value >= tau_val, i.e. ln p <= -tau_val ln 10
+        if (fisher_above(ctx.lf, w, y - w, x, z - x, -ctx.st->tau_val * 2.302585092994045684))
+            return;
         value = -fisher_lnp(ctx.lf, w, y - w, x, z - x) * 0.43429448190325182765;
     }
     append_candidate(ctx, value, rA, rB, fun, w, x, y, z);

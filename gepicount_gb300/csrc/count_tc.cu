@@ -120,7 +120,11 @@ constexpr uint32_t kTcIdesc = (1u << 7) | (1u << 10)           // A, B = E2M1
                               | ((uint32_t)(256 >> 4) << 24);  // M (the pair)
 constexpr size_t kTcPOff = kTcStages * (size_t)kTcBStageBytes;               // packed ring
 constexpr size_t kTcXOff = kTcPOff + kTcPStages * (size_t)kTcPStageBytes;    // exchange rows
-constexpr size_t kTcSmem = kTcXOff + (size_t)kTcEpiWarps * 32 * kTcXPitch * 2;
+// Fisher: each scoring warp queues the tests that pass its bounds (16 bytes
+// each) and evaluates them 32 at a time, one per lane
+constexpr int kTcQCap = 64;
+constexpr size_t kTcQOff = (kTcXOff + (size_t)kTcEpiWarps * 32 * kTcXPitch * 2 + 15) / 16 * 16;
+constexpr size_t kTcSmem = kTcQOff + (size_t)kTcEpiWarps * kTcQCap * 16;
 static_assert(kTcSfCol + 32 <= kTcCols, "tensor memory budget");
 static_assert(kTcBWarps * 32 == 2 * kTcBRows && kTcBWarps <= kTcProducerWarps, "B pieces");
 static_assert(kTcHalfWords == 4 || kTcHalfWords == 6,
@@ -632,12 +636,14 @@ struct TcScorer {
     static constexpr int kB = 8 * kTcEpiGroups;  // B SNPs of the warp: 32
     int eh, aoff;
     uint16_t *xh;
+    uint4 *qb;  // Fisher: this warp's queue of tests for exact evaluation
     uint32_t tq;
     __device__ __forceinline__ TcScorer(unsigned char *smem, uint32_t tbase, int warp, uint32_t rank) {
         const int q = warp & 3;
         const int ew = warp - kTcEpiWarp0;
         eh = ew >> 2;
         xh = reinterpret_cast<uint16_t *>(smem + kTcXOff) + (size_t)ew * 32 * kTcXPitch;
+        qb = reinterpret_cast<uint4 *>(smem + kTcQOff) + (size_t)ew * kTcQCap;
         aoff = kTcASnps * (int)rank + 10 * q;  // this warp's first A SNP in the tile
         tq = tbase + ((uint32_t)(32 * q) << 16) + 3 * kB * eh;
     }
@@ -695,35 +701,75 @@ struct TcScorer {
             return true;
         }
         const int sBt = sB0 + lane;
+        int fill = 0;  // Fisher queue entries (warp-uniform)
+        // Fisher: the queued tests, one per lane, then the queue is empty
+        auto drain = [&]() {
+            __syncwarp();
+            for (int i = lane; i < fill; i += 32) {
+                const uint4 e = qb[i];
+                exact_test(ctx, (int)e.x, (int)(e.y >> 3), (int)(e.y & 7u), (int)(e.z & 0xFFFFu),
+                           (int)(e.z >> 16), (int)(e.w & 0xFFFFu), (int)(e.w >> 16));
+            }
+            __syncwarp();
+            fill = 0;
+        };
         for (int r = 0; r < 10; ++r) {
             const int sA = sAq + r;
-            if (!(sA < a1 && sBt < b1 && sBt <= sA)) continue;
-            const uint16_t *xr = xh + 3 * r * kTcXPitch + lane;
             float G[18];
+            uint32_t mask = 0;
+            if (sA < a1 && sBt < b1 && sBt <= sA) {
+                const uint16_t *xr = xh + 3 * r * kTcXPitch + lane;
 #pragma unroll
-            for (int pp = 0; pp < 3; ++pp)
+                for (int pp = 0; pp < 3; ++pp)
 #pragma unroll
-                for (int qq = 0; qq < 3; ++qq) {
-                    const float2 g2 = u16f2(xr[pp * kTcXPitch + qq * kB],
-                                           xr[pp * kTcXPitch + 3 * kB + qq * kB]);  // class 0, 1
-                    G[pp * 3 + qq] = g2.x;
-                    G[9 + pp * 3 + qq] = g2.y;
+                    for (int qq = 0; qq < 3; ++qq) {
+                        const float2 g2 = u16f2(xr[pp * kTcXPitch + qq * kB],
+                                               xr[pp * kTcXPitch + 3 * kB + qq * kB]);  // class 0, 1
+                        G[pp * 3 + qq] = g2.x;
+                        G[9 + pp * 3 + qq] = g2.y;
+                    }
+                const uint32_t rp = rowpair_bounds(G, G + 9, sA == sBt, OBJ, theta, lp_thr);
+                if (rp) mask = tc_stage1<OBJ>(ctx, G, G + 9, rp, theta, lp_thr);
+            }
+            // Fisher: the tests that passed go to the warp's queue (their exact
+            // tail sums then run 32 at a time, one per lane, instead of on the
+            // one or two lanes whose tests passed); a round with more than the
+            // queue holds (no threshold yet) evaluates in place
+            bool queue = false;
+            int pos = 0;
+            if constexpr (OBJ == 1) {
+                const int n = __popc(mask);
+                int incl = n;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+                    if (lane >= o) incl += v;
                 }
-            const uint32_t rp = rowpair_bounds(G, G + 9, sA == sBt, OBJ, theta, lp_thr);
-            if (!rp) continue;
-            uint32_t mask = tc_stage1<OBJ>(ctx, G, G + 9, rp, theta, lp_thr);
-            const int y = (int)G[8], z = (int)G[17];
+                const int total = __shfl_sync(0xffffffffu, incl, 31);
+                if (total > 0 && fill + total > kTcQCap) drain();
+                queue = total > 0 && total <= kTcQCap;
+                pos = fill + incl - n;
+                if (queue) fill += total;
+            }
             while (mask) {
                 const int bit = __ffs(mask) - 1;
                 mask &= mask - 1;
                 const int rpi = bit / 5, f = bit - 5 * rpi, ri = rpi >> 1, rj = rpi & 1;
+                const int y = (int)G[8], z = (int)G[17];
                 int n11, rr, cc;
                 gram_cells(G, ri, rj, n11, rr, cc);
                 const int w = fun_count(n11, rr, cc, y, f);
                 gram_cells(G + 9, ri, rj, n11, rr, cc);
                 const int x = fun_count(n11, rr, cc, z, f);
-                tc_refine<OBJ>(ctx, 2 * sA + ri, 2 * sBt + rj, f, w, x, y, z);
+                if (queue)
+                    qb[pos++] = make_uint4((uint32_t)(2 * sA + ri), (uint32_t)(2 * sBt + rj) << 3 | (uint32_t)f,
+                                           (uint32_t)w | (uint32_t)x << 16, (uint32_t)y | (uint32_t)z << 16);
+                else
+                    tc_refine<OBJ>(ctx, 2 * sA + ri, 2 * sBt + rj, f, w, x, y, z);
             }
+        }
+        if constexpr (OBJ == 1) {
+            if (fill > 0) drain();
         }
         __syncwarp();
         return true;
@@ -1022,108 +1068,17 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(kTcThreads, 1)
         __syncwarp();
     } else {
         // ---------------- epilogue (warps 10-17) ----------------
-        const int q = warp & 3;                   // TMEM lane quarter
-        const int ew = warp - kTcEpiWarp0;        // 0..7
-        const int eh = ew >> 2;                   // B SNPs 32 eh .. 32 eh + 31
-        // this warp's accumulator region as 16-bit counts: row = TMEM lane,
-        // [group 0: class 0 (24), class 1 (24) | group 1: ...] (odd word pitch)
-        // this warp's accumulator region as 16-bit counts: row = TMEM lane (plane
-        // p of A SNP i at row 3i + p), laid out [class][B plane qq][B SNP jl] so
-        // that the 32 lanes reading one plane pair of 32 B SNPs hit 16
-        // consecutive words (odd word pitch: the copy-out is conflict-free too)
-        uint16_t *xh = reinterpret_cast<uint16_t *>(tc_smem + kTcXOff) + (size_t)ew * 32 * kTcXPitch;
+        const TcSync S{pfull_bar, pempty_bar, full_bar, empty_bar, dfull_bar, dempty_bar,
+                       vabort,    err,        budget};
+        const TcScorer E(tc_smem, tbase, warp, rank);
         const float theta = DUMP ? 0.f : ctx.st->theta;
         const float lp_thr = DUMP ? 0.f : ctx.st->lp_thr;
-        const int aoff = kTcASnps * (int)rank + 10 * q;  // this warp's first A SNP in the tile
-        constexpr int kB = 8 * kTcEpiGroups;             // B SNPs of the warp: 32
         uint32_t lt = 0;
-        bool live = true;
-        for (int t = pair; t < ntiles && live; t += npairs, ++lt) {
+        for (int t = pair; t < ntiles; t += npairs, ++lt) {
             const int2 tl = tiles[t];
-            const int sAq = a0 + tl.x * kTcPairASnps + aoff;  // A SNP 0 of the lane quarter
-            const int sB0 = b0 + tl.y * kTcBSnps + kB * eh;
-            const uint32_t tq = tbase + ((uint32_t)(32 * q) << 16) + 3 * kB * eh;
-            // copy each class half out as soon as its MMAs are done and hand it
-            // back: the tensor pipe goes on with the other half, then the next tile
-            for (int cls = 0; cls < 2; ++cls) {
-                if (!mbar_wait_warp(&dfull_bar[cls], lt & 1, vabort, err, 4, budget)) {
-                    live = false;
-                    break;
-                }
-                tc_fence_after();
-                uint32_t *rw = reinterpret_cast<uint32_t *>(xh + lane * kTcXPitch) + cls * (3 * kB / 2);
-#pragma unroll
-                for (int gl = 0; gl < kTcEpiGroups; ++gl) {
-                    uint32_t v[24];  // column 3 jl' + qq of B SNPs 8 gl + jl'
-                    tmem_ld16(tq + cls * kTcN + 24 * gl, *reinterpret_cast<uint32_t(*)[16]>(v));
-                    tmem_ld8(tq + cls * kTcN + 24 * gl + 16, *reinterpret_cast<uint32_t(*)[8]>(v + 16));
-                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-                    for (int qq = 0; qq < 3; ++qq)
-#pragma unroll
-                        for (int m = 0; m < 4; ++m)
-                            rw[qq * (kB / 2) + 4 * gl + m] =
-                                pack_counts(v[6 * m + qq], v[6 * m + 3 + qq]);
-                }
-                tc_fence_before();
-                __syncwarp();
-                mbar_arrive_warp_cl(cluster_addr(&dempty_bar[cls], 0));
-            }
-            if (!live) break;
-            __syncwarp();
-            if constexpr (DUMP) {
-                const int i = lane / 3, p = lane % 3, sA = sAq + i;
-                if (lane < 30 && sA < a1) {
-                    const uint16_t *xr = xh + lane * kTcXPitch;
-                    for (int jb = 0; jb < kB; ++jb) {
-                        const int sBt = sB0 + jb;
-                        if (sBt >= b1) continue;
-                        uint32_t *o = dump + ((size_t)(sA - a0) * (b1 - b0) + (sBt - b0)) * 18;
-#pragma unroll
-                        for (int qq = 0; qq < 3; ++qq) {
-                            o[p * 3 + qq] = xr[qq * kB + jb];
-                            o[9 + p * 3 + qq] = xr[3 * kB + qq * kB + jb];
-                        }
-                    }
-                }
-                __syncwarp();
-                continue;
-            }
-            // Round r bounds the pairs (A SNP r of the quarter, B SNP lane) per row
-            // pair; the rare lane whose bound passes runs the per-test bounds and
-            // the out-of-line refinement on the counts it holds.
-            const int sBt = sB0 + lane;
-            for (int r = 0; r < 10; ++r) {
-                const int sA = sAq + r;
-                if (!(sA < a1 && sBt < b1 && sBt <= sA)) continue;
-                const uint16_t *xr = xh + 3 * r * kTcXPitch + lane;
-                float G[18];
-#pragma unroll
-                for (int pp = 0; pp < 3; ++pp)
-#pragma unroll
-                    for (int qq = 0; qq < 3; ++qq) {
-                        const float2 g2 = u16f2(xr[pp * kTcXPitch + qq * kB],
-                                               xr[pp * kTcXPitch + 3 * kB + qq * kB]);  // class 0, 1
-                        G[pp * 3 + qq] = g2.x;
-                        G[9 + pp * 3 + qq] = g2.y;
-                    }
-                const uint32_t rp = rowpair_bounds(G, G + 9, sA == sBt, OBJ, theta, lp_thr);
-                if (!rp) continue;
-                uint32_t mask = tc_stage1<OBJ>(ctx, G, G + 9, rp, theta, lp_thr);
-                const int y = (int)G[8], z = (int)G[17];
-                while (mask) {
-                    const int bit = __ffs(mask) - 1;
-                    mask &= mask - 1;
-                    const int rpi = bit / 5, f = bit - 5 * rpi, ri = rpi >> 1, rj = rpi & 1;
-                    int n11, rr, cc;
-                    gram_cells(G, ri, rj, n11, rr, cc);
-                    const int w = fun_count(n11, rr, cc, y, f);
-                    gram_cells(G + 9, ri, rj, n11, rr, cc);
-                    const int x = fun_count(n11, rr, cc, z, f);
-                    tc_refine<OBJ>(ctx, 2 * sA + ri, 2 * sBt + rj, f, w, x, y, z);
-                }
-            }
-            __syncwarp();
+            if (!E.template tile<DUMP, OBJ>(S, lane, lt, tl.x, tl.y, a0, a1, b0, b1, ctx, theta, lp_thr,
+                                            dump))
+                break;
         }
     }
 

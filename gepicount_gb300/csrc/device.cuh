@@ -157,6 +157,35 @@ __device__ __forceinline__ double exact_mi(const uint64_t *__restrict__ T, int F
     return scalbn((double)(long long)num, -F) / (double)m;
 }
 
+// The sum of a tail walk, t_{j+1} = t_j * n(x) / d(x), x stepping by `dir`
+// from x0 while x stays in (lo_excl, hi_excl): S0 plus every term, stopping
+// once a term adds < 1e-17 of the sum.  No division per term: the terms and
+// their sum are kept over one common denominator (tn / td, sn / td), folded
+// back every 16 terms (two divisions): each numerator or denominator factor is
+// a product of two counts below 2^31, so 16 of them stay below 2^1024.
+template <class Ratio>
+__device__ inline double fisher_walk(double S0, double t0, int x0, int dir, int x_end,
+                                     Ratio ratio) {
+    double S = S0, tn = t0, td = 1.0, sn = 0.0;
+    int x = x0;
+    for (int j = 1; x != x_end; ++j) {
+        double n, d;
+        ratio(x, n, d);
+        x += dir;
+        tn *= n;
+        td *= d;
+        sn = fma(sn, d, tn);
+        if (tn < 1e-17 * fma(S, td, sn)) break;
+        if ((j & 15) == 0) {
+            S += sn / td;
+            tn /= td;
+            sn = 0.0;
+            td = 1.0;
+        }
+    }
+    return S + sn / td;
+}
+
 // Two-sided Fisher exact test for the table (n11 n12 / n21 n22), natural-log
 // p-value.  Terms with P(x) <= P(obs) * (1 + 1e-7) are summed (R's rule).  The
 // observed term is anchored with the log-factorial table; the hypergeometric
@@ -179,12 +208,25 @@ __device__ inline double fisher_lnp(const double *__restrict__ lf, int n11, int 
         return K - __ldg(lf + x) - __ldg(lf + (r1 - x)) - __ldg(lf + (c1 - x)) -
                __ldg(lf + (r2 - c1 + x));
     };
-    // P(x+1)/P(x) and P(x-1)/P(x)
+    // P(x+1)/P(x) and P(x-1)/P(x), as numerator and denominator (products of
+    // two counts)
+    auto up_nd = [&](int x, double &n, double &d) {
+        n = (double)(r1 - x) * (double)(c1 - x);
+        d = (double)(x + 1) * (double)(r2 - c1 + x + 1);
+    };
+    auto down_nd = [&](int x, double &n, double &d) {
+        n = (double)x * (double)(r2 - c1 + x);
+        d = (double)(r1 - x + 1) * (double)(c1 - x + 1);
+    };
     auto up = [&](int x) {
-        return ((double)(r1 - x) * (double)(c1 - x)) / ((double)(x + 1) * (double)(r2 - c1 + x + 1));
+        double n, d;
+        up_nd(x, n, d);
+        return n / d;
     };
     auto down = [&](int x) {
-        return ((double)x * (double)(r2 - c1 + x)) / ((double)(r1 - x + 1) * (double)(c1 - x + 1));
+        double n, d;
+        down_nd(x, n, d);
+        return n / d;
     };
     const double tol = 1.0 + 1e-7;
     const int xo = n11;
@@ -196,15 +238,9 @@ __device__ inline double fisher_lnp(const double *__restrict__ lf, int n11, int 
     double S = 1.0;
     if (xo <= xm) {
         // near tail: x < xo
-        double t = 1.0;
-        for (int x = xo; x > lo;) {
-            t *= down(x);
-            --x;
-            S += t;
-            if (t < 1e-17 * S) break;
-        }
+        S = fisher_walk(S, 1.0, xo, -1, lo, down_nd);
         // plateau between xo and the mode
-        t = 1.0;
+        double t = 1.0;
         for (int x = xo; x < xm;) {
             double t2 = t * up(x);
             if (t2 > tol) break;
@@ -220,25 +256,13 @@ __device__ inline double fisher_lnp(const double *__restrict__ lf, int n11, int 
                 int mid = (l + h) >> 1;
                 if (lpx(mid) <= lim) h = mid; else l = mid + 1;
             }
-            double u = exp(lpx(l) - lpo);
-            S += u;
-            for (int x = l; x < hi;) {
-                u *= up(x);
-                ++x;
-                S += u;
-                if (u < 1e-17 * S) break;
-            }
+            const double u = exp(lpx(l) - lpo);
+            S = fisher_walk(S + u, u, l, +1, hi, up_nd);
         }
     } else {
         // near tail: x > xo
+        S = fisher_walk(S, 1.0, xo, +1, hi, up_nd);
         double t = 1.0;
-        for (int x = xo; x < hi;) {
-            t *= up(x);
-            ++x;
-            S += t;
-            if (t < 1e-17 * S) break;
-        }
-        t = 1.0;
         for (int x = xo; x > xm;) {
             double t2 = t * down(x);
             if (t2 > tol) break;
@@ -254,14 +278,8 @@ __device__ inline double fisher_lnp(const double *__restrict__ lf, int n11, int 
                 int mid = (l + h + 1) >> 1;
                 if (lpx(mid) <= lim) l = mid; else h = mid - 1;
             }
-            double u = exp(lpx(l) - lpo);
-            S += u;
-            for (int x = l; x > lo;) {
-                u *= down(x);
-                --x;
-                S += u;
-                if (u < 1e-17 * S) break;
-            }
+            const double u = exp(lpx(l) - lpo);
+            S = fisher_walk(S + u, u, l, -1, lo, down_nd);
         }
     }
     double lnp = lpo + log(S);

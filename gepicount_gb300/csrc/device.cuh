@@ -158,16 +158,23 @@ __device__ __forceinline__ double exact_mi(const uint64_t *__restrict__ T, int F
 }
 
 // The sum of a tail walk, t_{j+1} = t_j * n(x) / d(x), x stepping by `dir`
-// from x0 while x stays in (lo_excl, hi_excl): S0 plus every term, stopping
-// once a term adds < 1e-17 of the sum.  No division per term: the terms and
-// their sum are kept over one common denominator (tn / td, sn / td), folded
-// back every 16 terms (two divisions): each numerator or denominator factor is
-// a product of two counts below 2^31, so 16 of them stay below 2^1024.
+// from x0 until x reaches x_end: S0 plus every term, stopping once a term adds
+// < 1e-17 of the sum.
+//
+// FP64 while the terms matter: no division per term -- the terms and their
+// sum are kept over one common denominator (tn / td, sn / td), folded back
+// every 16 terms (two divisions); each numerator or denominator factor is a
+// product of two counts below 2^31, so 16 of them stay below 2^1024.  Once a
+// term is below 1e-9 of the sum, the rest of the tail (log-concave: its ratios
+// keep falling) is below 1e-9 r / (1 - r) of it, and it is walked in FP32,
+// whose relative error over even thousands of terms (~1e-4) then moves the sum
+// by far less than the 1e-9 relative the p-values are held to.
 template <class Ratio>
 __device__ inline double fisher_walk(double S0, double t0, int x0, int dir, int x_end,
                                      Ratio ratio) {
     double S = S0, tn = t0, td = 1.0, sn = 0.0;
     int x = x0;
+    bool low = false;
     for (int j = 1; x != x_end; ++j) {
         double n, d;
         ratio(x, n, d);
@@ -175,7 +182,12 @@ __device__ inline double fisher_walk(double S0, double t0, int x0, int dir, int 
         tn *= n;
         td *= d;
         sn = fma(sn, d, tn);
-        if (tn < 1e-17 * fma(S, td, sn)) break;
+        const double tot = fma(S, td, sn);
+        if (tn < 1e-17 * tot) return S + sn / td;
+        if (tn < 1e-9 * tot) {
+            low = true;
+            break;
+        }
         if ((j & 15) == 0) {
             S += sn / td;
             tn /= td;
@@ -183,7 +195,19 @@ __device__ inline double fisher_walk(double S0, double t0, int x0, int dir, int 
             td = 1.0;
         }
     }
-    return S + sn / td;
+    S += sn / td;
+    if (!low) return S;
+    float t = (float)(tn / td), St = 0.f;
+    const float stop = (float)(1e-17 * S);
+    while (x != x_end) {
+        float n, d;
+        ratio(x, n, d);
+        x += dir;
+        t *= __fdividef(n, d);
+        St += t;
+        if (t < stop) break;
+    }
+    return S + (double)St;
 }
 
 // Two-sided Fisher exact test for the table (n11 n12 / n21 n22), natural-log
@@ -209,14 +233,16 @@ __device__ inline double fisher_lnp(const double *__restrict__ lf, int n11, int 
                __ldg(lf + (r2 - c1 + x));
     };
     // P(x+1)/P(x) and P(x-1)/P(x), as numerator and denominator (products of
-    // two counts)
-    auto up_nd = [&](int x, double &n, double &d) {
-        n = (double)(r1 - x) * (double)(c1 - x);
-        d = (double)(x + 1) * (double)(r2 - c1 + x + 1);
+    // two counts), in the type of n and d (double or float)
+    auto up_nd = [&](int x, auto &n, auto &d) {
+        using T = decltype(+n);
+        n = (T)(r1 - x) * (T)(c1 - x);
+        d = (T)(x + 1) * (T)(r2 - c1 + x + 1);
     };
-    auto down_nd = [&](int x, double &n, double &d) {
-        n = (double)x * (double)(r2 - c1 + x);
-        d = (double)(r1 - x + 1) * (double)(c1 - x + 1);
+    auto down_nd = [&](int x, auto &n, auto &d) {
+        using T = decltype(+n);
+        n = (T)x * (T)(r2 - c1 + x);
+        d = (T)(r1 - x + 1) * (T)(c1 - x + 1);
     };
     auto up = [&](int x) {
         double n, d;

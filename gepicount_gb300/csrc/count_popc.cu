@@ -139,12 +139,33 @@ __device__ __forceinline__ void popc_tile(uint32_t *smem, const int2 tile,
             }
     const float theta = ctx.st->theta;
     const float lp_thr = ctx.st->lp_thr;
+    // Fisher: tests that pass the bounds are queued (a shared atomic), and the
+    // exact sums run on all the CTA's threads once scoring is done -- not on the
+    // one or two lanes of a warp whose tests passed.  A full queue evaluates in
+    // place.
+    uint32_t *fq = nullptr;
+    if (ctx.objective != 0) {
+        fq = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(smem) + G::kCountBytes);
+        if (tid == 0) *fq = 0u;
+        __syncthreads();
+    }
 #pragma unroll 1
     for (int ij = 0; ij < 4; ++ij) {
         const int i = ij >> 1, j = ij & 1;
         const int s = sA0 + ty + (TA / 2) * i, t = sB0 + tx + 16 * j;
         if (s >= a1 || t >= b1 || t > s) continue;
-        score_pair(ctx, sG + ij * 18, s, t, theta, lp_thr);
+        score_pair(ctx, sG + ij * 18, s, t, theta, lp_thr, fq, G::kFisherQCap);
+    }
+    if (fq) {
+        __syncthreads();
+        const uint32_t n = min(*fq, (uint32_t)G::kFisherQCap);
+        const int4 *qa = reinterpret_cast<const int4 *>(fq + 4);
+        const int2 *qb = reinterpret_cast<const int2 *>(qa + G::kFisherQCap);
+        for (uint32_t e = tid; e < n; e += G::kThreads) {
+            const int4 a = qa[e];
+            const int2 b = qb[e];
+            exact_test(ctx, a.x, a.y >> 3, a.y & 7, a.z, a.w, b.x, b.y);
+        }
     }
 }
 

@@ -72,6 +72,7 @@ struct ScanCtx {
     const double *lf;    // log(n!) table (Fisher exact path)
     const float *lf32;   // log(n!) as float (Fisher bound)
     int objective;       // 0 entropy, 1 Fisher
+    int fisher_fp64;     // nonzero: Fisher tail walks in FP64 at every sample count
     Cand *cand;
     uint32_t cap;
     ScanState *st;
@@ -157,33 +158,130 @@ __device__ __forceinline__ double exact_mi(const uint64_t *__restrict__ T, int F
     return scalbn((double)(long long)num, -F) / (double)m;
 }
 
-// The sum of a tail walk, t_{j+1} = t_j * n(x) / d(x), x stepping by `dir`
-// from x0 until x reaches x_end: S0 plus every term, stopping once a term adds
-// < 1e-17 of the sum.
-//
-// FP64 while the terms matter: no division per term -- the terms and their
-// sum are kept over one common denominator (tn / td, sn / td), folded back
-// every 16 terms (two divisions); each numerator or denominator factor is a
-// product of two counts below 2^31, so 16 of them stay below 2^1024.  Once a
-// term is below 1e-9 of the sum, the rest of the tail (log-concave: its ratios
-// keep falling) is below 1e-9 r / (1 - r) of it, and it is walked in FP32,
-// whose relative error over even thousands of terms (~1e-4) then moves the sum
-// by far less than the 1e-9 relative the p-values are held to.
+// Float-float values hi + lo (|lo| <= ulp(hi) / 2) and the error-free
+// transformations they are built from: Dekker's product (1971, with a fused
+// multiply-add) and Knuth's sum (TAOCP vol. 2, 4.2.2).  About 46 significant
+// bits.  The explicit _rn intrinsics keep the compiler from contracting the
+// steps whose rounding errors are being captured.
+struct FFloat {
+    float hi, lo;
+};
+
+__device__ __forceinline__ FFloat ff_fast_sum(float a, float b) {  // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ FFloat ff_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b), v = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, v)), __fsub_rn(b, v))};
+}
+
+__device__ __forceinline__ FFloat ff_two_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return {p, __fmaf_rn(a, b, -p)};
+}
+
+// a + b for a, b >= 0 (no cancellation to guard against)
+__device__ __forceinline__ FFloat ff_add(FFloat a, FFloat b) {
+    const FFloat s = ff_two_sum(a.hi, b.hi);
+    return ff_fast_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+
+__device__ __forceinline__ FFloat ff_mul(FFloat a, FFloat b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
+    return ff_fast_sum(p, e);
+}
+
+// a / b: a first quotient q1, the remainder a - q1 b (a.hi - q1 b.hi is exact
+// by Sterbenz's lemma, q1 b.hi being within a few ulps of a.hi), and the
+// remainder's quotient as the correction.
+__device__ __forceinline__ FFloat ff_div(FFloat a, FFloat b) {
+    const float rb = __fdividef(1.f, b.hi);
+    const float q1 = __fmul_rn(a.hi, rb);
+    const FFloat p = ff_two_prod(q1, b.hi);
+    float r = __fsub_rn(a.hi, p.hi);
+    r = __fadd_rn(r, __fsub_rn(a.lo, p.lo));
+    r = __fmaf_rn(-q1, b.lo, r);
+    return ff_fast_sum(q1, __fmul_rn(r, rb));
+}
+
+__device__ __forceinline__ FFloat ff_of(double v) {
+    const float h = (float)v;
+    return {h, (float)(v - (double)h)};
+}
+
+// The end of a tail walk, once its terms add < 1e-9 of the sum S: continued
+// in FP32 until a term adds < 1e-17 of the sum; returns the terms' sum.  The
+// hypergeometric is log-concave, so what is left is at most 1e-9 r / (1 - r)
+// of S (r the term ratio there, falling further out), and FP32's relative
+// error on it -- about 1e-4 even over thousands of terms -- moves the sum by
+// far less than the 1e-9 relative the p-values are held to.
 template <class Ratio>
-__device__ inline double fisher_walk(double S0, double t0, int x0, int dir, int x_end,
-                                     Ratio ratio) {
+__device__ inline float fisher_walk_tail(double S, float t, int x, int dir, int x_end,
+                                         Ratio ratio) {
+    float St = 0.f;
+    const float stop = (float)(1e-17 * S);
+    while (x != x_end) {
+        const int4 f = ratio(x);
+        x += dir;
+        t *= __fdividef((float)f.x * (float)f.y, (float)f.z * (float)f.w);
+        St += t;
+        if (t < stop) break;
+    }
+    return St;
+}
+
+// The sum of a tail walk, t_{j+1} = t_j * (f.x f.y) / (f.z f.w) with
+// f = ratio(x), x stepping by `dir` from x0 until x reaches x_end: S0 plus
+// every term, stopping once a term adds < 1e-17 of the sum.  While the terms
+// add >= 1e-9 of the sum they are walked in float-float: the factors are
+// counts below 2^24, exact in FP32, so each ratio's numerator and denominator
+// are exact two-products; ratio, term and sum carry ~46 bits (CPU emulation
+// against exact rational sums, N up to 10^6: <= 3e-13 relative).  The FP64
+// pipe of this GPU issues at 1/64 of the FP32 rate, which makes these ~50
+// FP32 operations per term cheaper than the ~12 FP64 ones they replace.
+template <class Ratio>
+__device__ inline double fisher_walk_ff(double S0, double t0, int x, int dir, int x_end,
+                                        Ratio ratio) {
+    FFloat S = ff_of(S0), t = ff_of(t0);
+    bool low = false;
+    while (x != x_end) {
+        const int4 f = ratio(x);
+        x += dir;
+        const FFloat n = ff_two_prod((float)f.x, (float)f.y);
+        const FFloat d = ff_two_prod((float)f.z, (float)f.w);
+        t = ff_mul(t, ff_div(n, d));
+        S = ff_add(S, t);
+        if (t.hi < 1e-9f * S.hi) {
+            low = true;
+            break;
+        }
+    }
+    const double Sd = (double)S.hi + (double)S.lo;
+    return low ? Sd + (double)fisher_walk_tail(Sd, t.hi, x, dir, x_end, ratio) : Sd;
+}
+
+// The same sum in FP64, for counts of 2^24 and more.  No division per term:
+// the terms and their sum are kept over one common denominator (tn / td,
+// sn / td), folded back every 16 terms (two divisions); each numerator or
+// denominator factor is a product of two counts below 2^31, so 16 of them stay
+// below 2^1024.
+template <class Ratio>
+__device__ inline double fisher_walk_fp64(double S0, double t0, int x, int dir, int x_end,
+                                          Ratio ratio) {
     double S = S0, tn = t0, td = 1.0, sn = 0.0;
-    int x = x0;
     bool low = false;
     for (int j = 1; x != x_end; ++j) {
-        double n, d;
-        ratio(x, n, d);
+        const int4 f = ratio(x);
         x += dir;
-        tn *= n;
+        tn *= (double)f.x * (double)f.y;
+        const double d = (double)f.z * (double)f.w;
         td *= d;
         sn = fma(sn, d, tn);
         const double tot = fma(S, td, sn);
-        if (tn < 1e-17 * tot) return S + sn / td;
         if (tn < 1e-9 * tot) {
             low = true;
             break;
@@ -196,18 +294,7 @@ __device__ inline double fisher_walk(double S0, double t0, int x0, int dir, int 
         }
     }
     S += sn / td;
-    if (!low) return S;
-    float t = (float)(tn / td), St = 0.f;
-    const float stop = (float)(1e-17 * S);
-    while (x != x_end) {
-        float n, d;
-        ratio(x, n, d);
-        x += dir;
-        t *= __fdividef(n, d);
-        St += t;
-        if (t < stop) break;
-    }
-    return S + (double)St;
+    return low ? S + (double)fisher_walk_tail(S, (float)(tn / td), x, dir, x_end, ratio) : S;
 }
 
 // Two-sided Fisher exact test for the table (n11 n12 / n21 n22), natural-log
@@ -218,7 +305,7 @@ __device__ inline double fisher_walk(double S0, double t0, int x0, int dir, int 
 // term, and the first qualifying term past the mode is found by bisection
 // before that tail is walked.  Walks stop once a term adds < 1e-17 of the sum.
 __device__ inline double fisher_lnp(const double *__restrict__ lf, int n11, int n12, int n21,
-                                    int n22) {
+                                    int n22, bool fp64_walks = false) {
     const int r1 = n11 + n21;  // column-1 total
     const int r2 = n12 + n22;  // column-2 total
     const int c1 = n11 + n12;  // row-1 total
@@ -232,27 +319,21 @@ __device__ inline double fisher_lnp(const double *__restrict__ lf, int n11, int 
         return K - __ldg(lf + x) - __ldg(lf + (r1 - x)) - __ldg(lf + (c1 - x)) -
                __ldg(lf + (r2 - c1 + x));
     };
-    // P(x+1)/P(x) and P(x-1)/P(x), as numerator and denominator (products of
-    // two counts), in the type of n and d (double or float)
-    auto up_nd = [&](int x, auto &n, auto &d) {
-        using T = decltype(+n);
-        n = (T)(r1 - x) * (T)(c1 - x);
-        d = (T)(x + 1) * (T)(r2 - c1 + x + 1);
-    };
-    auto down_nd = [&](int x, auto &n, auto &d) {
-        using T = decltype(+n);
-        n = (T)x * (T)(r2 - c1 + x);
-        d = (T)(r1 - x + 1) * (T)(c1 - x + 1);
-    };
+    // P(x+1)/P(x) and P(x-1)/P(x) as (f.x f.y) / (f.z f.w), f four counts
+    auto up4 = [&](int x) { return make_int4(r1 - x, c1 - x, x + 1, r2 - c1 + x + 1); };
+    auto down4 = [&](int x) { return make_int4(x, r2 - c1 + x, r1 - x + 1, c1 - x + 1); };
     auto up = [&](int x) {
-        double n, d;
-        up_nd(x, n, d);
-        return n / d;
+        const int4 f = up4(x);
+        return ((double)f.x * (double)f.y) / ((double)f.z * (double)f.w);
     };
     auto down = [&](int x) {
-        double n, d;
-        down_nd(x, n, d);
-        return n / d;
+        const int4 f = down4(x);
+        return ((double)f.x * (double)f.y) / ((double)f.z * (double)f.w);
+    };
+    const bool ff = !fp64_walks && N < (1 << 24);
+    auto walk = [&](double S0, double t0, int x0, int dir, int x_end, auto ratio) {
+        return ff ? fisher_walk_ff(S0, t0, x0, dir, x_end, ratio)
+                  : fisher_walk_fp64(S0, t0, x0, dir, x_end, ratio);
     };
     const double tol = 1.0 + 1e-7;
     const int xo = n11;
@@ -264,7 +345,7 @@ __device__ inline double fisher_lnp(const double *__restrict__ lf, int n11, int 
     double S = 1.0;
     if (xo <= xm) {
         // near tail: x < xo
-        S = fisher_walk(S, 1.0, xo, -1, lo, down_nd);
+        S = walk(S, 1.0, xo, -1, lo, down4);
         // plateau between xo and the mode
         double t = 1.0;
         for (int x = xo; x < xm;) {
@@ -283,11 +364,11 @@ __device__ inline double fisher_lnp(const double *__restrict__ lf, int n11, int 
                 if (lpx(mid) <= lim) h = mid; else l = mid + 1;
             }
             const double u = exp(lpx(l) - lpo);
-            S = fisher_walk(S + u, u, l, +1, hi, up_nd);
+            S = walk(S + u, u, l, +1, hi, up4);
         }
     } else {
         // near tail: x > xo
-        S = fisher_walk(S, 1.0, xo, +1, hi, up_nd);
+        S = walk(S, 1.0, xo, +1, hi, up4);
         double t = 1.0;
         for (int x = xo; x > xm;) {
             double t2 = t * down(x);
@@ -305,7 +386,7 @@ __device__ inline double fisher_lnp(const double *__restrict__ lf, int n11, int 
                 if (lpx(mid) <= lim) l = mid; else h = mid - 1;
             }
             const double u = exp(lpx(l) - lpo);
-            S = fisher_walk(S + u, u, l, -1, lo, down_nd);
+            S = walk(S + u, u, l, -1, lo, down4);
         }
     }
     double lnp = lpo + log(S);
@@ -406,7 +487,7 @@ static __device__ __noinline__ void exact_test(const ScanCtx &ctx, int rA, int r
         // value >= tau_val, i.e. ln p <= -tau_val ln 10
         if (fisher_above(ctx.lf, w, y - w, x, z - x, -ctx.st->tau_val * 2.302585092994045684))
             return;
-        value = -fisher_lnp(ctx.lf, w, y - w, x, z - x) * 0.43429448190325182765;
+        value = -fisher_lnp(ctx.lf, w, y - w, x, z - x, ctx.fisher_fp64) * 0.43429448190325182765;
     }
     append_candidate(ctx, value, rA, rB, fun, w, x, y, z);
 }
@@ -528,7 +609,7 @@ __device__ __forceinline__ uint32_t rowpair_bounds(const float *G0, const float 
 // and only tests within that margin of tau reach the exact integer key.
 __device__ __forceinline__ void score_tests(const ScanCtx &ctx, const float *G0,
                                             const float *G1, int s, int t, float theta,
-                                            float lp_thr) {
+                                            float lp_thr, uint32_t *fq, int fq_cap) {
     const float y = G0[8], z = G1[8];
     const float m = y + z;
     const float yz = y * z;
@@ -590,23 +671,33 @@ __device__ __forceinline__ void score_tests(const ScanCtx &ctx, const float *G0,
                     const float mag = Tm + a + b + c + d + e + g + Ty + Tz + fabsf(tm);
                     pass = est + (2e-6f * mag + 1e-3f) >= tm;
                 }
-                if (pass)
-                    exact_test(ctx, 2 * s + i, 2 * t + j, f, (int)w, (int)x, (int)y, (int)z);
+                if (!pass) continue;
+                if (fq) {  // Fisher: queue for the CTA's threads to evaluate together
+                    const uint32_t e = atomicAdd(fq, 1u);
+                    if (e < (uint32_t)fq_cap) {
+                        int4 *qa = reinterpret_cast<int4 *>(fq + 4);
+                        reinterpret_cast<int2 *>(qa + fq_cap)[e] = make_int2((int)y, (int)z);
+                        qa[e] = make_int4(2 * s + i, (2 * t + j) * 8 + f, (int)w, (int)x);
+                        continue;
+                    }
+                }
+                exact_test(ctx, 2 * s + i, 2 * t + j, f, (int)w, (int)x, (int)y, (int)z);
             }
         }
     }
 }
 
-// Out-of-line wrapper: G points at 18 floats (class 0 Gram, class 1 Gram).
+// Out-of-line wrapper: G points at 18 floats (class 0 Gram, class 1 Gram);
+// fq, when not null, the CTA's Fisher queue of fq_cap entries.
 static __device__ __noinline__ void score_pair(const ScanCtx &ctx, const float *G, int s, int t,
-                                        float theta, float lp_thr) {
+                                        float theta, float lp_thr, uint32_t *fq, int fq_cap) {
     float G0[9], G1[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
         G0[k] = G[k];
         G1[k] = G[9 + k];
     }
-    score_tests(ctx, G0, G1, s, t, theta, lp_thr);
+    score_tests(ctx, G0, G1, s, t, theta, lp_thr, fq, fq_cap);
 }
 
 #endif  // __CUDACC__

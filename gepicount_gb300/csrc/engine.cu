@@ -676,6 +676,7 @@ void Engine::step(std::vector<Job *> &active) {
         R.ctx.lf = pl->d_lf;
         R.ctx.lf32 = pl->d_lf32;
         R.ctx.objective = j->rq.objective;
+        R.ctx.fisher_fp64 = fisher_fp64_walks();
         R.ctx.cand = j->buf->cand[j->cur];
         R.ctx.cap = j->buf->cap;
         R.ctx.st = d_states_ + s;

@@ -43,6 +43,7 @@ cudaError_t launch_popc_batch(int ta, int kc, const ReqDesc *reqs, WorkQueue *q,
                               cudaStream_t stream, bool setup = false);
 bool tc_shape_ok(int Wp, int W0);  // class widths the tensor-core kernel takes
 bool tc_debug_stall();             // the timeout test's setting (GEPI_DEBUG_STALL) is on
+int fisher_fp64_walks();           // GEPI_DEBUG_FISHER_FP64: Fisher walks in FP64 at any N
 int tc_rows_pad(int n_snps);       // rows of the block-major operand copy
 size_t tc_block_words(int n_snps, int Wp, int W0);
 cudaError_t tc_measure_peak(int num_sms, int reps, int kind, double *tflops, int *err,

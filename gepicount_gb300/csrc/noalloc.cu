@@ -58,6 +58,7 @@ cudaError_t launch_decode_rows(const uint64_t *bits, const uint64_t *valid, int 
 cudaError_t launch_popc_tiles(int ta, int kc, const uint32_t *planes, int Wp, int W0,
                               const int2 *tiles, int ntiles, int a0, int a1, int b0, int b1,
                               const ScanCtx &ctx, uint32_t *dump, cudaStream_t stream);
+int fisher_fp64_walks();
 cudaError_t run_select_compact(Cand *in, Cand *out, ScanState *st, void *sel, uint32_t cap,
                                uint32_t k, int n_override, uint32_t n_compact, int objective,
                                float lp_margin, int num_sms, cudaStream_t stream);
@@ -362,6 +363,7 @@ extern "C" gepi_status gepi_process_gpu_1_noalloc(const uint64_t *bits, const ui
     ctx.lf = d_lf;
     ctx.lf32 = d_lf32;
     ctx.objective = par->objective;
+    ctx.fisher_fp64 = fisher_fp64_walks();
     ctx.cap = kNoAllocCap;
     ctx.st = d_state;
     const float lp_margin = 2e-6f * (float)std::lgamma((double)nmax + 1.0) + 1e-3f;

@@ -417,6 +417,7 @@ gepi_status time_count_kernel(gepi_planes *pl, const CountVariant &v, int n, flo
     ctx.lf = pl->d_lf;
     ctx.lf32 = pl->d_lf32;
     ctx.objective = GEPI_ENTROPY;
+    ctx.fisher_fp64 = 0;
     ctx.cap = pl->cap;
     ctx.st = pl->d_state;
     ctx.cand = pl->d_cand[0];
@@ -673,6 +674,7 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
     ctx.lf = pl->d_lf;
     ctx.lf32 = pl->d_lf32;
     ctx.objective = par->objective;
+    ctx.fisher_fp64 = fisher_fp64_walks();
     ctx.cap = pl->cap;
     ctx.st = pl->d_state;
 
@@ -820,6 +822,15 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
 }  // namespace
 
 namespace gepi {
+
+// GEPI_DEBUG_FISHER_FP64=1 runs the Fisher tail walks in FP64 at every
+// sample count, as they run from 2^24 samples up, so tests reach that code on
+// small inputs.
+int fisher_fp64_walks() {
+    const char *e = std::getenv("GEPI_DEBUG_FISHER_FP64");
+    return e && std::atoi(e) != 0 ? 1 : 0;
+}
+
 cudaError_t pool_alloc(int device, void **ptr, size_t bytes, cudaStream_t s) {
     cudaMemPool_t p = device_pool(device);
     if (!p) return cudaErrorMemoryAllocation;

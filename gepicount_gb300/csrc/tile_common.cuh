@@ -25,7 +25,11 @@ struct PopcGeom {
     static constexpr int kStages = 3;
     static constexpr size_t kStageWords = (size_t)(kARows + kBRows) * kStride;
     static constexpr size_t kPipeBytes = (size_t)kStages * kStageWords * 4;
-    static constexpr size_t kEpiBytes = (size_t)kThreads * 72 * 4;  // 72 counts per thread
+    static constexpr size_t kCountBytes = (size_t)kThreads * 72 * 4;  // 72 counts per thread
+    // Fisher tests that passed the bounds, queued for the whole CTA to
+    // evaluate (a count, then int4 {rA, rB * 8 + f, w, x} and int2 {y, z}).
+    static constexpr int kFisherQCap = kThreads;
+    static constexpr size_t kEpiBytes = kCountBytes + 16 + (size_t)kFisherQCap * 24;
     static constexpr size_t kSmem = kPipeBytes > kEpiBytes ? kPipeBytes : kEpiBytes;
     static constexpr int kMinBlocks = TA == 32 ? 2 : 1;  // 128 registers per thread
 };

@@ -338,6 +338,30 @@ def test_device_fp64_values_within_tolerance(gepi, tmp_path, kw, method):
     pl.close()
 
 
+@pytest.mark.parametrize("method", sorted(METHODS))
+@pytest.mark.parametrize("kw", [
+    dict(n_snps=40, n_cases=300, n_controls=420, missing=0.05, n_planted=2, seed=82),
+    dict(n_snps=120, n_cases=1500, n_controls=1700, missing=0.01, n_planted=2, seed=83),
+])
+def test_device_fisher_fp64_walks_within_tolerance(gepi, tmp_path, monkeypatch, kw, method):
+    """The FP64 tail walks that tables of 2^24 samples and more take, forced
+    at these sizes with GEPI_DEBUG_FISHER_FP64=1: every returned p within
+    1e-9 relative of the oracle's FP64 Fisher, like the float-float walks
+    that run by default."""
+    pl, rows, fs, _ = make_planes(gepi, kw, tmp_path)
+    k = 150
+    monkeypatch.setenv("GEPI_DEBUG_FISHER_FP64", "1")
+    got = pl.scan(k, objective=gepi.FISHER, method=METHODS[method])
+    err64 = _device_value_errors(gepi, rows, got, pl.last_values(k), 1)
+    monkeypatch.delenv("GEPI_DEBUG_FISHER_FP64")
+    got = pl.scan(k, objective=gepi.FISHER, method=METHODS[method])
+    err_ff = _device_value_errors(gepi, rows, got, pl.last_values(k), 1)
+    assert err64 <= FISHER_RTOL, err64
+    assert err_ff <= FISHER_RTOL, err_ff
+    print(f"max device error: Fisher |d ln p| FP64 walks {err64:.3e}, float-float {err_ff:.3e}")
+    pl.close()
+
+
 def test_device_fisher_fp64_config2_full_size(gepi):
     """Config 2 at full size (20,000 SNPs x 4,000 samples, 3 planted pairs),
     Fisher top-1,000 through both counting kernels: the same list, and every

@@ -297,15 +297,38 @@ __device__ inline double fisher_walk_fp64(double S0, double t0, int x, int dir, 
     return low ? S + (double)fisher_walk_tail(S, (float)(tn / td), x, dir, x_end, ratio) : S;
 }
 
+// ln P(obs) of the table (n11 n12 / n21 n22) under the hypergeometric with
+// its margins, from the log-factorial table; K receives the margins' part,
+// ln P(x) = K - lf[x] - lf[r1 - x] - lf[c1 - x] - lf[r2 - c1 + x].
+__device__ __forceinline__ double fisher_lpo(const double *__restrict__ lf, int n11, int n12,
+                                             int n21, int n22, double &K) {
+    const int r1 = n11 + n21, r2 = n12 + n22, c1 = n11 + n12, N = r1 + r2;
+    K = __ldg(lf + r1) + __ldg(lf + r2) + __ldg(lf + c1) + __ldg(lf + (N - c1)) - __ldg(lf + N);
+    return K - __ldg(lf + n11) - __ldg(lf + n21) - __ldg(lf + n12) - __ldg(lf + n22);
+}
+
 // Two-sided Fisher exact test for the table (n11 n12 / n21 n22), natural-log
-// p-value.  Terms with P(x) <= P(obs) * (1 + 1e-7) are summed (R's rule).  The
-// observed term is anchored with the log-factorial table; the hypergeometric
-// is log-concave, so the tail beyond xo (away from the mode) is walked with
-// the term ratio, a possible plateau between xo and the mode is walked term by
+// p-value, given K and lpo = ln P(obs) from fisher_lpo.  Terms with
+// P(x) <= P(obs) * (1 + 1e-7) are summed (R's rule).  The hypergeometric is
+// log-concave, so the tail beyond xo (away from the mode) is walked with the
+// term ratio, a possible plateau between xo and the mode is walked term by
 // term, and the first qualifying term past the mode is found by bisection
 // before that tail is walked.  Walks stop once a term adds < 1e-17 of the sum.
-__device__ inline double fisher_lnp(const double *__restrict__ lf, int n11, int n12, int n21,
-                                    int n22, bool fp64_walks = false) {
+//
+// FP64 issues at 1/64 of the FP32 rate on this GPU, so the search on the far
+// side runs in FP32 first: g32(x), ln P(x) - ln lim from the float table
+// lf32, is within E = 2e-6 lf32[N] + 1e-6 of the exact value (each table
+// entry within half an ulp of lf[N], five terms, four roundings of sums below
+// 4 lf[N]: under 1.5e-6 lf[N] in all).  Where g32 > E a term certainly fails
+// the rule and where g32 < -E it certainly passes, so two FP32 bisections
+// bracket the first qualifying term, and the FP64 bisection that decides it
+// runs only inside the bracket (usually one to three terms wide).  The
+// plateau's first step is likewise decided in FP32 when the ratio is clearly
+// above 1 + 1e-7.  The terms summed, and the FP64 values deciding them, are
+// those of the plain FP64 search.
+__device__ inline double fisher_lnp(const double *__restrict__ lf, const float *__restrict__ lf32,
+                                    int n11, int n12, int n21, int n22, double K, double lpo,
+                                    bool fp64_walks = false) {
     const int r1 = n11 + n21;  // column-1 total
     const int r2 = n12 + n22;  // column-2 total
     const int c1 = n11 + n12;  // row-1 total
@@ -313,8 +336,6 @@ __device__ inline double fisher_lnp(const double *__restrict__ lf, int n11, int 
     const int lo = c1 <= r2 ? 0 : c1 - r2;
     const int hi = c1 < r1 ? c1 : r1;
     if (lo >= hi) return 0.0;
-    const double K = __ldg(lf + r1) + __ldg(lf + r2) + __ldg(lf + c1) + __ldg(lf + (N - c1)) -
-                     __ldg(lf + N);
     auto lpx = [&](int x) {
         return K - __ldg(lf + x) - __ldg(lf + (r1 - x)) - __ldg(lf + (c1 - x)) -
                __ldg(lf + (r2 - c1 + x));
@@ -322,13 +343,12 @@ __device__ inline double fisher_lnp(const double *__restrict__ lf, int n11, int 
     // P(x+1)/P(x) and P(x-1)/P(x) as (f.x f.y) / (f.z f.w), f four counts
     auto up4 = [&](int x) { return make_int4(r1 - x, c1 - x, x + 1, r2 - c1 + x + 1); };
     auto down4 = [&](int x) { return make_int4(x, r2 - c1 + x, r1 - x + 1, c1 - x + 1); };
-    auto up = [&](int x) {
-        const int4 f = up4(x);
+    auto ratio64 = [](int4 f) {
         return ((double)f.x * (double)f.y) / ((double)f.z * (double)f.w);
     };
-    auto down = [&](int x) {
-        const int4 f = down4(x);
-        return ((double)f.x * (double)f.y) / ((double)f.z * (double)f.w);
+    // the FP32 ratio is within 4 ulps: above 1 + 1e-6 the FP64 one is above 1 + 1e-7
+    auto clearly_rising = [](int4 f) {
+        return ((float)f.x * (float)f.y) / ((float)f.z * (float)f.w) > 1.000001f;
     };
     const bool ff = !fp64_walks && N < (1 << 24);
     auto walk = [&](double S0, double t0, int x0, int dir, int x_end, auto ratio) {
@@ -337,30 +357,52 @@ __device__ inline double fisher_lnp(const double *__restrict__ lf, int n11, int 
     };
     const double tol = 1.0 + 1e-7;
     const int xo = n11;
-    const double lpo = lpx(xo);
     const double lim = lpo + 9.99999950000003e-08;  // log1p(1e-7)
-    int xm = (int)(((double)(r1 + 1) * (double)(c1 + 1)) / (double)(N + 2));
+    int xm = (int)(((long long)(r1 + 1) * (long long)(c1 + 1)) / (long long)(N + 2));
     if (xm < lo) xm = lo;
     if (xm > hi) xm = hi;
+    const float E = 2e-6f * __ldg(lf32 + N) + 1e-6f;
+    const float gc = (float)(K - lim);
+    auto g32 = [&](int x) {
+        return gc - __ldg(lf32 + x) - __ldg(lf32 + (r1 - x)) - __ldg(lf32 + (c1 - x)) -
+               __ldg(lf32 + (r2 - c1 + x));
+    };
+    auto passes = [&](int x) {  // lpx(x) <= lim, in FP32 where the margin decides it
+        const float g = g32(x);
+        return g < -E ? true : g > E ? false : lpx(x) <= lim;
+    };
     double S = 1.0;
     if (xo <= xm) {
         // near tail: x < xo
         S = walk(S, 1.0, xo, -1, lo, down4);
         // plateau between xo and the mode
-        double t = 1.0;
-        for (int x = xo; x < xm;) {
-            double t2 = t * up(x);
-            if (t2 > tol) break;
-            ++x;
-            t = t2;
-            S += t;
+        if (xo < xm && !clearly_rising(up4(xo))) {
+            double t = 1.0;
+            for (int x = xo; x < xm;) {
+                double t2 = t * ratio64(up4(x));
+                if (t2 > tol) break;
+                ++x;
+                t = t2;
+                S += t;
+            }
         }
         // falling side x in [xm+1, hi]: first x with lpx(x) <= lim
-        int a = xm + 1, b = hi;
-        if (a <= b && lpx(b) <= lim) {
-            int l = a, h = b;
+        const int a = xm + 1, b = hi;
+        if (a <= b && passes(b)) {
+            int l = a, h = b;  // first x with g32 <= E: no x before it passes
             while (l < h) {
-                int mid = (l + h) >> 1;
+                const int mid = (l + h) >> 1;
+                if (g32(mid) <= E) h = mid; else l = mid + 1;
+            }
+            const int t0 = l;
+            h = b;  // first x with g32 < -E (or b): it passes
+            while (l < h) {
+                const int mid = (l + h) >> 1;
+                if (g32(mid) < -E) h = mid; else l = mid + 1;
+            }
+            l = t0;
+            while (l < h) {
+                const int mid = (l + h) >> 1;
                 if (lpx(mid) <= lim) h = mid; else l = mid + 1;
             }
             const double u = exp(lpx(l) - lpo);
@@ -369,20 +411,33 @@ __device__ inline double fisher_lnp(const double *__restrict__ lf, int n11, int 
     } else {
         // near tail: x > xo
         S = walk(S, 1.0, xo, +1, hi, up4);
-        double t = 1.0;
-        for (int x = xo; x > xm;) {
-            double t2 = t * down(x);
-            if (t2 > tol) break;
-            --x;
-            t = t2;
-            S += t;
+        if (!clearly_rising(down4(xo))) {
+            double t = 1.0;
+            for (int x = xo; x > xm;) {
+                double t2 = t * ratio64(down4(x));
+                if (t2 > tol) break;
+                --x;
+                t = t2;
+                S += t;
+            }
         }
         // falling side x in [lo, xm-1]: last x with lpx(x) <= lim
-        int a = lo, b = xm - 1;
-        if (a <= b && lpx(a) <= lim) {
-            int l = a, h = b;
+        const int a = lo, b = xm - 1;
+        if (a <= b && passes(a)) {
+            int l = a, h = b;  // last x with g32 <= E: no x after it passes
             while (l < h) {
-                int mid = (l + h + 1) >> 1;
+                const int mid = (l + h + 1) >> 1;
+                if (g32(mid) <= E) l = mid; else h = mid - 1;
+            }
+            const int t0 = h;
+            l = a;  // last x with g32 < -E (or a): it passes
+            while (l < h) {
+                const int mid = (l + h + 1) >> 1;
+                if (g32(mid) < -E) l = mid; else h = mid - 1;
+            }
+            h = t0;
+            while (l < h) {
+                const int mid = (l + h + 1) >> 1;
                 if (lpx(mid) <= lim) l = mid; else h = mid - 1;
             }
             const double u = exp(lpx(l) - lpo);
@@ -397,21 +452,19 @@ __device__ inline double fisher_lnp(const double *__restrict__ lf, int n11, int 
 // observed term and up to 8 terms beyond it on its own side of the mode --
 // each at most P(obs), the hypergeometric being unimodal, so each is in the
 // sum -- already show ln p > ln_thr.  Such a test cannot reach the ranking,
-// and the exact tail sums it would cost are skipped.  The terms are walked
-// with the term ratio in FP32 and only counted while below 1 - 1e-5 of
-// P(obs); the sum is taken 1e-5 low and its log 1e-5 low, and the comparison
-// keeps a margin of 1e-7 + 1e-10 |ln_thr| nats, far above the rounding of
-// fisher_lnp, so the tests it drops are tests the exact evaluation drops.
-__device__ inline bool fisher_above(const double *__restrict__ lf, int n11, int n12, int n21,
-                                    int n22, double ln_thr) {
+// and the exact tail sums it would cost are skipped.  lpo = ln P(obs) from
+// fisher_lpo.  The terms are walked with the term ratio in FP32 and only
+// counted while below 1 - 1e-5 of P(obs); the sum is taken 1e-5 low and its
+// log 1e-5 low, and the comparison keeps a margin of 1e-7 + 1e-10 |ln_thr|
+// nats, far above the rounding of fisher_lnp, so the tests it drops are tests
+// the exact evaluation drops.
+__device__ inline bool fisher_above(int n11, int n12, int n21, int n22, double lpo,
+                                    double ln_thr) {
     if (!(ln_thr < 0.0)) return false;  // no threshold yet
-    const int r1 = n11 + n21, r2 = n12 + n22, c1 = n11 + n12, N = r1 + r2;
+    const int r1 = n11 + n21, r2 = n12 + n22, c1 = n11 + n12;
     const int lo = c1 <= r2 ? 0 : c1 - r2;
     const int hi = c1 < r1 ? c1 : r1;
     if (lo >= hi) return false;
-    const double lpo = __ldg(lf + r1) + __ldg(lf + r2) + __ldg(lf + c1) + __ldg(lf + (N - c1)) -
-                       __ldg(lf + N) - __ldg(lf + n11) - __ldg(lf + (r1 - n11)) -
-                       __ldg(lf + (c1 - n11)) - __ldg(lf + (r2 - c1 + n11));
     const double margin = 1e-7 + 1e-10 * -ln_thr;
     const double d = ln_thr + margin - lpo;  // reject when ln(sum of the terms) > d
     if (d > 2.25) return false;              // 9 terms sum to at most 9 < e^2.25
@@ -485,9 +538,12 @@ static __device__ __noinline__ void exact_test(const ScanCtx &ctx, int rA, int r
     } else {
         // print order (w, y-w, x, z-x); value = -log10 p, appended when
         // value >= tau_val, i.e. ln p <= -tau_val ln 10
-        if (fisher_above(ctx.lf, w, y - w, x, z - x, -ctx.st->tau_val * 2.302585092994045684))
+        double K;
+        const double lpo = fisher_lpo(ctx.lf, w, y - w, x, z - x, K);
+        if (fisher_above(w, y - w, x, z - x, lpo, -ctx.st->tau_val * 2.302585092994045684))
             return;
-        value = -fisher_lnp(ctx.lf, w, y - w, x, z - x, ctx.fisher_fp64) * 0.43429448190325182765;
+        value = -fisher_lnp(ctx.lf, ctx.lf32, w, y - w, x, z - x, K, lpo, ctx.fisher_fp64) *
+                0.43429448190325182765;
     }
     append_candidate(ctx, value, rA, rB, fun, w, x, y, z);
 }

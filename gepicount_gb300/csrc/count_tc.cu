@@ -731,12 +731,15 @@ struct TcScorer {
                 const uint32_t rp = rowpair_bounds(G, G + 9, sA == sBt, OBJ, theta, lp_thr);
                 if (rp) mask = tc_stage1<OBJ>(ctx, G, G + 9, rp, theta, lp_thr);
             }
-            // Fisher: the tests that passed go to the warp's queue (their exact
-            // tail sums then run 32 at a time, one per lane, instead of on the
-            // one or two lanes whose tests passed); a round with more than the
-            // queue holds (no threshold yet) evaluates in place
+            // Fisher: the tests that passed go to the launch's pending list, for
+            // a launch across the GPU to evaluate (a test past its capacity is
+            // evaluated here); without one (batched engine), to the warp's
+            // queue, whose exact tail sums then run 32 at a time, one per lane,
+            // instead of on the one or two lanes whose tests passed -- a round
+            // with more than the queue holds evaluates in place
             bool queue = false;
             int pos = 0;
+            uint32_t gpos = 0;
             if constexpr (OBJ == 1) {
                 const int n = __popc(mask);
                 int incl = n;
@@ -746,10 +749,18 @@ struct TcScorer {
                     if (lane >= o) incl += v;
                 }
                 const int total = __shfl_sync(0xffffffffu, incl, 31);
-                if (total > 0 && fill + total > kTcQCap) drain();
-                queue = total > 0 && total <= kTcQCap;
-                pos = fill + incl - n;
-                if (queue) fill += total;
+                if (ctx.pend) {
+                    if (total > 0) {
+                        uint32_t base = 0;
+                        if (lane == 31) base = atomicAdd(&ctx.st->pend, (uint32_t)total);
+                        gpos = __shfl_sync(0xffffffffu, base, 31) + (uint32_t)(incl - n);
+                    }
+                } else {
+                    if (total > 0 && fill + total > kTcQCap) drain();
+                    queue = total > 0 && total <= kTcQCap;
+                    pos = fill + incl - n;
+                    if (queue) fill += total;
+                }
             }
             while (mask) {
                 const int bit = __ffs(mask) - 1;
@@ -761,9 +772,12 @@ struct TcScorer {
                 const int w = fun_count(n11, rr, cc, y, f);
                 gram_cells(G + 9, ri, rj, n11, rr, cc);
                 const int x = fun_count(n11, rr, cc, z, f);
-                if (queue)
-                    qb[pos++] = make_uint4((uint32_t)(2 * sA + ri), (uint32_t)(2 * sBt + rj) << 3 | (uint32_t)f,
+                const uint4 e = make_uint4((uint32_t)(2 * sA + ri), (uint32_t)(2 * sBt + rj) << 3 | (uint32_t)f,
                                            (uint32_t)w | (uint32_t)x << 16, (uint32_t)y | (uint32_t)z << 16);
+                if (OBJ == 1 && ctx.pend && gpos < ctx.pend_cap)
+                    ctx.pend[gpos++] = e;
+                else if (queue)
+                    qb[pos++] = e;
                 else
                     tc_refine<OBJ>(ctx, 2 * sA + ri, 2 * sBt + rj, f, w, x, y, z);
             }
@@ -1423,6 +1437,22 @@ static cudaError_t launch_tc_pairs(const uint32_t *blk, int rows_pad, int Wp, in
     pairs = std::max(1, std::min(pairs, ntiles));
     kern<<<2 * pairs, kTcThreads, kTcSmem, stream>>>(blk, rows_pad, Wp, W0, tiles, ntiles, a0, a1,
                                                     b0, b1, ctx, dump, err, wait_cycles, TEST ? 1 : 0);
+    return cudaGetLastError();
+}
+
+// The Fisher tests a counting launch left in ctx.pend (the first min(count,
+// cap); any beyond were evaluated in the launch), one per thread.
+__global__ void __launch_bounds__(256) fisher_pending_kernel(ScanCtx ctx) {
+    const uint32_t n = min(ctx.st->pend, ctx.pend_cap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint4 e = ctx.pend[i];
+        exact_test(ctx, (int)e.x, (int)(e.y >> 3), (int)(e.y & 7u), (int)(e.z & 0xFFFFu),
+                   (int)(e.z >> 16), (int)(e.w & 0xFFFFu), (int)(e.w >> 16));
+    }
+}
+
+cudaError_t launch_fisher_pending(const ScanCtx &ctx, int num_sms, cudaStream_t stream) {
+    fisher_pending_kernel<<<num_sms * 4, 256, 0, stream>>>(ctx);
     return cudaGetLastError();
 }
 

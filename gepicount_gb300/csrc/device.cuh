@@ -48,6 +48,7 @@ struct ScanState {
     uint32_t sel_mode;           // batched engine: select run after the last batch
                                  // (0 none, 1 threshold select, 2 overflow retry)
     uint32_t count_batch;        // batched engine: count after the last batch, before its select
+    uint32_t pend;               // Fisher tests appended to ScanCtx::pend (may exceed its cap)
 };
 
 struct SelState;
@@ -73,6 +74,11 @@ struct ScanCtx {
     const float *lf32;   // log(n!) as float (Fisher bound)
     int objective;       // 0 entropy, 1 Fisher
     int fisher_fp64;     // nonzero: Fisher tail walks in FP64 at every sample count
+    // Fisher tests that passed the bounds, left for fisher_pending_kernel to
+    // evaluate across the GPU after the counting launch ({rA, rB * 8 + f,
+    // w | x << 16, y | z << 16}); null: evaluated inside the counting kernel
+    uint4 *pend;
+    uint32_t pend_cap;
     Cand *cand;
     uint32_t cap;
     ScanState *st;

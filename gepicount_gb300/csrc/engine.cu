@@ -677,6 +677,8 @@ void Engine::step(std::vector<Job *> &active) {
         R.ctx.lf32 = pl->d_lf32;
         R.ctx.objective = j->rq.objective;
         R.ctx.fisher_fp64 = fisher_fp64_walks();
+        R.ctx.pend = nullptr;
+        R.ctx.pend_cap = 0;
         R.ctx.cand = j->buf->cand[j->cur];
         R.ctx.cap = j->buf->cap;
         R.ctx.st = d_states_ + s;

@@ -27,6 +27,8 @@ cudaError_t launch_decode_rows(const uint64_t *bits, const uint64_t *valid, int 
 cudaError_t launch_popc_tiles(int ta, int kc, const uint32_t *planes, int Wp, int W0,
                               const int2 *tiles, int ntiles, int a0, int a1, int b0, int b1,
                               const ScanCtx &ctx, uint32_t *dump, cudaStream_t stream);
+// Exact evaluation of the Fisher tests a counting launch left in ctx.pend.
+cudaError_t launch_fisher_pending(const ScanCtx &ctx, int num_sms, cudaStream_t stream);
 cudaError_t launch_tc_tiles(const uint32_t *blk, int n_snps, int Wp, int W0, const int2 *tiles,
                             int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
                             uint32_t *dump, int *err, int num_sms, cudaStream_t stream);
@@ -159,6 +161,7 @@ struct gepi_planes {
     float lf_max = 0.f;
     gepi::Cand *d_cand[2] = {nullptr, nullptr};
     uint32_t cap = 0;
+    uint4 *d_pend = nullptr;  // Fisher pending tests of a tensor-core launch (lazy)
     gepi::ScanState *d_state = nullptr;
     gepi::ScanState *h_state = nullptr;
     void *d_sel = nullptr;

@@ -364,6 +364,8 @@ extern "C" gepi_status gepi_process_gpu_1_noalloc(const uint64_t *bits, const ui
     ctx.lf32 = d_lf32;
     ctx.objective = par->objective;
     ctx.fisher_fp64 = fisher_fp64_walks();
+    ctx.pend = nullptr;
+    ctx.pend_cap = 0;
     ctx.cap = kNoAllocCap;
     ctx.st = d_state;
     const float lp_margin = 2e-6f * (float)std::lgamma((double)nmax + 1.0) + 1e-3f;

@@ -122,6 +122,7 @@ void planes_free(gepi_planes *pl) {
         pool_free(pl->d_tc_blocks, pl->stream);
         pool_free(pl->d_cand[0], pl->stream);
         pool_free(pl->d_cand[1], pl->stream);
+        pool_free(pl->d_pend, pl->stream);
         pool_free(pl->d_T, pl->stream);
         pool_free(pl->d_lf, pl->stream);
         pool_free(pl->d_lf32, pl->stream);
@@ -300,6 +301,7 @@ gepi_status ensure_marginal(gepi_planes *pl) {
 // The ranked result does not depend on the order.
 constexpr int kHotSnps = 16;
 constexpr size_t kHotMinTiles = 4096;  // smaller scans keep the band order
+constexpr uint32_t kPendCap = 1u << 18;  // Fisher pending tests per launch (4 MB)
 
 // The triangle scan's tile list in that order, generated directly: counted,
 // sized once and written through a pointer (no sort, no partition).  Empty hot
@@ -418,6 +420,8 @@ gepi_status time_count_kernel(gepi_planes *pl, const CountVariant &v, int n, flo
     ctx.lf32 = pl->d_lf32;
     ctx.objective = GEPI_ENTROPY;
     ctx.fisher_fp64 = 0;
+    ctx.pend = nullptr;
+    ctx.pend_cap = 0;
     ctx.cap = pl->cap;
     ctx.st = pl->d_state;
     ctx.cand = pl->d_cand[0];
@@ -677,6 +681,21 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
     ctx.fisher_fp64 = fisher_fp64_walks();
     ctx.cap = pl->cap;
     ctx.st = pl->d_state;
+    ctx.pend = nullptr;
+    ctx.pend_cap = 0;
+    if (par->objective == GEPI_FISHER && cv->method == GEPI_METHOD_TENSOR) {
+        // The first batches hold one or a few tiles and, with no threshold
+        // yet, up to all their tests reach the exact sum: on the few CTAs of
+        // such a launch they would run nearly serially, so the counting kernel
+        // leaves them to a launch across the GPU.
+        if (!pl->d_pend) {
+            GEPI_TRY(check_mem((size_t)kPendCap * sizeof(uint4), "Fisher pending tests"));
+            GEPI_CUDA(pool_alloc(pl->device, reinterpret_cast<void **>(&pl->d_pend),
+                                 (size_t)kPendCap * sizeof(uint4), pl->stream));
+        }
+        ctx.pend = pl->d_pend;
+        ctx.pend_cap = kPendCap;
+    }
 
     const double tests_per_tile = 20.0 * TA * TB;
     const uint32_t budget = select_budget(pl->cap, k);
@@ -860,9 +879,16 @@ const CountVariant *count_variant(int id) {
 cudaError_t launch_count(const CountVariant &v, const gepi_planes *pl, const int2 *tiles,
                          int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
                          uint32_t *dump, int *err, cudaStream_t stream) {
-    if (v.method == GEPI_METHOD_TENSOR)
-        return launch_tc_tiles(pl->d_tc_blocks, pl->n_snps, pl->Wp, pl->W0, tiles, ntiles, a0, a1,
-                               b0, b1, ctx, dump, err, pl->num_sms, stream);
+    if (v.method == GEPI_METHOD_TENSOR) {
+        if (ctx.pend) {
+            cudaError_t e = cudaMemsetAsync(&ctx.st->pend, 0, sizeof(uint32_t), stream);
+            if (e != cudaSuccess) return e;
+        }
+        cudaError_t e = launch_tc_tiles(pl->d_tc_blocks, pl->n_snps, pl->Wp, pl->W0, tiles, ntiles,
+                                        a0, a1, b0, b1, ctx, dump, err, pl->num_sms, stream);
+        if (e == cudaSuccess && ctx.pend) e = launch_fisher_pending(ctx, pl->num_sms, stream);
+        return e;
+    }
     return launch_popc_tiles(v.ta, v.words, pl->d_planes, pl->Wp, pl->W0, tiles, ntiles, a0, a1, b0,
                              b1, ctx, dump, stream);
 }

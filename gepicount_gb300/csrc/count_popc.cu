@@ -144,7 +144,7 @@ __device__ __forceinline__ void popc_tile(uint32_t *smem, const int2 tile,
     // one or two lanes of a warp whose tests passed.  A full queue evaluates in
     // place.
     uint32_t *fq = nullptr;
-    if (ctx.objective != 0) {
+    if (ctx.objective != 0 && !ctx.pend) {
         fq = reinterpret_cast<uint32_t *>(reinterpret_cast<char *>(smem) + G::kCountBytes);
         if (tid == 0) *fq = 0u;
         __syncthreads();

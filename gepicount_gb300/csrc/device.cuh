@@ -734,7 +734,16 @@ __device__ __forceinline__ void score_tests(const ScanCtx &ctx, const float *G0,
                     pass = est + (2e-6f * mag + 1e-3f) >= tm;
                 }
                 if (!pass) continue;
-                if (fq) {  // Fisher: queue for the CTA's threads to evaluate together
+                if (ctx.pend) {  // Fisher: left for the launch across the GPU after this one
+                    const uint32_t e = atomicAdd(&ctx.st->pend, 1u);
+                    if (e < ctx.pend_cap) {
+                        ctx.pend[e] = make_uint4((uint32_t)(2 * s + i),
+                                                 (uint32_t)(2 * t + j) << 3 | (uint32_t)f,
+                                                 (uint32_t)w | (uint32_t)x << 16,
+                                                 (uint32_t)y | (uint32_t)z << 16);
+                        continue;
+                    }
+                } else if (fq) {  // Fisher: queue for the CTA's threads to evaluate together
                     const uint32_t e = atomicAdd(fq, 1u);
                     if (e < (uint32_t)fq_cap) {
                         int4 *qa = reinterpret_cast<int4 *>(fq + 4);

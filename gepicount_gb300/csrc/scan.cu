@@ -683,11 +683,11 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
     ctx.st = pl->d_state;
     ctx.pend = nullptr;
     ctx.pend_cap = 0;
-    if (par->objective == GEPI_FISHER && cv->method == GEPI_METHOD_TENSOR) {
+    if (par->objective == GEPI_FISHER && pl->S0 < 65536 && pl->S1 < 65536) {
         // The first batches hold one or a few tiles and, with no threshold
         // yet, up to all their tests reach the exact sum: on the few CTAs of
         // such a launch they would run nearly serially, so the counting kernel
-        // leaves them to a launch across the GPU.
+        // leaves them to a launch across the GPU (entries hold 16-bit counts).
         if (!pl->d_pend) {
             GEPI_TRY(check_mem((size_t)kPendCap * sizeof(uint4), "Fisher pending tests"));
             GEPI_CUDA(pool_alloc(pl->device, reinterpret_cast<void **>(&pl->d_pend),
@@ -879,18 +879,18 @@ const CountVariant *count_variant(int id) {
 cudaError_t launch_count(const CountVariant &v, const gepi_planes *pl, const int2 *tiles,
                          int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
                          uint32_t *dump, int *err, cudaStream_t stream) {
-    if (v.method == GEPI_METHOD_TENSOR) {
-        if (ctx.pend) {
-            cudaError_t e = cudaMemsetAsync(&ctx.st->pend, 0, sizeof(uint32_t), stream);
-            if (e != cudaSuccess) return e;
-        }
-        cudaError_t e = launch_tc_tiles(pl->d_tc_blocks, pl->n_snps, pl->Wp, pl->W0, tiles, ntiles,
-                                        a0, a1, b0, b1, ctx, dump, err, pl->num_sms, stream);
-        if (e == cudaSuccess && ctx.pend) e = launch_fisher_pending(ctx, pl->num_sms, stream);
-        return e;
+    if (ctx.pend) {
+        cudaError_t e = cudaMemsetAsync(&ctx.st->pend, 0, sizeof(uint32_t), stream);
+        if (e != cudaSuccess) return e;
     }
-    return launch_popc_tiles(v.ta, v.words, pl->d_planes, pl->Wp, pl->W0, tiles, ntiles, a0, a1, b0,
-                             b1, ctx, dump, stream);
+    cudaError_t e =
+        v.method == GEPI_METHOD_TENSOR
+            ? launch_tc_tiles(pl->d_tc_blocks, pl->n_snps, pl->Wp, pl->W0, tiles, ntiles, a0, a1, b0,
+                              b1, ctx, dump, err, pl->num_sms, stream)
+            : launch_popc_tiles(v.ta, v.words, pl->d_planes, pl->Wp, pl->W0, tiles, ntiles, a0, a1,
+                                b0, b1, ctx, dump, stream);
+    if (e == cudaSuccess && ctx.pend) e = launch_fisher_pending(ctx, pl->num_sms, stream);
+    return e;
 }
 gepi_status pl_scan_tiles(gepi_planes *pl, int a0, int a1, int b0, int b1, int TA, int TB, bool hot,
                           std::vector<int2> &out) {

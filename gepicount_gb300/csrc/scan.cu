@@ -695,6 +695,12 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
         }
         ctx.pend = pl->d_pend;
         ctx.pend_cap = kPendCap;
+        // GEPI_DEBUG_PEND_CAP shrinks the list so tests reach the in-launch
+        // evaluation of the tests past its capacity
+        if (const char *e = std::getenv("GEPI_DEBUG_PEND_CAP")) {
+            const long long v = std::atoll(e);
+            if (v > 0 && v < (long long)kPendCap) ctx.pend_cap = (uint32_t)v;
+        }
     }
 
     const double tests_per_tile = 20.0 * TA * TB;

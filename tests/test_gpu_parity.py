@@ -362,6 +362,31 @@ def test_device_fisher_fp64_walks_within_tolerance(gepi, tmp_path, monkeypatch, 
     pl.close()
 
 
+@pytest.mark.parametrize("method", sorted(METHODS))
+def test_fisher_pending_list_overflow(gepi, tmp_path, monkeypatch, method):
+    """Fisher tests that pass the bounds go to a pending list evaluated by a
+    launch across the GPU; those past its capacity are evaluated inside the
+    counting launch.  With the list shrunk to 7 entries (GEPI_DEBUG_PEND_CAP)
+    most tests take that path: the same ranked tests with the same counts,
+    FP64 values equal to 1e-12 (the two evaluations are one function, built
+    into different kernels), and within 1e-9 of the oracle."""
+    kw = dict(n_snps=120, n_cases=1500, n_controls=1700, missing=0.01, n_planted=2, seed=83)
+    pl, rows, fs, _ = make_planes(gepi, kw, tmp_path)
+    k = 150
+    want = pl.scan(k, objective=gepi.FISHER, method=METHODS[method])
+    want_v = pl.last_values(k)
+    monkeypatch.setenv("GEPI_DEBUG_PEND_CAP", "7")
+    got = pl.scan(k, objective=gepi.FISHER, method=METHODS[method])
+    got_v = pl.last_values(k)
+    monkeypatch.delenv("GEPI_DEBUG_PEND_CAP")
+    for f in ("sA", "sB", "n", "fun"):
+        assert np.array_equal(got[f], want[f]), f
+    assert np.allclose(got_v, want_v, rtol=1e-12, atol=0.0)
+    err = _device_value_errors(gepi, rows, got, got_v, 1)
+    assert err <= FISHER_RTOL, err
+    pl.close()
+
+
 def test_device_fisher_fp64_config2_full_size(gepi):
     """Config 2 at full size (20,000 SNPs x 4,000 samples, 3 planted pairs),
     Fisher top-1,000 through both counting kernels: the same list, and every

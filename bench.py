@@ -267,17 +267,18 @@ def run_ours(args, cfg):
     _, ph, _ = g.synth_bed(spec, out=bed)
     k = cfg["k"]
     method = {"auto": g.METHOD_AUTO, "popc": g.METHOD_POPC, "tensor": g.METHOD_TENSOR}[args.method]
+    obj = g.FISHER if args.objective == "fisher" else g.ENTROPY
 
     planes = g.Planes.from_bed(bed, spec.n_snps, ph, device=local)
     tune = planes.autotune() if method == g.METHOD_AUTO else None
     for _ in range(args.warmup):
-        planes.scan(k, method=method)
+        planes.scan(k, method=method, objective=obj)
     barrier()
     stats = []
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            tops = planes.scan(k, method=method)
+            tops = planes.scan(k, method=method, objective=obj)
             stats.append(planes.last_stats())
         barrier()
         wall = time.perf_counter() - t0
@@ -286,10 +287,10 @@ def run_ours(args, cfg):
     # The plain popcount kernel on the same resident planes (the metric's "vs plain kernel").
     plain = None
     if args.plain_steps > 0 and stats[0]["method"] != g.METHOD_POPC:
-        planes.scan(k, method=g.METHOD_POPC)
+        planes.scan(k, method=g.METHOD_POPC, objective=obj)
         pms = []
         for _ in range(args.plain_steps):
-            planes.scan(k, method=g.METHOD_POPC)
+            planes.scan(k, method=g.METHOD_POPC, objective=obj)
             pms.append(planes.last_stats()["scan_ms"])
         pmean = sum(pms) / len(pms)
         plain = {"value": world * pairs_per_scan / (pmean / 1000.0), "ms_per_step": pmean,
@@ -358,7 +359,7 @@ def run_ours(args, cfg):
         barrier()
         t1 = time.perf_counter()
         with g.Planes.from_bed(bed, spec.n_snps, ph, device=local) as pl:
-            pl.scan(k, method=method)
+            pl.scan(k, method=method, objective=obj)
         torch.cuda.synchronize()
         e2e_times.append(time.perf_counter() - t1)
     e2e_t = sum(e2e_times) / len(e2e_times)  # mean step time: throughput over the steps
@@ -371,7 +372,8 @@ def run_ours(args, cfg):
     e2e_value = world * pairs_per_scan / e2e_t
 
     cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
+    # the oracle's CPU gold loop ranks by entropy only
+    if rank == 0 and not args.no_cpu_baseline and obj == g.ENTROPY:
         r = cpu_baseline(cfg, bed, ph, target_s=args.cpu_seconds, threads=1)
         cpu = {"value": r["value"], "unit": UNIT, "cores": 1, "kind": "port",
                "sample": r["sample"]}
@@ -384,7 +386,8 @@ def run_ours(args, cfg):
             "dtype": "e2m1 0/1 operands, f32 accumulate (exact counts)" if tensor else "u32 popcount",
             "data": "synthetic (seeded generator, HWE, planted pairs)",
             "config": {"workload": describe(args.config, cfg), "n_snps": spec.n_snps,
-                       "n_samples": n_samples, "k": k, "method": ["auto", "popc", "tensor"][stats[0]["method"]] if args.method == "auto" else args.method,
+                       "n_samples": n_samples, "k": k, "objective": args.objective,
+                       "method": ["auto", "popc", "tensor"][stats[0]["method"]] if args.method == "auto" else args.method,
                        "pair_tests_per_step": pairs_per_scan,
                        "boolean_tests_per_step": 5 * (2 * spec.n_snps) * (2 * spec.n_snps + 1) // 2,
                        "l2": "inputs larger than L2 (genotype planes "
@@ -639,6 +642,8 @@ def main():
     ap.add_argument("--requests", type=int, default=200,
                     help="requests per offered-load level (--config serving)")
     ap.add_argument("--method", choices=["auto", "popc", "tensor"], default="auto")
+    ap.add_argument("--objective", choices=["entropy", "fisher"], default="entropy",
+                    help="ranking objective of the scan (the metric is quoted on entropy)")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--ref-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -654,6 +659,11 @@ def main():
         return run_cohorts(args) if args.config == "cohorts64" else run_serving(args)
     cfg = CONFIGS[args.config]
     if args.impl == "reference":
+        if args.objective == "fisher":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference ranks by Fisher "
+                              "only on its CUDA path; its CPU gold loop ranks by entropy"}),
+                  flush=True)
+            return 0
         return run_reference(args, cfg)
     return run_ours(args, cfg)
 

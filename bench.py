@@ -445,7 +445,8 @@ def run_cohorts(args):
     cohorts = [_make_cohort(g, rng, c["snps"], c["samples"], c["case_frac"], c["missing"],
                             c["seed"] * 100 + i + 7919 * rank, local)
                for i in range(c["n_cohorts"])]
-    reqs = [g.ScanRequest(pl, c["k"]) for pl, _, _ in cohorts]
+    obj = g.FISHER if args.objective == "fisher" else g.ENTROPY
+    reqs = [g.ScanRequest(pl, c["k"], objective=obj) for pl, _, _ in cohorts]
     tunes = [pl.autotune_variants() for pl, _, _ in cohorts]
     for _ in range(args.warmup):
         g.scan_batch(reqs)
@@ -463,9 +464,10 @@ def run_cohorts(args):
     for _ in range(max(1, min(args.steps, 2))):
         t0 = time.perf_counter()
         for pl, _, _ in cohorts:
-            pl.scan(c["k"])
+            pl.scan(c["k"], objective=obj)
         seq.append(time.perf_counter() - t0)
-    same = all(o.tobytes() == pl.scan(c["k"]).tobytes() for o, (pl, _, _) in zip(outs, cohorts))
+    same = all(o.tobytes() == pl.scan(c["k"], objective=obj).tobytes()
+               for o, (pl, _, _) in zip(outs, cohorts))
     t_b, t_s = statistics.median(times), statistics.median(seq)
     nsamp = [s for _, _, s in cohorts]
     nsnp = [n for _, n, _ in cohorts]
@@ -478,7 +480,7 @@ def run_cohorts(args):
         "config": {"workload": (f"{c['n_cohorts']} cohorts, SNPs log-U{c['snps']}, samples "
                                 f"log-U{c['samples']}, case fraction U{c['case_frac']}, "
                                 f"{c['missing']:.0%} missing, top-{c['k']:,} each"),
-                   "snps_total": sum(nsnp), "snps_max": max(nsnp), "samples_max": max(nsamp),
+                   "objective": args.objective, "snps_total": sum(nsnp), "snps_max": max(nsnp), "samples_max": max(nsamp),
                    "pair_tests_per_step": pairs,
                    "variants": {name: sum(t["name"] == name for t in tunes)
                                 for name in sorted({t["name"] for t in tunes})}},

@@ -752,7 +752,7 @@ struct TcScorer {
                 if (ctx.pend) {
                     if (total > 0) {
                         uint32_t base = 0;
-                        if (lane == 31) base = atomicAdd(&ctx.st->pend, (uint32_t)total);
+                        if (lane == 31) base = atomicAdd(&ctx.pend->n, (uint32_t)total);
                         gpos = __shfl_sync(0xffffffffu, base, 31) + (uint32_t)(incl - n);
                     }
                 } else {
@@ -774,9 +774,11 @@ struct TcScorer {
                 const int x = fun_count(n11, rr, cc, z, f);
                 const uint4 e = make_uint4((uint32_t)(2 * sA + ri), (uint32_t)(2 * sBt + rj) << 3 | (uint32_t)f,
                                            (uint32_t)w | (uint32_t)x << 16, (uint32_t)y | (uint32_t)z << 16);
-                if (OBJ == 1 && ctx.pend && gpos < ctx.pend_cap)
-                    ctx.pend[gpos++] = e;
-                else if (queue)
+                if (OBJ == 1 && ctx.pend && gpos < ctx.pend->cap) {
+                    ctx.pend->ent[gpos] = e;
+                    if (ctx.pend->tag) ctx.pend->tag[gpos] = ctx.pend_req;
+                    ++gpos;
+                } else if (queue)
                     qb[pos++] = e;
                 else
                     tc_refine<OBJ>(ctx, 2 * sA + ri, 2 * sBt + rj, f, w, x, y, z);
@@ -1440,19 +1442,41 @@ static cudaError_t launch_tc_pairs(const uint32_t *blk, int rows_pad, int Wp, in
     return cudaGetLastError();
 }
 
+__device__ __forceinline__ void pending_test(const ScanCtx &ctx, uint4 e) {
+    exact_test(ctx, (int)e.x, (int)(e.y >> 3), (int)(e.y & 7u), (int)(e.z & 0xFFFFu),
+               (int)(e.z >> 16), (int)(e.w & 0xFFFFu), (int)(e.w >> 16));
+}
+
 // The Fisher tests a counting launch left in ctx.pend (the first min(count,
 // cap); any beyond were evaluated in the launch), one per thread.
 __global__ void __launch_bounds__(256) fisher_pending_kernel(ScanCtx ctx) {
-    const uint32_t n = min(ctx.st->pend, ctx.pend_cap);
+    const PendList &L = *ctx.pend;
+    const uint32_t n = min(L.n, L.cap);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        pending_test(ctx, L.ent[i]);
+}
+
+// The same for a batched engine step: one list for all its requests, each
+// entry evaluated with its own request's tables, threshold and buffer.
+__global__ void __launch_bounds__(256)
+    fisher_pending_batch_kernel(const ReqDesc *__restrict__ reqs, const PendList *list) {
+    const PendList &L = *list;
+    const uint32_t n = min(L.n, L.cap);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint4 e = ctx.pend[i];
-        exact_test(ctx, (int)e.x, (int)(e.y >> 3), (int)(e.y & 7u), (int)(e.z & 0xFFFFu),
-                   (int)(e.z >> 16), (int)(e.w & 0xFFFFu), (int)(e.w >> 16));
+        // a local copy, as every other caller of exact_test passes one
+        const ScanCtx ctx = reqs[L.tag[i]].ctx;
+        pending_test(ctx, L.ent[i]);
     }
 }
 
 cudaError_t launch_fisher_pending(const ScanCtx &ctx, int num_sms, cudaStream_t stream) {
     fisher_pending_kernel<<<num_sms * 4, 256, 0, stream>>>(ctx);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fisher_pending_batch(const ReqDesc *reqs, const PendList *list, int num_sms,
+                                        cudaStream_t stream) {
+    fisher_pending_batch_kernel<<<num_sms * 4, 256, 0, stream>>>(reqs, list);
     return cudaGetLastError();
 }
 

@@ -48,7 +48,6 @@ struct ScanState {
     uint32_t sel_mode;           // batched engine: select run after the last batch
                                  // (0 none, 1 threshold select, 2 overflow retry)
     uint32_t count_batch;        // batched engine: count after the last batch, before its select
-    uint32_t pend;               // Fisher tests appended to ScanCtx::pend (may exceed its cap)
 };
 
 struct SelState;
@@ -67,6 +66,16 @@ struct SelJob {
     int32_t active;         // 0: no batch this step
 };
 
+// A pending list of Fisher tests (device memory): entries {rA, rB * 8 + f,
+// w | x << 16, y | z << 16}, the fill counter (may exceed cap), and -- in a
+// list shared by a batched engine step's requests -- each entry's request.
+struct PendList {
+    uint4 *ent;
+    uint32_t *tag;  // null for a single scan
+    uint32_t n;
+    uint32_t cap;
+};
+
 struct ScanCtx {
     const uint64_t *T;   // fixed-point n*log2(n) table, n in [0, Smax]
     int F;               // its fraction bits
@@ -74,11 +83,12 @@ struct ScanCtx {
     const float *lf32;   // log(n!) as float (Fisher bound)
     int objective;       // 0 entropy, 1 Fisher
     int fisher_fp64;     // nonzero: Fisher tail walks in FP64 at every sample count
-    // Fisher tests that passed the bounds, left for fisher_pending_kernel to
-    // evaluate across the GPU after the counting launch ({rA, rB * 8 + f,
-    // w | x << 16, y | z << 16}); null: evaluated inside the counting kernel
-    uint4 *pend;
-    uint32_t pend_cap;
+    // Fisher tests that passed the bounds are left in this list for a launch
+    // across the GPU to evaluate after the counting launch; null: evaluated
+    // inside the counting kernel.  pend_req: this request's tag in a list
+    // shared by the requests of a batched engine step (its ReqDesc index).
+    PendList *pend;
+    uint32_t pend_req;
     Cand *cand;
     uint32_t cap;
     ScanState *st;
@@ -500,8 +510,11 @@ __device__ __forceinline__ void append_candidate(const ScanCtx &ctx, double valu
     if (key < ctx.st->tau_key) return;
     // One atomic per group of lanes appending together: in a scan's first
     // batch, with no threshold yet, every test of a tile is appended, and one
-    // atomic per test on the one counter would serialise them.
-    const unsigned grp = __activemask();
+    // atomic per test on the one counter would serialise them.  The lanes are
+    // grouped by their scan state: a batched engine step's pending list mixes
+    // requests within a warp.
+    const unsigned grp =
+        __match_any_sync(__activemask(), (unsigned long long)(uintptr_t)ctx.st);
     unsigned lane;
     asm("mov.u32 %0, %%laneid;" : "=r"(lane));
     const int leader = __ffs(grp) - 1;
@@ -735,12 +748,14 @@ __device__ __forceinline__ void score_tests(const ScanCtx &ctx, const float *G0,
                 }
                 if (!pass) continue;
                 if (ctx.pend) {  // Fisher: left for the launch across the GPU after this one
-                    const uint32_t e = atomicAdd(&ctx.st->pend, 1u);
-                    if (e < ctx.pend_cap) {
-                        ctx.pend[e] = make_uint4((uint32_t)(2 * s + i),
-                                                 (uint32_t)(2 * t + j) << 3 | (uint32_t)f,
-                                                 (uint32_t)w | (uint32_t)x << 16,
-                                                 (uint32_t)y | (uint32_t)z << 16);
+                    PendList &L = *ctx.pend;
+                    const uint32_t e = atomicAdd(&L.n, 1u);
+                    if (e < L.cap) {
+                        L.ent[e] = make_uint4((uint32_t)(2 * s + i),
+                                              (uint32_t)(2 * t + j) << 3 | (uint32_t)f,
+                                              (uint32_t)w | (uint32_t)x << 16,
+                                              (uint32_t)y | (uint32_t)z << 16);
+                        if (L.tag) L.tag[e] = ctx.pend_req;
                         continue;
                     }
                 } else if (fq) {  // Fisher: queue for the CTA's threads to evaluate together

@@ -79,6 +79,9 @@ constexpr size_t kTileCacheBytes = 1ull << 30;
 // Kernel groups of a step, in launch order: tensor cores (entropy, Fisher),
 // then one per popcount variant.
 constexpr int kGroups = 5;
+// Fisher tests a step leaves for its pending-list launch (all requests; 80 MB
+// with the request tags); past it they are evaluated in the counting launch
+constexpr uint32_t kEnginePendCap = 1u << 22;
 int group_of(const CountVariant &v, int objective) {
     if (v.method == GEPI_METHOD_TENSOR) return objective == GEPI_ENTROPY ? 0 : 1;
     return 1 + v.id;  // popcount variants 1..3 -> groups 2..4
@@ -169,6 +172,7 @@ class Engine {
 
    private:
     gepi_status ensure_slots(int need);
+    gepi_status ensure_pending();
     // setup = true: only the kernels' shared-memory opt-ins and occupancy
     // queries (outside any capture)
     cudaError_t enqueue_step(unsigned mask, bool setup = false);
@@ -196,6 +200,10 @@ class Engine {
     unsigned char *h_step_ = nullptr, *d_step_ = nullptr;
     WorkQueue *h_queues_ = nullptr;  // pinned: the launches' error codes, read back each step
     std::map<unsigned, cudaGraphExec_t> graphs_;
+    // the steps' Fisher pending list (allocated with the first Fisher request):
+    // fill counter, request tags, entries
+    unsigned char *d_pend_buf_ = nullptr;
+    PendList *d_pend_ = nullptr;  // its header, at the start of d_pend_buf_
     // estimated device ms per unit of tile weight, per kernel group
     double ms_per_weight_[kGroups] = {0, 0, 0, 0, 0};
     std::vector<std::unique_ptr<JobBuffers>> pool_;
@@ -217,6 +225,7 @@ Engine::~Engine() {
     dfree(d_states_);
     dfree(d_sel_);
     dfree(d_step_);
+    dfree(d_pend_buf_);
     if (h_states_) cudaFreeHost(h_states_);
     if (h_step_) cudaFreeHost(h_step_);
     if (h_queues_) cudaFreeHost(h_queues_);
@@ -298,6 +307,30 @@ gepi_status Engine::ensure_slots(int need) {
     return GEPI_OK;
 }
 
+// The Fisher pending list of the steps.  The step graphs bake in its address,
+// so those captured before it existed (without its launches) are dropped.
+gepi_status Engine::ensure_pending() {
+    if (d_pend_buf_) return GEPI_OK;
+    const size_t tags = 256, ents = tags + (size_t)kEnginePendCap * 4;
+    unsigned char *b = nullptr;
+    GEPI_CUDA(cudaMalloc(&b, ents + (size_t)kEnginePendCap * sizeof(uint4)));
+    PendList hdr{};
+    hdr.ent = reinterpret_cast<uint4 *>(b + ents);
+    hdr.tag = reinterpret_cast<uint32_t *>(b + tags);
+    hdr.cap = kEnginePendCap;
+    cudaError_t e = cudaMemcpy(b, &hdr, sizeof hdr, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
+    if (e != cudaSuccess) {
+        cudaFree(b);
+        return set_error(GEPI_ERR_CUDA, std::string("engine pending list: ") + cudaGetErrorString(e));
+    }
+    for (auto &kv : graphs_) cudaGraphExecDestroy(kv.second);
+    graphs_.clear();
+    d_pend_buf_ = b;
+    d_pend_ = reinterpret_cast<PendList *>(b);
+    return GEPI_OK;
+}
+
 // The device work of one step on the engine's stream: upload, the counting
 // launches of the kernel groups in `mask` (bit g), the batched selects, the
 // read-back.
@@ -313,6 +346,8 @@ cudaError_t Engine::enqueue_step(unsigned mask, bool setup) {
     cudaError_t e = cudaSuccess;
     if (!setup) e = cudaMemcpyAsync(d_step_, h_step_, step_bytes_, cudaMemcpyHostToDevice, stream_);
     if (e == cudaSuccess && !setup) e = record(ev_[0]);
+    if (e == cudaSuccess && !setup && d_pend_)
+        e = cudaMemsetAsync(&d_pend_->n, 0, sizeof(uint32_t), stream_);
     for (int g = 0; g < kGroups && e == cudaSuccess; ++g) {
         if (!(mask & (1u << g))) continue;
         if (g < 2) {
@@ -323,6 +358,7 @@ cudaError_t Engine::enqueue_step(unsigned mask, bool setup) {
         }
     }
     if (setup) return e;
+    if (e == cudaSuccess && d_pend_) e = launch_fisher_pending_batch(dreqs, d_pend_, num_sms_, stream_);
     if (e == cudaSuccess) e = record(ev_[1]);
     if (e == cudaSuccess) e = run_select_batch(djobs, nslots_, num_sms_, stream_);
     if (e == cudaSuccess)
@@ -643,6 +679,13 @@ void Engine::step(std::vector<Job *> &active) {
         return;
     }
     plan(run);
+    for (Job *j : run) {
+        if (j->rq.objective == GEPI_FISHER && !d_pend_buf_ && ensure_pending() != GEPI_OK) {
+            // without the list the counting kernels evaluate the tests themselves
+            (void)cudaGetLastError();
+            break;
+        }
+    }
 
     // the step's descriptors
     WorkQueue *hq = reinterpret_cast<WorkQueue *>(h_step_);
@@ -677,8 +720,12 @@ void Engine::step(std::vector<Job *> &active) {
         R.ctx.lf32 = pl->d_lf32;
         R.ctx.objective = j->rq.objective;
         R.ctx.fisher_fp64 = fisher_fp64_walks();
-        R.ctx.pend = nullptr;
-        R.ctx.pend_cap = 0;
+        // Fisher: tests that pass the bounds go to the step's pending list
+        // (entries hold 16-bit counts)
+        const bool pend = j->rq.objective == GEPI_FISHER && d_pend_ && pl->S0 < 65536 &&
+                          pl->S1 < 65536;
+        R.ctx.pend = pend ? d_pend_ : nullptr;
+        R.ctx.pend_req = (uint32_t)s;
         R.ctx.cand = j->buf->cand[j->cur];
         R.ctx.cap = j->buf->cap;
         R.ctx.st = d_states_ + s;

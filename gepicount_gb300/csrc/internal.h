@@ -29,6 +29,9 @@ cudaError_t launch_popc_tiles(int ta, int kc, const uint32_t *planes, int Wp, in
                               const ScanCtx &ctx, uint32_t *dump, cudaStream_t stream);
 // Exact evaluation of the Fisher tests a counting launch left in ctx.pend.
 cudaError_t launch_fisher_pending(const ScanCtx &ctx, int num_sms, cudaStream_t stream);
+// The same for a batched engine step's shared list (entries tagged by request).
+cudaError_t launch_fisher_pending_batch(const ReqDesc *reqs, const PendList *list, int num_sms,
+                                        cudaStream_t stream);
 cudaError_t launch_tc_tiles(const uint32_t *blk, int n_snps, int Wp, int W0, const int2 *tiles,
                             int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
                             uint32_t *dump, int *err, int num_sms, cudaStream_t stream);
@@ -161,7 +164,8 @@ struct gepi_planes {
     float lf_max = 0.f;
     gepi::Cand *d_cand[2] = {nullptr, nullptr};
     uint32_t cap = 0;
-    uint4 *d_pend = nullptr;  // Fisher pending tests of a tensor-core launch (lazy)
+    // Fisher pending list of the scans (lazy): its PendList header, then the entries
+    gepi::PendList *d_pend = nullptr;
     gepi::ScanState *d_state = nullptr;
     gepi::ScanState *h_state = nullptr;
     void *d_sel = nullptr;

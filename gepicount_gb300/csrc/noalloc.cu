@@ -365,7 +365,7 @@ extern "C" gepi_status gepi_process_gpu_1_noalloc(const uint64_t *bits, const ui
     ctx.objective = par->objective;
     ctx.fisher_fp64 = fisher_fp64_walks();
     ctx.pend = nullptr;
-    ctx.pend_cap = 0;
+    ctx.pend_req = 0;
     ctx.cap = kNoAllocCap;
     ctx.st = d_state;
     const float lp_margin = 2e-6f * (float)std::lgamma((double)nmax + 1.0) + 1e-3f;

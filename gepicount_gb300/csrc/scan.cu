@@ -421,7 +421,7 @@ gepi_status time_count_kernel(gepi_planes *pl, const CountVariant &v, int n, flo
     ctx.objective = GEPI_ENTROPY;
     ctx.fisher_fp64 = 0;
     ctx.pend = nullptr;
-    ctx.pend_cap = 0;
+    ctx.pend_req = 0;
     ctx.cap = pl->cap;
     ctx.st = pl->d_state;
     ctx.cand = pl->d_cand[0];
@@ -682,25 +682,30 @@ gepi_status scan_impl(gepi_planes *pl, const gepi_params *par, int a0, int na, i
     ctx.cap = pl->cap;
     ctx.st = pl->d_state;
     ctx.pend = nullptr;
-    ctx.pend_cap = 0;
+    ctx.pend_req = 0;
     if (par->objective == GEPI_FISHER && pl->S0 < 65536 && pl->S1 < 65536) {
         // The first batches hold one or a few tiles and, with no threshold
         // yet, up to all their tests reach the exact sum: on the few CTAs of
         // such a launch they would run nearly serially, so the counting kernel
         // leaves them to a launch across the GPU (entries hold 16-bit counts).
+        const size_t bytes = 256 + (size_t)kPendCap * sizeof(uint4);
         if (!pl->d_pend) {
-            GEPI_TRY(check_mem((size_t)kPendCap * sizeof(uint4), "Fisher pending tests"));
-            GEPI_CUDA(pool_alloc(pl->device, reinterpret_cast<void **>(&pl->d_pend),
-                                 (size_t)kPendCap * sizeof(uint4), pl->stream));
+            GEPI_TRY(check_mem(bytes, "Fisher pending tests"));
+            GEPI_CUDA(pool_alloc(pl->device, reinterpret_cast<void **>(&pl->d_pend), bytes,
+                                 pl->stream));
         }
-        ctx.pend = pl->d_pend;
-        ctx.pend_cap = kPendCap;
+        PendList hdr{};
+        hdr.ent = reinterpret_cast<uint4 *>(reinterpret_cast<char *>(pl->d_pend) + 256);
+        hdr.cap = kPendCap;
         // GEPI_DEBUG_PEND_CAP shrinks the list so tests reach the in-launch
         // evaluation of the tests past its capacity
         if (const char *e = std::getenv("GEPI_DEBUG_PEND_CAP")) {
             const long long v = std::atoll(e);
-            if (v > 0 && v < (long long)kPendCap) ctx.pend_cap = (uint32_t)v;
+            if (v > 0 && v < (long long)kPendCap) hdr.cap = (uint32_t)v;
         }
+        // pageable source: staged before the call returns
+        GEPI_CUDA(cudaMemcpyAsync(pl->d_pend, &hdr, sizeof hdr, cudaMemcpyHostToDevice, pl->stream));
+        ctx.pend = pl->d_pend;
     }
 
     const double tests_per_tile = 20.0 * TA * TB;
@@ -886,7 +891,7 @@ cudaError_t launch_count(const CountVariant &v, const gepi_planes *pl, const int
                          int ntiles, int a0, int a1, int b0, int b1, const ScanCtx &ctx,
                          uint32_t *dump, int *err, cudaStream_t stream) {
     if (ctx.pend) {
-        cudaError_t e = cudaMemsetAsync(&ctx.st->pend, 0, sizeof(uint32_t), stream);
+        cudaError_t e = cudaMemsetAsync(&ctx.pend->n, 0, sizeof(uint32_t), stream);
         if (e != cudaSuccess) return e;
     }
     cudaError_t e =

@@ -23,7 +23,9 @@
 // Limits: the inputs, planes and tables must fit the array next to the
 // candidate buffers (two buffers of kNoAllocCap = 65,536 records), and
 // k <= kNoAllocCap / 4; larger requests return GEPI_ERR_LIMIT before any
-// device work.
+// device work.  A Fisher scan also takes a pending list of tests for exact
+// evaluation from the scratch left over (up to kNoAllocPendCap entries),
+// and evaluates them in the counting launch when none is left.
 //
 // Device address: the host-side symbol g_noalloc_scratch is only a stand-in
 // and must never be passed to a kernel.  Every call, with the caller's device
@@ -59,6 +61,7 @@ cudaError_t launch_popc_tiles(int ta, int kc, const uint32_t *planes, int Wp, in
                               const int2 *tiles, int ntiles, int a0, int a1, int b0, int b1,
                               const ScanCtx &ctx, uint32_t *dump, cudaStream_t stream);
 int fisher_fp64_walks();
+cudaError_t launch_fisher_pending(const ScanCtx &ctx, int num_sms, cudaStream_t stream);
 cudaError_t run_select_compact(Cand *in, Cand *out, ScanState *st, void *sel, uint32_t cap,
                                uint32_t k, int n_override, uint32_t n_compact, int objective,
                                float lp_margin, int num_sms, cudaStream_t stream);
@@ -70,6 +73,9 @@ constexpr int kNoAllocStageWords = 32;
 
 constexpr size_t kNoAllocScratchBytes = 32ull << 20;
 constexpr uint32_t kNoAllocCap = 65536;
+// Fisher pending list: at most this many entries, from scratch the request
+// leaves free (a request never needs it to fit)
+constexpr uint32_t kNoAllocPendCap = 1u << 18;
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
@@ -300,6 +306,17 @@ extern "C" gepi_status gepi_process_gpu_1_noalloc(const uint64_t *bits, const ui
                              " bytes of scratch and k <= " + std::to_string(kNoAllocCap / 4) +
                              "; the fixed scratch array holds " +
                              std::to_string(kNoAllocScratchBytes) + " bytes");
+    // Fisher: tests that pass the bounds are evaluated by a launch across the
+    // GPU after each counting launch, from a pending list in the free scratch
+    // (entries hold 16-bit counts); without room they run in the counting launch
+    uint32_t pend_cap = 0;
+    size_t o_pend = 0;
+    if (par->objective == GEPI_FISHER && S0 < 65536 && S1 < 65536 &&
+        cv.used + 256 + 4096 * sizeof(uint4) <= kNoAllocScratchBytes) {
+        pend_cap = (uint32_t)std::min<size_t>(
+            kNoAllocPendCap, (kNoAllocScratchBytes - cv.used - 256) / sizeof(uint4));
+        o_pend = cv.take(256 + (size_t)pend_cap * sizeof(uint4));
+    }
 
     int prev = -1;
     cudaGetDevice(&prev);
@@ -368,6 +385,13 @@ extern "C" gepi_status gepi_process_gpu_1_noalloc(const uint64_t *bits, const ui
     ctx.pend_req = 0;
     ctx.cap = kNoAllocCap;
     ctx.st = d_state;
+    if (pend_cap) {
+        PendList hdr{};
+        hdr.ent = reinterpret_cast<uint4 *>(base + o_pend + 256);
+        hdr.cap = pend_cap;
+        GEPI_CUDA(cudaMemcpy(base + o_pend, &hdr, sizeof hdr, cudaMemcpyHostToDevice));
+        ctx.pend = reinterpret_cast<PendList *>(base + o_pend);
+    }
     const float lp_margin = 2e-6f * (float)std::lgamma((double)nmax + 1.0) + 1e-3f;
 
     // Adaptive batches over the tile list, as in the allocating scan.
@@ -381,9 +405,11 @@ extern "C" gepi_status gepi_process_gpu_1_noalloc(const uint64_t *bits, const ui
     while (t < (size_t)ntiles) {
         const size_t nbt = std::min(batch, (size_t)ntiles - t);
         ctx.cand = d_cand[cur];
+        if (ctx.pend) GEPI_CUDA(cudaMemsetAsync(&ctx.pend->n, 0, sizeof(uint32_t), stream));
         GEPI_CUDA(launch_popc_tiles(kNoAllocTile, kNoAllocStageWords, d_planes, Wp, W0, d_tiles + t,
                                     (int)nbt, 0, n_snps, 0, n_snps,
                                     ctx, nullptr, stream));
+        if (ctx.pend) GEPI_CUDA(launch_fisher_pending(ctx, num_sms, stream));
         GEPI_CUDA(cudaMemcpy(&st, d_state, sizeof st, cudaMemcpyDeviceToHost));
         if (st.overflow) {
             if (++retries > 64)

@@ -22,16 +22,24 @@
 
 namespace gepi {
 
+// Shared memory of decode_bed_kernel: the staged rows (+ up to 15 bytes of
+// alignment offset), then the 33 x 32 permutation entries of 32 output words.
+__host__ __device__ inline size_t decode_rows_bytes(int spc, size_t bps) {
+    return ((size_t)spc * bps + 16 + 15) & ~size_t(15);
+}
+constexpr size_t kDecodePermBytes = 33 * 32 * 4;
+
 // One CTA decodes `spc` consecutive SNPs whose .bed rows are staged in shared
 // memory.  The rows are contiguous in the file, so the staging is one copy of
 // spc * bps bytes: 16-byte loads, four in flight per thread (byte loads kept a
 // warp at 32 bytes in flight, about 250 GB/s over the GPU), into a shared
 // buffer offset to match the source's alignment (the payload follows a 3-byte
 // header), with byte loads for the unaligned head and tail.
-// Each warp produces 32 consecutive output words of one SNP at a time:
-// iteration j ballots the three plane bits of word w0 + j, lane L carrying slot
-// 4*(L%8) + L/8 of that word (bit L); lane j keeps word j, then the warp stores
-// 32 words per plane, coalesced.
+// Then, 32 output words at a time, the CTA stages those words' sample
+// permutation in shared memory (32 x 32 entries, row pitch 33 so that the
+// lanes' reads fall in distinct banks), and each warp produces the 32 words of
+// one SNP: lane L builds word w0 + L of the three planes from its 32 slots,
+// slot k at bit 8 (k % 4) + k / 4, and the warp stores them coalesced.
 __global__ void decode_bed_kernel(const uint8_t *__restrict__ bed, size_t bps, int n_snps,
                                   const int32_t *__restrict__ perm, int Wp, int spc,
                                   uint32_t *__restrict__ planes) {
@@ -61,36 +69,38 @@ __global__ void decode_bed_kernel(const uint8_t *__restrict__ bed, size_t bps, i
         for (; i < nvec; i += bd) vd[i] = __ldg(vs + i);
     }
     for (size_t i = head + nvec * 16 + threadIdx.x; i < tot; i += bd) srow[i] = __ldg(src + i);
-    __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    const int slot = 4 * (lane & 7) + (lane >> 3);  // slot whose bit is `lane`
+    int32_t *sperm = reinterpret_cast<int32_t *>(sbuf + decode_rows_bytes(spc, bps));
     const int nchunks = (Wp + 31) / 32;
-    for (int job = warp; job < nchunks * ns; job += nwarp) {
-        const int si = job / nchunks, ch = job - si * nchunks;
+    for (int ch = 0; ch < nchunks; ++ch) {
         const int w0 = ch * 32;
-        const uint8_t *row = srow + (size_t)si * bps;
-        uint32_t myA = 0, mya = 0, myV = 0;
-        for (int j = 0; j < 32; ++j) {
-            const int w = w0 + j;
-            if (w >= Wp) break;  // uniform across the warp
-            const int sample = __ldg(perm + (size_t)w * 32 + slot);
-            int code = 1;
-            if (sample >= 0) code = (row[sample >> 2] >> ((sample & 3) * 2)) & 3;
-            const uint32_t A = __ballot_sync(0xffffffffu, code == 0 || code == 2);
-            const uint32_t a = __ballot_sync(0xffffffffu, code >= 2);
-            const uint32_t V = __ballot_sync(0xffffffffu, code != 1);
-            if (lane == j) {
-                myA = A;
-                mya = a;
-                myV = V;
-            }
+        __syncthreads();  // the rows are staged; the previous chunk's readers are done
+        for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) {
+            const int w = w0 + (i >> 5);
+            sperm[(i >> 5) * 33 + (i & 31)] = w < Wp ? __ldg(perm + (size_t)w0 * 32 + i) : -1;
         }
+        __syncthreads();
+        const int32_t *myperm = sperm + lane * 33;
         const int w = w0 + lane;
-        if (w < Wp) {
-            uint32_t *out = planes + (size_t)(s0 + si) * 3 * Wp + w;
-            out[0] = myA;
-            out[(size_t)Wp] = mya;
-            out[2 * (size_t)Wp] = myV;
+        for (int si = warp; si < ns; si += nwarp) {
+            const uint8_t *row = srow + (size_t)si * bps;
+            uint32_t A = 0, a = 0, V = 0;
+#pragma unroll 8
+            for (int k = 0; k < 32; ++k) {
+                const int sample = myperm[k];
+                int code = 1;  // pad slot: missing
+                if (sample >= 0) code = (row[sample >> 2] >> ((sample & 3) * 2)) & 3;
+                const uint32_t bit = 1u << (8 * (k & 3) + (k >> 2));
+                A |= (code & 1) == 0 ? bit : 0u;  // 00, 10
+                a |= code >= 2 ? bit : 0u;        // 10, 11
+                V |= code != 1 ? bit : 0u;        // not 01
+            }
+            if (w < Wp) {
+                uint32_t *out = planes + (size_t)(s0 + si) * 3 * Wp + w;
+                out[0] = A;
+                out[(size_t)Wp] = a;
+                out[2 * (size_t)Wp] = V;
+            }
         }
     }
 }
@@ -153,7 +163,7 @@ cudaError_t launch_decode_bed(const uint8_t *bed_payload, size_t bps, int n_snps
     int spc = (int)(budget / (bps ? bps : 1));
     if (spc < 1) spc = 1;
     if (spc > 32) spc = 32;
-    size_t smem = (size_t)spc * bps + 16;  // + the alignment offset
+    size_t smem = decode_rows_bytes(spc, bps) + kDecodePermBytes;
     if (smem > 200 * 1024) return cudaErrorInvalidValue;  // > ~800k samples: not supported
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(decode_bed_kernel,

@@ -29,3 +29,23 @@ def test_reference_arm_prints_one_contract_line():
     assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
     assert d["config"]["workload"].startswith("cfg1")
+
+
+def _reference_line(*args):
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                        *args], capture_output=True, text=True, timeout=120, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.strip().startswith("{")]
+    assert len(lines) == 1, r.stdout
+    return json.loads(lines[0])
+
+
+def test_reference_arm_unavailable_where_the_reference_has_no_counterpart():
+    """The reference's CPU gold loop ranks by entropy and scans one cohort per
+    process: the Fisher, cohort and serving arms print one `unavailable` line
+    and exit 0 without running anything."""
+    for args in (("--config", "cfg2", "--objective", "fisher"), ("--config", "cohorts64"),
+                 ("--config", "serving")):
+        d = _reference_line(*args)
+        assert d["impl"] == "reference" and d["unavailable"], args
+        assert set(d) == {"impl", "unavailable"}, args

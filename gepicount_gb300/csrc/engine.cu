@@ -172,7 +172,7 @@ class Engine {
 
    private:
     gepi_status ensure_slots(int need);
-    gepi_status ensure_pending();
+    cudaError_t ensure_pending();
     // setup = true: only the kernels' shared-memory opt-ins and occupancy
     // queries (outside any capture)
     cudaError_t enqueue_step(unsigned mask, bool setup = false);
@@ -308,27 +308,30 @@ gepi_status Engine::ensure_slots(int need) {
 }
 
 // The Fisher pending list of the steps.  The step graphs bake in its address,
-// so those captured before it existed (without its launches) are dropped.
-gepi_status Engine::ensure_pending() {
-    if (d_pend_buf_) return GEPI_OK;
+// so those captured before it existed (without its launches) are dropped.  A
+// failure is not an error of the call: without the list the counting kernels
+// evaluate the tests themselves.
+cudaError_t Engine::ensure_pending() {
+    if (d_pend_buf_) return cudaSuccess;
     const size_t tags = 256, ents = tags + (size_t)kEnginePendCap * 4;
     unsigned char *b = nullptr;
-    GEPI_CUDA(cudaMalloc(&b, ents + (size_t)kEnginePendCap * sizeof(uint4)));
+    cudaError_t e = cudaMalloc(&b, ents + (size_t)kEnginePendCap * sizeof(uint4));
+    if (e != cudaSuccess) return e;
     PendList hdr{};
     hdr.ent = reinterpret_cast<uint4 *>(b + ents);
     hdr.tag = reinterpret_cast<uint32_t *>(b + tags);
     hdr.cap = kEnginePendCap;
-    cudaError_t e = cudaMemcpy(b, &hdr, sizeof hdr, cudaMemcpyHostToDevice);
+    e = cudaMemcpy(b, &hdr, sizeof hdr, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaStreamSynchronize(stream_);
     if (e != cudaSuccess) {
         cudaFree(b);
-        return set_error(GEPI_ERR_CUDA, std::string("engine pending list: ") + cudaGetErrorString(e));
+        return e;
     }
     for (auto &kv : graphs_) cudaGraphExecDestroy(kv.second);
     graphs_.clear();
     d_pend_buf_ = b;
     d_pend_ = reinterpret_cast<PendList *>(b);
-    return GEPI_OK;
+    return cudaSuccess;
 }
 
 // The device work of one step on the engine's stream: upload, the counting
@@ -680,9 +683,8 @@ void Engine::step(std::vector<Job *> &active) {
     }
     plan(run);
     for (Job *j : run) {
-        if (j->rq.objective == GEPI_FISHER && !d_pend_buf_ && ensure_pending() != GEPI_OK) {
-            // without the list the counting kernels evaluate the tests themselves
-            (void)cudaGetLastError();
+        if (j->rq.objective == GEPI_FISHER && !d_pend_buf_) {
+            if (ensure_pending() != cudaSuccess) (void)cudaGetLastError();
             break;
         }
     }

@@ -324,8 +324,12 @@ __device__ __forceinline__ double fisher_lpo(const double *__restrict__ lf, int 
 }
 
 // Two-sided Fisher exact test for the table (n11 n12 / n21 n22), natural-log
-// p-value, given K and lpo = ln P(obs) from fisher_lpo.  Terms with
-// P(x) <= P(obs) * (1 + 1e-7) are summed (R's rule).  The hypergeometric is
+// p-value, given K and lpo = ln P(obs) from fisher_lpo: the quantity the
+// reference's fisher_pval_d (src/kernels/fisher_d.cu:249-311) and host
+// fisher_pval (src/misc/fisher_p.c:52-76) compute, here in log space and in
+// FP64 throughout.  Terms with P(x) <= P(obs) * (1 + 1e-7) are summed (R's
+// rule; the reference compares log d(x) <= log d(obs) strictly, fisher_p.c:72,
+// so the two differ only on mathematically tied terms).  The hypergeometric is
 // log-concave, so the tail beyond xo (away from the mode) is walked with the
 // term ratio, a possible plateau between xo and the mode is walked term by
 // term, and the first qualifying term past the mode is found by bisection
